@@ -1,0 +1,148 @@
+/*
+ * sam_gpu.h -- C ABI of the GB300 implementation of SAM's pseudo-spectral RK3
+ * step (tslund/sam).  One process, one GPU, one context, no MPI.
+ *
+ * Every entry point replaces a Fortran subroutine of the reference and keeps
+ * its argument list and meaning (array base addresses, n_var, isymm), so a
+ * thin ISO_C_BINDING module lets sam.f call it unchanged.  Array extents come
+ * from the configuration given to sam_gpu_init, just as the reference takes
+ * them from its COMMON blocks (sam.h).  Arrays are HOST arrays in the
+ * reference's Fortran layouts with one rank (nxp = Nx_min, nzp = Nze = Nz);
+ * complex arrays are interleaved (re, im) doubles.  The same array may be
+ * passed for input and output wherever the reference does so.
+ *
+ * All functions return 0 on success or a negative SAM_GPU_E* code; nothing
+ * traps or aborts.  sam_gpu_error_string() describes the last failure.
+ */
+#ifndef SAM_GPU_H
+#define SAM_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SAM_GPU_OK 0
+#define SAM_GPU_EINVAL -1       /* bad argument or configuration */
+#define SAM_GPU_ENOTINIT -2     /* sam_gpu_init has not been called */
+#define SAM_GPU_EUNSUPPORTED -3 /* a branch the reference itself cannot run */
+#define SAM_GPU_ECUDA -4        /* CUDA runtime failure */
+#define SAM_GPU_ENONFINITE -5   /* vel_max met NaN/Inf in the physical field */
+
+/* The input.dat values the hot path reads (set_labels.f:29-102) and the
+ * derived values of init.f / initial_field.f.  Mirrors /static/, /strat/,
+ * /gravity_wave/ and the RK choice of /tstep/ (sam.h:14-62). */
+typedef struct sam_gpu_config {
+  int nx, ny, nz;     /* Nx, Ny, Nz; Nx even */
+  int n_dealias;      /* 0, 1 (2/3 rule), 2 (init.f:49-62) */
+  int i_strat;        /* 0: Lu=3, Lr=6;  1: Lu=4, Lr=9 (init.f:35-41) */
+  int i_cfl;          /* 1: dt from the CFL number (vel_max.f:187-192) */
+  int nrk_max;        /* 1, 2 or 3 (init.f:117-145) */
+  int rot_sav;        /* 1 for the tilted-box wave, i_prob = 4 (sam.f:176-185) */
+  int i_les;          /* Chollet-Lesieur spectra (spectra.f:21) */
+  int precision;      /* 64: FP64 drop-in; 32: FP32 bulk with FP64 reductions */
+  double xl, yl, zl;  /* box */
+  double vis, pr;     /* viscosity, Prandtl number */
+  double dt0, cfl0;
+  double buoy_fac_x, buoy_fac_z, lapse; /* initial_field.f:37-39,159-161,272-273 */
+  double cos_theta, sin_theta;          /* initial_field.f:252-254 */
+  double c_smag;                        /* sm.f:32 */
+} sam_gpu_config;
+
+/* /statistics/, /dynamic/ and the CFL numbers of /tstep/ (sam.h:58-77). */
+typedef struct sam_gpu_stats {
+  double time, dt;
+  double u_avg[4], u_var[4], u_max[4];
+  double energy, cfl_x, cfl_y, cfl_z;
+  int nonfinite;
+  int pad;
+} sam_gpu_stats;
+
+/* ---- setup (sam.f:48-62) ---- */
+/* After init and fft_init (sam.f:48-51): builds the device context, the FFT
+ * plans and twiddles, and allocates every device buffer the step needs. */
+int sam_gpu_init(const sam_gpu_config* cfg);
+int sam_gpu_finalize(void);
+/* out[11]: Nx_min Ny_min Nz_min Nze Lu Lr kx_max ky_max kz_max Lm Nx/2 */
+int sam_gpu_dims(int* out11);
+/* /tstep/ nrk and /dynamic/ time, dt as the caller holds them (sam.h:58-62) */
+int sam_gpu_set_tstep(int nrk, double dt, double time);
+int sam_gpu_get_stats(sam_gpu_stats* out);
+/* optional: launch on the caller's cudaStream_t (NULL = the library's own) */
+int sam_gpu_set_stream(void* cuda_stream);
+const char* sam_gpu_error_string(void);
+
+/* ---- per-routine drop-ins (host arrays, reference layouts) ---- */
+/* z_trans_b.f:1  u1(Nze,Ny_min,nxp,n_var) -> u2 blocks (Ny_min,nxp,Nze,n_var);
+ * isymm(n_var) must be 0 (the sine/cosine branches of the reference use
+ * undefined variables, z_trans_b.f:256,260). u_c, u_r, u_i are workspace and
+ * may be NULL. */
+int sam_gpu_z_trans_b(const double* u1, double* u2, int n_var, const int* isymm, double* u_c, double* u_r,
+                      double* u_i);
+/* x2z_decomp.f:1  u1 blocks (Ny_min,nxp,Nze,n_var) -> u2(Ny,Nx/2,nzp,n_var);
+ * columns kx >= Nx_min of u2 are left as they were; u3 may equal u2. */
+int sam_gpu_x2z_decomp(double* u1, double* u2, int n_var, double* u3);
+/* xy_trans_b.f:1  complex u1(Ny,Nx/2,nzp,n_var) -> real u2(Nx,Ny,nzp,n_var);
+ * u1 and u2 may be the same array. */
+int sam_gpu_xy_trans_b(double* u1, double* u2, int n_var, double* work);
+/* xy_trans_f.f:1  real u1(Nx,Ny,nzp,n_var) -> complex u2(nzp,Ny_min,Nx_min,n_var) */
+int sam_gpu_xy_trans_f(double* u1, double* u2, int n_var, double* work);
+/* z2x_decomp.f:1  with one rank the all-to-all is the identity on the
+ * (nzp,Ny_min,nxp,n_var) = (Nze,Ny_min,nxp,n_var) layout; u1 and u2 may be
+ * the same array, u3 is unused. */
+int sam_gpu_z2x_decomp(double* u1, double* u2, int n_var, double* u3);
+/* z_trans_f.f:1  in place on u(Nze,Ny_min,nxp,n_var): rows 1..Nz_min receive
+ * the truncated, 1/Nz-scaled modes; rows above Nz_min are unspecified, as in
+ * the reference. isymm(n_var) must be 0. */
+int sam_gpu_z_trans_f(double* u, int n_var, const int* isymm, double* u_r, double* u_i);
+/* vel_max.f:1  real u(Nx,Ny,nzp,Lu): updates the statistics, CFL numbers and
+ * (i_cfl = 1) dt; read them with sam_gpu_get_stats. */
+int sam_gpu_vel_max(const double* u, double* work);
+/* rhs.f:1  uu(Nx,Ny,nzp,Lr) holds the physical u in its first Lu slots (u
+ * and uu may be the same array); r(Nze,Ny_min,nxp,Lr+ipad) receives the
+ * projected rhs in fields 1..Lu and the pressure in field Lu+1;
+ * u_sav(Nz_min,Ny_min,nxp,3:4) is read when stratified; vel_max runs when
+ * the nrk last given to sam_gpu_set_tstep is 1. */
+int sam_gpu_rhs(double* u, double* uu, double* r, const double* u_sav, double* work);
+/* x_deriv.f:1 / y_deriv.f:1  spectral derivative of one real (Nx,Ny) plane */
+int sam_gpu_x_deriv(const double* u, double* du, double* work);
+int sam_gpu_y_deriv(const double* u, double* du, double* work);
+
+/* ---- resident fused path: state stays in HBM between steps ---- */
+/* after initial_field / read_field (sam.f:102-108): u(Nze,Ny_min,nxp,Lu) */
+int sam_gpu_upload(const double* u);
+/* r may be NULL; when given it receives (Nze,Ny_min,nxp,Lu+1): rhs + p */
+int sam_gpu_download(double* u, double* r);
+/* one RK stage of sam.f:169-314 on the resident state (no output branches) */
+int sam_gpu_stage(int nrk);
+/* nsteps steps of sam.f:122-318 (stages 1..nrk_max, then time += dt),
+ * replayed from a captured CUDA graph */
+int sam_gpu_step(int nsteps);
+
+/* Measurement hook (no counterpart in the reference, which has no timers):
+ * runs `reps` stages nrk on the resident state with CUDA events between the
+ * five passes and returns their mean durations in ms:
+ * ms5 = {z inverse, y inverse, x pass (+ vel_max), y forward, z forward+update}.
+ * The state advances as in sam_gpu_stage. */
+int sam_gpu_profile_stage(int nrk, int reps, float* ms5);
+/* Measurement hook: FP64 FMA throughput of this GPU (TFLOP/s), the ALU
+ * roofline of the FP64 drop-in.  No counterpart in the reference. */
+int sam_gpu_measure_fp64_peak(double* tflops);
+
+/* ---- diagnostics on the resident state ---- */
+/* spectra.f:1  out[5*Lm+3]: ek tk dk vt sample, energy_w, div_rms, div_max */
+int sam_gpu_spectra(double* out);
+/* div_check.f:1  out[4]: div_avg div_rms div_max n_div */
+int sam_gpu_div_check(double* out4);
+/* cl_energy.f:1 */
+int sam_gpu_cl_energy(double* e_cl);
+
+/* ---- initial fields on the device (written to the resident state) ---- */
+int sam_gpu_init_taylor_green(void);
+int sam_gpu_init_random(unsigned long long seed, int kind_u, double flct_u, int kind_t, double flct_t);
+int sam_gpu_init_packet(unsigned long long seed, int kx0, int ky0, int kz0, double sigma, double amplitude,
+                        double noise);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,242 @@
+// Batched mixed-radix FFT engine for sm_103a: lines of length n <= 1024 held
+// in shared memory, each line transformed by a team of TW threads (TW a power
+// of two, TW >= n/8; teams wider than a warp synchronise on a named barrier).
+// A stage of radix p (2, 3, 4, 5, 8) is a self-sorting Stockham step done in
+// place: every thread first loads all of its butterfly inputs (at most 8
+// complex values) into registers, the team synchronises, then the thread
+// computes and writes its outputs.  The plan is read from shared memory.
+//
+// Conventions are FFTPACK's (the reference's fft.f): unnormalised transforms,
+// SIGN = -1 is cfftf (exp(-i ...)), SIGN = +1 is cfftb (exp(+i ...)).
+// Twiddles w_{l p}^{f q} are tabulated per stage (forward sign) by the host in
+// extended precision and rounded once; the backward transform conjugates them.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace samgpu {
+
+template <typename T> struct Cx;
+template <> struct Cx<double> { using type = double2; };
+template <> struct Cx<float> { using type = float2; };
+template <typename T> using cx_t = typename Cx<T>::type;
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) { C r; r.x = a; r.y = b; return r; }
+
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+// a * w (SIGN=-1) or a * conj(w) (SIGN=+1)
+template <int SIGN, typename C> __device__ __forceinline__ C ctw(C a, C w) {
+  if (SIGN < 0) return mk<C>(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+  return mk<C>(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
+}
+// multiply by SIGN * i  (exp(SIGN i pi/2))
+template <int SIGN, typename C> __device__ __forceinline__ C cmul_si(C a) {
+  if (SIGN < 0) return mk<C>(a.y, -a.x);
+  return mk<C>(-a.y, a.x);
+}
+
+struct FftStage {
+  int p;       // radix
+  int l;       // length of the sub-transforms already combined
+  int m;       // n / (l p)
+  int tw_off;  // offset of this stage's l*(p-1) twiddles
+  uint32_t mmul;  // exact b / m == (b * mmul) >> 21 for b < 2^11
+};
+
+struct FftPlan {
+  int n;
+  int nst;
+  int tw_total;
+  int team;  // lanes per line
+  FftStage st[10];
+};
+
+__device__ __forceinline__ int div_m(int b, const FftStage& s) { return (int)(((uint32_t)b * s.mmul) >> 21); }
+
+// ---- radix-p DFT kernels on registers (in place on a[0..P-1])
+template <int SIGN, typename C> __device__ __forceinline__ void dft2(C* a) {
+  C t = a[1];
+  a[1] = csub(a[0], t);
+  a[0] = cadd(a[0], t);
+}
+
+template <int SIGN, typename C> __device__ __forceinline__ void dft4(C* a) {
+  C t0 = cadd(a[0], a[2]), t1 = csub(a[0], a[2]);
+  C t2 = cadd(a[1], a[3]), t3 = cmul_si<SIGN>(csub(a[1], a[3]));
+  a[0] = cadd(t0, t2);
+  a[2] = csub(t0, t2);
+  a[1] = cadd(t1, t3);
+  a[3] = csub(t1, t3);
+}
+
+template <int SIGN, typename C> __device__ __forceinline__ void dft8(C* a) {
+  using T = decltype(C::x);
+  const T h = (T)0.70710678118654752440084436210484903928;  // sqrt(2)/2
+  // first level: pairs (q, q+4)
+  C b0 = cadd(a[0], a[4]), b4 = csub(a[0], a[4]);
+  C b1 = cadd(a[1], a[5]), b5 = csub(a[1], a[5]);
+  C b2 = cadd(a[2], a[6]), b6 = csub(a[2], a[6]);
+  C b3 = cadd(a[3], a[7]), b7 = csub(a[3], a[7]);
+  // twiddles w8^{q} on the odd half: q=1 -> (1 + SIGN i) h, q=2 -> SIGN i, q=3 -> (-1 + SIGN i) h
+  b6 = cmul_si<SIGN>(b6);
+  {
+    C t = b5;  // (t.x - SIGN? ) : multiply by h (1 + SIGN i)
+    if (SIGN < 0) b5 = mk<C>((t.x + t.y) * h, (t.y - t.x) * h);
+    else b5 = mk<C>((t.x - t.y) * h, (t.y + t.x) * h);
+    t = b7;  // multiply by h (-1 + SIGN i)
+    if (SIGN < 0) b7 = mk<C>((-t.x + t.y) * h, (-t.y - t.x) * h);
+    else b7 = mk<C>((-t.x - t.y) * h, (-t.y + t.x) * h);
+  }
+  // two length-4 DFTs on (b0,b1,b2,b3) and (b4,b5,b6,b7)
+  C e[4] = {b0, b1, b2, b3};
+  C o[4] = {b4, b5, b6, b7};
+  dft4<SIGN>(e);
+  dft4<SIGN>(o);
+  // outputs: even-indexed from e, odd-indexed from o
+  a[0] = e[0]; a[2] = e[1]; a[4] = e[2]; a[6] = e[3];
+  a[1] = o[0]; a[3] = o[1]; a[5] = o[2]; a[7] = o[3];
+}
+
+template <int SIGN, typename C> __device__ __forceinline__ void dft3(C* a) {
+  using T = decltype(C::x);
+  const T c1 = (T)-0.5;
+  const T s1 = (T)SIGN * (T)0.86602540378443864676372317075293618347;  // SIGN*sin(2pi/3)
+  C t = cadd(a[1], a[2]);
+  C d = csub(a[1], a[2]);
+  C y0 = cadd(a[0], t);
+  C m = mk<C>(a[0].x + c1 * t.x, a[0].y + c1 * t.y);
+  // SIGN i s * d
+  C r = mk<C>(-s1 * d.y, s1 * d.x);
+  a[0] = y0;
+  a[1] = cadd(m, r);
+  a[2] = csub(m, r);
+}
+
+template <int SIGN, typename C> __device__ __forceinline__ void dft5(C* a) {
+  using T = decltype(C::x);
+  const T c1 = (T)0.30901699437494742410229341718281905886;   // cos(2pi/5)
+  const T c2 = (T)-0.80901699437494742410229341718281905886;  // cos(4pi/5)
+  const T s1 = (T)SIGN * (T)0.95105651629515357211643933337938214340;  // sin(2pi/5)
+  const T s2 = (T)SIGN * (T)0.58778525229247312916870595463907276860;  // sin(4pi/5)
+  C t1 = cadd(a[1], a[4]), d1 = csub(a[1], a[4]);
+  C t2 = cadd(a[2], a[3]), d2 = csub(a[2], a[3]);
+  C y0 = cadd(a[0], cadd(t1, t2));
+  C m1 = mk<C>(a[0].x + c1 * t1.x + c2 * t2.x, a[0].y + c1 * t1.y + c2 * t2.y);
+  C m2 = mk<C>(a[0].x + c2 * t1.x + c1 * t2.x, a[0].y + c2 * t1.y + c1 * t2.y);
+  // i*(s1 d1 + s2 d2) and i*(s2 d1 - s1 d2)
+  C n1 = mk<C>(-(s1 * d1.y + s2 * d2.y), s1 * d1.x + s2 * d2.x);
+  C n2 = mk<C>(-(s2 * d1.y - s1 * d2.y), s2 * d1.x - s1 * d2.x);
+  a[0] = y0;
+  a[1] = cadd(m1, n1);
+  a[4] = csub(m1, n1);
+  a[2] = cadd(m2, n2);
+  a[3] = csub(m2, n2);
+}
+
+template <int P, int SIGN, typename C> __device__ __forceinline__ void dftp(C* a) {
+  if (P == 2) dft2<SIGN>(a);
+  else if (P == 3) dft3<SIGN>(a);
+  else if (P == 4) dft4<SIGN>(a);
+  else if (P == 5) dft5<SIGN>(a);
+  else dft8<SIGN>(a);
+}
+
+// One Stockham stage of radix P on one line held in shared memory.
+// tl: lane index within the team, TW: team width.
+__device__ __forceinline__ void team_sync(int TW) {
+  if (TW <= 32) {
+    __syncwarp();
+  } else {
+    const int id = 1 + (int)(threadIdx.x / TW);
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(TW) : "memory");
+  }
+}
+
+template <int P, int SIGN, typename C>
+__device__ __forceinline__ void fft_stage(C* line, const C* __restrict__ tw, const FftStage& s, int n, int tl,
+                                          int TW) {
+  constexpr int MAXB = 8 / P;
+  const int nb = n / P;
+  C a[MAXB][P];
+  int fo[MAXB], ko[MAXB];
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    const int b = tl + i * TW;
+    fo[i] = 0; ko[i] = 0;
+    if (b < nb) {
+      const int f = div_m(b, s);
+      const int k = b - f * s.m;
+      fo[i] = f; ko[i] = k;
+      const C* src = line + f * s.m * P + k;
+      a[i][0] = src[0];
+      if (s.l == 1) {
+#pragma unroll
+        for (int q = 1; q < P; ++q) a[i][q] = src[s.m * q];
+      } else {
+        const C* w = tw + s.tw_off + f * (P - 1);
+#pragma unroll
+        for (int q = 1; q < P; ++q) a[i][q] = ctw<SIGN>(src[s.m * q], w[q - 1]);
+      }
+    }
+  }
+  team_sync(TW);
+#pragma unroll
+  for (int i = 0; i < MAXB; ++i) {
+    const int b = tl + i * TW;
+    if (b < nb) {
+      dftp<P, SIGN>(a[i]);
+      C* dst = line + fo[i] * s.m + ko[i];
+      const int os = s.l * s.m;
+#pragma unroll
+      for (int q = 0; q < P; ++q) dst[q * os] = a[i][q];
+    }
+  }
+  team_sync(TW);
+}
+
+// Full transform of one line (all threads of the team call this together;
+// a team with no line passes active=false and still synchronises).
+template <int SIGN, typename C>
+__device__ __forceinline__ void fft_line(C* line, const C* __restrict__ tw, const FftPlan& pl, int tl, bool active) {
+  const int n = pl.n;
+  const int TW = pl.team;
+  for (int s = 0; s < pl.nst; ++s) {
+    const FftStage& st = pl.st[s];
+    const int tla = active ? tl : (1 << 20);  // inactive lanes own no butterfly
+    switch (st.p) {
+      case 8: fft_stage<8, SIGN>(line, tw, st, n, tla, TW); break;
+      case 4: fft_stage<4, SIGN>(line, tw, st, n, tla, TW); break;
+      case 2: fft_stage<2, SIGN>(line, tw, st, n, tla, TW); break;
+      case 3: fft_stage<3, SIGN>(line, tw, st, n, tla, TW); break;
+      default: fft_stage<5, SIGN>(line, tw, st, n, tla, TW); break;
+    }
+  }
+}
+
+// Transform `nlines` lines of a CTA's shared-memory tile.  Line L starts at
+// base + L*ld.  Every thread of the CTA must call this with the same plan.
+template <int SIGN, typename C>
+__device__ __forceinline__ void fft_lines(C* base, int ld, int nlines, const C* __restrict__ tw, const FftPlan& pl) {
+  if (pl.n == 1) return;
+  const int TW = pl.team;
+  const int nteams = blockDim.x / TW;
+  const int team = threadIdx.x / TW;
+  const int tl = threadIdx.x - team * TW;
+  const int rounds = (nlines + nteams - 1) / nteams;
+  for (int r = 0; r < rounds; ++r) {
+    const int L = r * nteams + team;
+    const bool active = L < nlines;
+    fft_line<SIGN>(base + (active ? L : 0) * ld, tw, pl, tl, active);
+  }
+}
+
+// Copy a plan from global memory into shared memory (call before a barrier).
+__device__ __forceinline__ void load_plan(FftPlan* s_plan, const FftPlan* __restrict__ g_plan) {
+  const int nw = (int)(sizeof(FftPlan) / sizeof(int));
+  const int* src = reinterpret_cast<const int*>(g_plan);
+  int* dst = reinterpret_cast<int*>(s_plan);
+  for (int i = threadIdx.x; i < nw; i += blockDim.x) dst[i] = src[i];
+}
+
+}  // namespace samgpu

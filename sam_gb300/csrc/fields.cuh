@@ -1,0 +1,17 @@
+// Initial fields and precision conversion (fields.cu).
+#pragma once
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace samgpu {
+void fields_zero(double2* u, long long n, cudaStream_t s);
+void fields_init_tg(double2* u, const Grid& g, cudaStream_t s);
+void fields_init_random(double2* u, const Grid& g, uint64_t seed, int kind_u, double flct_u, int kind_t, double flct_t,
+                        cudaStream_t s);
+void fields_init_packet(double2* u, const Grid& g, uint64_t seed, int kx0, int ky0, int kz0, double sigma,
+                        double amplitude, double noise, double xl, double yl, double zl, double buoy_fac_z,
+                        double lapse, cudaStream_t s);
+template <typename T> void convert_in(const double2* src, cx_t<T>* dst, long long n, cudaStream_t s);
+template <typename T> void convert_out(const cx_t<T>* src, double2* dst, long long n, cudaStream_t s);
+}  // namespace samgpu

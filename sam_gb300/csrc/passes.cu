@@ -1,0 +1,633 @@
+// The five HBM passes of one RK3 stage and the reference-layout variants of
+// each transform.  Every pass moves a tile of pencils from HBM into shared
+// memory, transforms it there (fft_engine.cuh) and writes it back transposed
+// for the next pass, so the reference's MPI slab transposes (x2z_decomp.f,
+// z2x_decomp.f) become the store patterns of these kernels.
+//
+//   z_inv  : z_trans_b.f:224-250     wave (kx,ky,kz)  -> (z, kx, ky)
+//   y_inv  : xy_trans_b.f:74-98      (z, kx, ky)      -> (z, y, kx)
+//   x_pass : xy_trans_b.f:99-120 + rhs.f:26-61 + xy_trans_f.f:26-37
+//            (z, y, kx) -> physical line -> vel_max partials, products ->
+//            (m, z, kx, y)
+//   y_fwd  : xy_trans_f.f:39-54      (m, z, kx, y)    -> (m, kx, ky, z)
+//   z_fwd  : z_trans_f.f:144-157 + rhs.f:108-142 + sam.f:210-221,293-314
+//            (m, kx, ky, z) -> projected rhs, RK3 update of u
+#include <cuda_runtime.h>
+#include <math.h>
+
+#include "common.cuh"
+#include "passes.cuh"
+
+namespace samgpu {
+
+template <typename T>
+__device__ __forceinline__ void load_twiddles(cx_t<T>* s_tw, const cx_t<T>* __restrict__ g_tw, int n) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s_tw[i] = g_tw[i];
+}
+
+// --------------------------------------------------------------- z inverse
+// Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
+// modes; output A(n, z, kx, ky) with ky fastest.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ FftPlan pl;
+  load_plan(&pl, gpl);
+  __syncthreads();
+  C* s_tw = reinterpret_cast<C*>(smem_raw);
+  C* s_ln = s_tw + pl.tw_total;
+  const int nz = a.g.nz, mz = a.g.mz, km = a.g.kz, my = a.g.my;
+  const int ld = a.ld;
+  const int nty = (my + a.ty - 1) / a.ty;
+  int b = blockIdx.x;
+  const int jt = b % nty; b /= nty;
+  const int i = b % a.g.mx; b /= a.g.mx;
+  const int n = b;
+  const int j0 = jt * a.ty;
+  const int nl = min(a.ty, my - j0);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  const C* src = a.in + (long long)n * a.in_n + (long long)i * a.in_kx + (long long)j0 * a.in_ky;
+  for (int e = threadIdx.x; e < nl * nz; e += blockDim.x) {
+    const int t = e / nz, p = e - t * nz;
+    C v = mk<C>((T)0, (T)0);
+    if (p <= km) v = src[(long long)t * a.in_ky + p];
+    else if (p >= nz - km) v = src[(long long)t * a.in_ky + p - (nz - mz)];
+    s_ln[t * ld + p] = v;
+  }
+  __syncthreads();
+  fft_lines<+1>(s_ln, ld, nl, s_tw, pl);
+  __syncthreads();
+  C* dst = a.out + (long long)n * a.out_n + (long long)i * a.out_kx + j0;
+  for (int e = threadIdx.x; e < nl * nz; e += blockDim.x) {
+    const int z = e / nl, t = e - z * nl;
+    dst[(long long)z * a.out_z + t] = s_ln[t * ld + z];
+  }
+}
+
+// --------------------------------------------------------------- y inverse
+// Tile: field n, plane z, kx columns i0 .. i0+TX-1.  Input rows (one per kx)
+// hold either Ny_min compact modes (zero band inserted here, as
+// x2z_decomp.f:111-124 does) or Ny values with the band already present.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ FftPlan pl;
+  load_plan(&pl, gpl);
+  __syncthreads();
+  C* s_tw = reinterpret_cast<C*>(smem_raw);
+  C* s_ln = s_tw + pl.tw_total;
+  const int ny = a.g.ny, my = a.g.my, km = a.g.ky, mx = a.g.mx;
+  const int ld = a.ld;
+  const int ntx = (mx + a.tx - 1) / a.tx;
+  int b = blockIdx.x;
+  const int it = b % ntx; b /= ntx;
+  const int z = b % a.g.nz; b /= a.g.nz;
+  const int n = b;
+  const int i0 = it * a.tx;
+  const int nl = min(a.tx, mx - i0);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  const C* src = a.in + (long long)n * a.in_n + (long long)z * a.in_z + (long long)i0 * a.in_kx;
+  for (int e = threadIdx.x; e < nl * ny; e += blockDim.x) {
+    const int t = e / ny, p = e - t * ny;
+    C v;
+    if (a.in_full) {
+      v = src[(long long)t * a.in_kx + p];
+    } else {
+      v = mk<C>((T)0, (T)0);
+      if (p <= km) v = src[(long long)t * a.in_kx + p];
+      else if (p >= ny - km) v = src[(long long)t * a.in_kx + p - (ny - my)];
+    }
+    s_ln[t * ld + p] = v;
+  }
+  __syncthreads();
+  fft_lines<+1>(s_ln, ld, nl, s_tw, pl);
+  __syncthreads();
+  C* dst = a.out + (long long)n * a.out_n + (long long)z * a.out_z + i0;
+  for (int e = threadIdx.x; e < nl * ny; e += blockDim.x) {
+    const int y = e / nl, t = e - y * nl;
+    dst[(long long)y * a.out_y + t] = s_ln[t * ld + y];
+  }
+}
+
+// ------------------------------------------------------------------ x pass
+// Tile: plane z, rows y0 .. y0+Y-1 (Y even).  Two real x-lines (rows y0+2c
+// and y0+2c+1 of the same field) share one complex line: x + i y.
+__device__ __forceinline__ void product_pair(int m, int& a, int& b) {
+  // rhs.f:49-57 column order of the upper triangle: uu uv vv uw vw ww ut vt wt
+  // (m = 0..5 is the triangle of the velocity, 6..8 pair u,v,w with T)
+  if (m < 6) {
+    b = m < 1 ? 0 : (m < 3 ? 1 : 2);
+    a = m - (b * (b + 1)) / 2;
+  } else {
+    b = 3;
+    a = m - 6;
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ FftPlan pl;
+  load_plan(&pl, gpl);
+  __syncthreads();
+  C* s_tw = reinterpret_cast<C*>(smem_raw);
+  C* s_in = s_tw + pl.tw_total;                  // nin * yp lines
+  const int nx = a.g.nx, ny = a.g.ny, kmx = a.g.kx, mx = a.g.mx;
+  const int Y = a.yt, yp = Y / 2, ld = a.ld;
+  const int nin = a.nin;
+  C* s_pr = s_in + nin * yp * ld;                // group * yp product lines
+  double* s_red = reinterpret_cast<double*>(s_pr + a.group * yp * ld);  // reduction scratch
+  const int nyt = (ny + Y - 1) / Y;
+  const int yt = blockIdx.x % nyt;
+  const int z = blockIdx.x / nyt;
+  const int y0 = yt * Y;
+  const int yv = min(Y, ny - y0);  // valid rows in the tile
+  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+
+  // ---- build the input lines
+  if (a.in_mode == 0) {
+    // spectral rows of B(n, z, y, kx): Hermitian half spectra with kx <= kx_max
+    const int nband = nx - 2 * kmx - 1;
+    for (int e = threadIdx.x; e < nin * yp * nband; e += blockDim.x) {
+      const int L = e / nband, p = e - L * nband;
+      s_in[L * ld + kmx + 1 + p] = mk<C>((T)0, (T)0);
+    }
+    for (int e = threadIdx.x; e < nin * yp * mx; e += blockDim.x) {
+      const int L = e / mx, kx = e - L * mx;
+      const int f = L / yp, c = L - f * yp;
+      const int ya = y0 + 2 * c, yb = ya + 1;
+      const C* src = a.in + (long long)f * a.in_n + (long long)z * a.in_z;
+      C X = mk<C>((T)0, (T)0), Yv = mk<C>((T)0, (T)0);
+      if (ya < ny) X = src[(long long)ya * a.in_y + kx];
+      if (yb < ny) Yv = src[(long long)yb * a.in_y + kx];
+      if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
+        X.y = (T)0;
+        Yv.y = (T)0;
+      }
+      s_in[L * ld + kx] = mk<C>(X.x - Yv.y, X.y + Yv.x);
+      if (kx > 0) s_in[L * ld + nx - kx] = mk<C>(X.x + Yv.y, Yv.x - X.y);
+    }
+    __syncthreads();
+    fft_lines<+1>(s_in, ld, nin * yp, s_tw, pl);
+  } else {
+    // physical rows of P(n, z, y, x)
+    for (int e = threadIdx.x; e < nin * yp * nx; e += blockDim.x) {
+      const int L = e / nx, x = e - L * nx;
+      const int f = L / yp, c = L - f * yp;
+      const int ya = y0 + 2 * c, yb = ya + 1;
+      const T* src = a.in_phys + (long long)f * a.in_n + (long long)z * a.in_z;
+      T va = (T)0, vb = (T)0;
+      if (ya < ny) va = src[(long long)ya * a.in_y + x];
+      if (yb < ny) vb = src[(long long)yb * a.in_y + x];
+      s_in[L * ld + x] = mk<C>(va, vb);
+    }
+  }
+  __syncthreads();
+
+  // ---- vel_max partial sums (vel_max.f:158-168), FP64, deterministic order
+  if (a.partials) {
+    for (int f = 0; f < a.g.lu; ++f) {
+      double s1 = 0.0, s2 = 0.0, mxv = 0.0;
+      int bad = 0;
+      for (int e = threadIdx.x; e < yp * nx; e += blockDim.x) {
+        const int c = e / nx, x = e - c * nx;
+        const C v = s_in[(f * yp + c) * ld + x];
+        if (y0 + 2 * c < ny) {
+          const double d = (double)v.x;
+          s1 += d; s2 += d * d; mxv = fmax(mxv, fabs(d));
+          bad |= !isfinite(d);
+        }
+        if (y0 + 2 * c + 1 < ny) {
+          const double d = (double)v.y;
+          s1 += d; s2 += d * d; mxv = fmax(mxv, fabs(d));
+          bad |= !isfinite(d);
+        }
+      }
+      // warp reduce then CTA reduce
+      for (int o = 16; o > 0; o >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        mxv = fmax(mxv, __shfl_xor_sync(0xffffffffu, mxv, o));
+        bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+      }
+      const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+      if ((threadIdx.x & 31) == 0) {
+        s_red[w * 4 + 0] = s1; s_red[w * 4 + 1] = s2; s_red[w * 4 + 2] = mxv; s_red[w * 4 + 3] = (double)bad;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double t1 = 0, t2 = 0, tm = 0, tb = 0;
+        for (int k = 0; k < nw; ++k) {
+          t1 += s_red[k * 4 + 0]; t2 += s_red[k * 4 + 1];
+          tm = fmax(tm, s_red[k * 4 + 2]); tb += s_red[k * 4 + 3];
+        }
+        double* dst = a.partials + ((long long)blockIdx.x * a.g.lu + f) * 4;
+        dst[0] = t1; dst[1] = t2; dst[2] = tm; dst[3] = tb;
+      }
+      __syncthreads();
+    }
+  }
+
+  // ---- outputs
+  if (a.out_mode == 3) return;  // statistics only (vel_max.f)
+  if (a.out_mode == 0) {
+    // physical rows (xy_trans_b.f:117-119)
+    for (int e = threadIdx.x; e < nin * Y * nx; e += blockDim.x) {
+      const int x = e % nx, r = e / nx;
+      const int yy = r % Y, f = r / Y;
+      if (yy < yv) {
+        const C v = s_in[(f * yp + (yy >> 1)) * ld + x];
+        a.out_phys[(long long)f * a.out_pn + (long long)z * a.out_pz + (long long)(y0 + yy) * a.out_py + x] =
+            (yy & 1) ? v.y : v.x;
+      }
+    }
+    return;
+  }
+  const T fn = (T)(0.5 / ((double)nx * (double)ny));  // 1/(Nx Ny) (xy_trans_f.f:20) and the 1/2 of the split
+  const int nout = a.out_mode == 1 ? nin : a.g.lr;
+  // out_mode 1 transforms the input lines in place, all at once; out_mode 2
+  // forms the products `group` fields at a time (group >= 1 by construction)
+  const int gstep = a.out_mode == 1 ? nin : max(a.group, 1);
+  for (int m0 = 0; m0 < nout; m0 += gstep) {
+    const int gm = min(gstep, nout - m0);
+    C* lines;
+    if (a.out_mode == 1) {
+      lines = s_in + m0 * yp * ld;
+    } else {
+      // rhs.f:46-60 products of the physical lines
+      for (int e = threadIdx.x; e < gm * yp * nx; e += blockDim.x) {
+        const int L = e / nx, x = e - L * nx;
+        const int gi = L / yp, c = L - gi * yp;
+        int fa, fb;
+        product_pair(m0 + gi, fa, fb);
+        const C va = s_in[(fa * yp + c) * ld + x];
+        const C vb = s_in[(fb * yp + c) * ld + x];
+        s_pr[L * ld + x] = mk<C>(va.x * vb.x, va.y * vb.y);
+      }
+      lines = s_pr;
+      __syncthreads();
+    }
+    fft_lines<-1>(lines, ld, gm * yp, s_tw, pl);
+    __syncthreads();
+    // split the two real transforms, keep kx <= kx_max, scale, store C(m, z, kx, y)
+    for (int e = threadIdx.x; e < gm * mx * Y; e += blockDim.x) {
+      const int yy = e % Y, r = e / Y;
+      const int kx = r % mx, gi = r / mx;
+      if (yy < yv) {
+        const C* ln = lines + (gi * yp + (yy >> 1)) * ld;
+        const C z1 = ln[kx];
+        const C z2 = ln[kx == 0 ? 0 : nx - kx];
+        C v;
+        if ((yy & 1) == 0) v = mk<C>((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
+        else v = mk<C>((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
+        a.out[(long long)(m0 + gi) * a.out_n + (long long)z * a.out_z + (long long)kx * a.out_kx + y0 + yy] = v;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// --------------------------------------------------------------- y forward
+// Tile: field m, kx column i, planes z0 .. z0+TZ-1.  Output D(m, kx, ky, z)
+// keeps |ky| <= ky_max (xy_trans_f.f:45-52).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ FftPlan pl;
+  load_plan(&pl, gpl);
+  __syncthreads();
+  C* s_tw = reinterpret_cast<C*>(smem_raw);
+  C* s_ln = s_tw + pl.tw_total;
+  const int ny = a.g.ny, my = a.g.my, km = a.g.ky, nz = a.g.nz;
+  const int ld = a.ld;
+  const int ntz = (nz + a.tz - 1) / a.tz;
+  int b = blockIdx.x;
+  const int zt = b % ntz; b /= ntz;
+  const int i = b % a.g.mx; b /= a.g.mx;
+  const int m = b;
+  const int z0 = zt * a.tz;
+  const int nl = min(a.tz, nz - z0);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  const C* src = a.in + (long long)m * a.in_n + (long long)i * a.in_kx + (long long)z0 * a.in_z;
+  for (int e = threadIdx.x; e < nl * ny; e += blockDim.x) {
+    const int t = e / ny, p = e - t * ny;
+    s_ln[t * ld + p] = src[(long long)t * a.in_z + p];
+  }
+  __syncthreads();
+  fft_lines<-1>(s_ln, ld, nl, s_tw, pl);
+  __syncthreads();
+  C* dst = a.out + (long long)m * a.out_n + (long long)i * a.out_kx + z0;
+  for (int e = threadIdx.x; e < nl * my; e += blockDim.x) {
+    const int j = e / nl, t = e - j * nl;
+    dst[(long long)j * a.out_ky + t] = s_ln[t * ld + kpos(j, km, my, ny)];
+  }
+}
+
+// --------------------------------------------------------------- z forward
+// Tile: kx column i, ky rows j0 .. j0+TY-1, all nf fields.  Forward z
+// transform, truncation to Nz_min and 1/Nz (z_trans_f.f:150-156), then one of
+//   mode 0: write the truncated modes back in place (z_trans_f),
+//   mode 1: rhs epilogue (rhs.f:108-142) into r with u_sav from memory,
+//   mode 2: full stage epilogue: rhs, then sam.f:210-221 and 293-314.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+  using C = cx_t<T>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ FftPlan pl;
+  load_plan(&pl, gpl);
+  __syncthreads();
+  C* s_tw = reinterpret_cast<C*>(smem_raw);
+  C* s_ln = s_tw + pl.tw_total;
+  const Grid& g = a.g;
+  const int nz = g.nz, mz = g.mz, km = g.kz, my = g.my;
+  const int ld = a.ld, nf = a.nf;
+  const int nty = (my + a.ty - 1) / a.ty;
+  const int jt = blockIdx.x % nty;
+  const int i = blockIdx.x / nty;
+  const int j0 = jt * a.ty;
+  const int nl = min(a.ty, my - j0);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  for (int e = threadIdx.x; e < nf * nl * nz; e += blockDim.x) {
+    const int p = e % nz, r = e / nz;
+    const int t = r % nl, f = r / nl;
+    s_ln[(f * nl + t) * ld + p] =
+        a.in[(long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky + p];
+  }
+  __syncthreads();
+  fft_lines<-1>(s_ln, ld, nf * nl, s_tw, pl);
+  __syncthreads();
+  const T nz_inv = (T)(1.0 / (double)nz);
+  if (a.mode == 0) {
+    for (int e = threadIdx.x; e < nf * nl * mz; e += blockDim.x) {
+      const int k = e % mz, r = e / mz;
+      const int t = r % nl, f = r / nl;
+      C v = s_ln[(f * nl + t) * ld + kpos(k, km, mz, nz)];
+      v.x *= nz_inv;
+      v.y *= nz_inv;
+      a.in[(long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky + k] = v;
+    }
+    return;
+  }
+  const StageConsts& sc = a.sc;
+  const double rkx = g.wave_x * (double)i;
+  const double rkx2 = rkx * rkx;
+  double dt = 0.0, dt_fac1 = 0.0, dt_fac2 = 0.0, vis_f = 0.0;
+  if (a.mode == 2) {
+    dt = a.state->dt;
+    dt_fac1 = sc.gamma * dt;
+    dt_fac2 = sc.zeta * dt;
+    vis_f = sc.vis * (dt_fac1 + dt_fac2);
+  }
+  for (int e = threadIdx.x; e < nl * mz; e += blockDim.x) {
+    const int k = e % mz, t = e / mz;
+    const int j = j0 + t;
+    const double rky = g.wave_y * (double)kwave(j, g.ky, my);
+    const double rk_sq2 = rkx2 + rky * rky;
+    const double rkz = g.wave_z * (double)kwave(k, km, mz);
+    const double rk_sq_raw = rk_sq2 + rkz * rkz;
+    const double rk_sq = fmax(rk_sq_raw, 1.0e-10);
+    const int pos = kpos(k, km, mz, nz);
+    double tr[9], ti[9];
+#pragma unroll
+    for (int f = 0; f < 9; ++f) {
+      if (f < nf) {
+        const C v = s_ln[(f * nl + t) * ld + pos];
+        tr[f] = (double)v.x * (double)nz_inv;
+        ti[f] = (double)v.y * (double)nz_inv;
+      } else {
+        tr[f] = 0.0; ti[f] = 0.0;
+      }
+    }
+    // -i (a + i b) = b - i a
+    double s1r = rkx * tr[0] + rky * tr[1] + rkz * tr[3], s1i = rkx * ti[0] + rky * ti[1] + rkz * ti[3];
+    double s2r = rkx * tr[1] + rky * tr[2] + rkz * tr[4], s2i = rkx * ti[1] + rky * ti[2] + rkz * ti[4];
+    double s3r = rkx * tr[3] + rky * tr[4] + rkz * tr[5], s3i = rkx * ti[3] + rky * ti[4] + rkz * ti[5];
+    double r1r = s1i, r1i = -s1r, r2r = s2i, r2i = -s2r, r3r = s3i, r3i = -s3r, r4r = 0.0, r4i = 0.0;
+    double u_r[4] = {0, 0, 0, 0}, u_i[4] = {0, 0, 0, 0};
+    const long long uidx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
+    if (a.mode == 2) {
+#pragma unroll
+      for (int f = 0; f < 4; ++f)
+        if (f < g.lu) {
+          const C v = a.u[(long long)f * a.u_n + uidx];
+          u_r[f] = (double)v.x;
+          u_i[f] = (double)v.y;
+        }
+    }
+    if (sc.i_strat) {
+      double wr, wi, thr, thi;
+      if (a.mode == 2) {
+        wr = u_r[2]; wi = u_i[2];
+        if (sc.rot_sav) {  // sam.f:180-181
+          wr = sc.cos_theta * u_r[2] - sc.sin_theta * u_r[0];
+          wi = sc.cos_theta * u_i[2] - sc.sin_theta * u_i[0];
+        }
+        thr = u_r[3]; thi = u_i[3];
+      } else {
+        const long long sidx = (long long)i * a.sav_kx + (long long)j * a.sav_ky + k;
+        const C w = a.usav[sidx];
+        const C th = a.usav[a.sav_n + sidx];
+        wr = (double)w.x; wi = (double)w.y; thr = (double)th.x; thi = (double)th.y;
+      }
+      r1r += sc.buoy_fac_x * thr; r1i += sc.buoy_fac_x * thi;
+      r3r += sc.buoy_fac_z * thr; r3i += sc.buoy_fac_z * thi;
+      const double s4r = rkx * tr[6] + rky * tr[7] + rkz * tr[8];
+      const double s4i = rkx * ti[6] + rky * ti[7] + rkz * ti[8];
+      r4r = s4i - sc.lapse * wr;
+      r4i = -s4r - sc.lapse * wi;
+    }
+    // p = -i (k . R) / k^2 ;  R -= i k p   (rhs.f:134-139)
+    const double qr = rkx * r1r + rky * r2r + rkz * r3r, qi = rkx * r1i + rky * r2i + rkz * r3i;
+    const double pr = qi / rk_sq, pim = -qr / rk_sq;
+    // -i rk p = rk * (p.i, -p.r)
+    r1r += rkx * pim; r1i -= rkx * pr;
+    r2r += rky * pim; r2i -= rky * pr;
+    r3r += rkz * pim; r3i -= rkz * pr;
+    const double rr[4] = {r1r, r2r, r3r, r4r}, ri[4] = {r1i, r2i, r3i, r4i};
+    if (a.mode == 1) {
+      const long long ridx = (long long)i * a.r_kx + (long long)j * a.r_ky + k;
+#pragma unroll
+      for (int f = 0; f < 4; ++f)
+        if (f < g.lu) a.r[(long long)f * a.r_n + ridx] = mk<C>((T)rr[f], (T)ri[f]);
+      a.r[(long long)g.lu * a.r_n + ridx] = mk<C>((T)pr, (T)pim);
+    } else {
+      const long long ridx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
+      const double ef = exp(-vis_f * rk_sq_raw);
+      const double et = sc.pr_inv == 1.0 ? ef : exp(-(vis_f * sc.pr_inv) * rk_sq_raw);
+#pragma unroll
+      for (int f = 0; f < 4; ++f)
+        if (f < g.lu) {
+          double ur = u_r[f], ui = u_i[f];
+          if (sc.nrk > 1) {  // sam.f:211-221
+            const C ro = a.r[(long long)f * a.u_n + ridx];
+            ur = ur + dt_fac2 * (double)ro.x;
+            ui = ui + dt_fac2 * (double)ro.y;
+          }
+          const double vf = f == 3 ? et : ef;  // sam.f:297
+          ur = (ur + dt_fac1 * rr[f]) * vf;
+          ui = (ui + dt_fac1 * ri[f]) * vf;
+          a.u[(long long)f * a.u_n + uidx] = mk<C>((T)ur, (T)ui);
+          a.r[(long long)f * a.u_n + ridx] = mk<C>((T)rr[f], (T)ri[f]);
+        }
+      if (sc.write_p) a.p[ridx] = mk<C>((T)pr, (T)pim);
+    }
+  }
+  if (a.mode == 2 && sc.last && blockIdx.x == 0 && threadIdx.x == 0) {
+    // sam.f:318 time = time + dt, once per step (no CTA of this launch reads
+    // time, and none writes dt)
+    a.state->time = a.state->time + dt;
+  }
+}
+
+// ----------------------------------------------------- vel_max completion
+// vel_max.f:170-196 on the per-CTA partials written by k_x_pass.
+__global__ void k_vel_max_finish(const double* __restrict__ partials, int nblk, Grid g, DevState* st, int i_cfl,
+                                 double cfl0, double adv_cfl_limit) {
+  __shared__ double red[kThreads];
+  __shared__ double fin[4][4];
+  for (int f = 0; f < g.lu; ++f) {
+    for (int q = 0; q < 4; ++q) {
+      double v = 0.0;
+      for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+        const double x = partials[((long long)b * g.lu + f) * 4 + q];
+        v = (q == 2) ? fmax(v, x) : v + x;
+      }
+      red[threadIdx.x] = v;
+      __syncthreads();
+      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] = (q == 2) ? fmax(red[threadIdx.x], red[threadIdx.x + s])
+                                                         : red[threadIdx.x] + red[threadIdx.x + s];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) fin[f][q] = red[0];
+      __syncthreads();
+    }
+  }
+  if (threadIdx.x == 0) {
+    const double inv = 1.0 / ((double)g.nx * (double)g.ny * (double)g.nz);
+    int bad = 0;
+    for (int f = 0; f < g.lu; ++f) {
+      st->u_avg[f] = fin[f][0] * inv;
+      st->u_var[f] = fin[f][1] * inv - st->u_avg[f] * st->u_avg[f];
+      st->u_max[f] = fin[f][2];
+      bad |= fin[f][3] != 0.0;
+    }
+    st->energy = 0.5 * (st->u_var[0] + st->u_var[1] + st->u_var[2]);
+    const double cx = st->u_max[0] * g.kx * g.wave_x;
+    const double cy = st->u_max[1] * g.ky * g.wave_y;
+    const double cz = st->u_max[2] * g.kz * g.wave_z;
+    if (i_cfl == 1) {
+      const double cb = fmax(cx, fmax(cy, cz));
+      if (cb > 0.0 && !bad) st->dt = cfl0 * adv_cfl_limit / cb;
+    }
+    st->cfl_x = cx * st->dt;
+    st->cfl_y = cy * st->dt;
+    st->cfl_z = cz * st->dt;
+    if (bad) st->nonfinite = 1;
+  }
+}
+
+// ------------------------------------------------------ x2z layout kernel
+// x2z_decomp.f:59-152 with one rank: (Ny_min, Nx_min, Nze, n) blocks to
+// (Ny, Nx/2, Nz, n) planes with the truncated ky band zeroed.
+__global__ void k_x2z(const double2* __restrict__ in, double2* __restrict__ out, Grid g, int nvar, int nx2) {
+  const long long total = (long long)g.ny * g.mx * g.nz * nvar;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(e % g.ny);
+    long long r = e / g.ny;
+    const int i = (int)(r % g.mx);
+    r /= g.mx;
+    const int k = (int)(r % g.nz);
+    const int n = (int)(r / g.nz);
+    double2 v = make_double2(0.0, 0.0);
+    int j = -1;
+    if (y <= g.ky) j = y;
+    else if (y >= g.ny - g.ky) j = y - (g.ny - g.my);
+    if (j >= 0) v = in[(((long long)n * g.nze + k) * g.mx + i) * g.my + j];
+    out[(((long long)n * g.nz + k) * nx2 + i) * g.ny + y] = v;
+  }
+}
+
+// ------------------------------------------------------------ instantiation
+template <typename T>
+void launch_z_inv(const ZInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  const int nty = (a.g.my + a.ty - 1) / a.ty;
+  const int grid = a.nvar * a.g.mx * nty;
+  k_z_inv<T><<<grid, kThreads, smem, s>>>(a, pl);
+}
+template <typename T>
+void launch_y_inv(const YInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  const int ntx = (a.g.mx + a.tx - 1) / a.tx;
+  const int grid = a.nvar * a.g.nz * ntx;
+  k_y_inv<T><<<grid, kThreads, smem, s>>>(a, pl);
+}
+template <typename T>
+int x_pass_blocks(const XPassArgs<T>& a) {
+  return a.g.nz * ((a.g.ny + a.yt - 1) / a.yt);
+}
+template <typename T>
+void launch_x_pass(const XPassArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  k_x_pass<T><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
+}
+template <typename T>
+void launch_y_fwd(const YFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  const int ntz = (a.g.nz + a.tz - 1) / a.tz;
+  const int grid = a.nvar * a.g.mx * ntz;
+  k_y_fwd<T><<<grid, kThreads, smem, s>>>(a, pl);
+}
+template <typename T>
+void launch_z_fwd(const ZFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  const int nty = (a.g.my + a.ty - 1) / a.ty;
+  const int grid = a.g.mx * nty;
+  k_z_fwd<T><<<grid, kThreads, smem, s>>>(a, pl);
+}
+void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
+                           double adv_cfl_limit, cudaStream_t s) {
+  k_vel_max_finish<<<1, kThreads, 0, s>>>(partials, nblk, g, st, i_cfl, cfl0, adv_cfl_limit);
+}
+void launch_x2z(const double2* in, double2* out, const Grid& g, int nvar, int nx2, cudaStream_t s) {
+  long long total = (long long)g.ny * g.mx * g.nz * nvar;
+  int grid = (int)((total + kThreads - 1) / kThreads);
+  if (grid > 152 * 16) grid = 152 * 16;
+  if (grid < 1) grid = 1;
+  k_x2z<<<grid, kThreads, 0, s>>>(in, out, g, nvar, nx2);
+}
+
+static void allow_dynamic_smem(const void* fn, int optin) {
+  cudaFuncAttributes at;
+  if (cudaFuncGetAttributes(&at, fn) != cudaSuccess) return;
+  cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)at.sharedSizeBytes);
+}
+
+// Opt every pass into the largest dynamic shared memory the device allows
+// (the per-block opt-in limit less the kernel's static shared memory).
+template <typename T>
+void set_smem_limits() {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  allow_dynamic_smem((const void*)k_z_inv<T>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T>, optin);
+}
+
+#define SAMGPU_INST(T)                                                                           \
+  template void launch_z_inv<T>(const ZInvArgs<T>&, const FftPlan*, size_t, cudaStream_t);     \
+  template void launch_y_inv<T>(const YInvArgs<T>&, const FftPlan*, size_t, cudaStream_t);     \
+  template void launch_x_pass<T>(const XPassArgs<T>&, const FftPlan*, size_t, cudaStream_t);   \
+  template int x_pass_blocks<T>(const XPassArgs<T>&);                                          \
+  template void launch_y_fwd<T>(const YFwdArgs<T>&, const FftPlan*, size_t, cudaStream_t);     \
+  template void launch_z_fwd<T>(const ZFwdArgs<T>&, const FftPlan*, size_t, cudaStream_t);     \
+  template void set_smem_limits<T>();
+
+SAMGPU_INST(double)
+SAMGPU_INST(float)
+
+}  // namespace samgpu

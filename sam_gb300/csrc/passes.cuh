@@ -1,0 +1,87 @@
+// Argument blocks and launchers of the transform passes (passes.cu).
+// Strides are in complex (or real, for physical arrays) elements.
+#pragma once
+#include "common.cuh"
+
+namespace samgpu {
+
+template <typename T>
+struct ZInvArgs {
+  Grid g;
+  const cx_t<T>* in;   // rows of Nz_min modes
+  cx_t<T>* out;        // A(n, z, kx, ky)
+  const cx_t<T>* tw;   // twiddles of the Nz plan
+  int nvar, ty, ld;
+  long long in_ky, in_kx, in_n;
+  long long out_kx, out_z, out_n;
+};
+
+template <typename T>
+struct YInvArgs {
+  Grid g;
+  const cx_t<T>* in;  // rows (one per kx) of Ny_min modes or Ny values
+  cx_t<T>* out;       // B(n, z, y, kx)
+  const cx_t<T>* tw;
+  int nvar, tx, ld, in_full;
+  long long in_kx, in_z, in_n;
+  long long out_y, out_z, out_n;
+};
+
+template <typename T>
+struct XPassArgs {
+  Grid g;
+  const cx_t<T>* in;   // in_mode 0: B(n, z, y, kx)
+  const T* in_phys;    // in_mode 1: P(n, z, y, x)
+  cx_t<T>* out;        // out_mode 1/2: C(m, z, kx, y)
+  T* out_phys;         // out_mode 0: P(n, z, y, x)
+  double* partials;    // vel_max partials (nblocks, lu, 4) or null
+  const cx_t<T>* tw;
+  int in_mode, out_mode, nin, yt, group, ld;
+  long long in_y, in_z, in_n;
+  long long out_kx, out_z, out_n;
+  long long out_py, out_pz, out_pn;
+};
+
+template <typename T>
+struct YFwdArgs {
+  Grid g;
+  const cx_t<T>* in;  // C(m, z, kx, y)
+  cx_t<T>* out;       // D(m, kx, ky, z)
+  const cx_t<T>* tw;
+  int nvar, tz, ld;
+  long long in_kx, in_z, in_n;
+  long long out_ky, out_kx, out_n;
+};
+
+template <typename T>
+struct ZFwdArgs {
+  Grid g;
+  cx_t<T>* in;  // D(m, kx, ky, z); mode 0 writes the result back here
+  const cx_t<T>* tw;
+  int mode, nf, ty, ld;
+  long long in_ky, in_kx, in_n;
+  // mode 1 (rhs): r out and u_sav in
+  cx_t<T>* r;
+  long long r_ky, r_kx, r_n;
+  const cx_t<T>* usav;
+  long long sav_ky, sav_kx, sav_n;
+  // mode 2 (stage): u, r (same layout), p, device state
+  cx_t<T>* u;
+  cx_t<T>* p;
+  long long u_ky, u_kx, u_n;
+  DevState* state;
+  StageConsts sc;
+};
+
+template <typename T> void launch_z_inv(const ZInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
+template <typename T> void launch_y_inv(const YInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
+template <typename T> void launch_x_pass(const XPassArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
+template <typename T> int x_pass_blocks(const XPassArgs<T>& a);
+template <typename T> void launch_y_fwd(const YFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
+template <typename T> void launch_z_fwd(const ZFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
+template <typename T> void set_smem_limits();
+void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
+                           double adv_cfl_limit, cudaStream_t s);
+void launch_x2z(const double2* in, double2* out, const Grid& g, int nvar, int nx2, cudaStream_t s);
+
+}  // namespace samgpu

@@ -1,0 +1,929 @@
+// Host side of the C ABI (include/sam_gpu.h): the device context that mirrors
+// the reference's COMMON blocks, the FFT plans, buffer management, the
+// per-routine drop-ins in the reference layouts, and the resident fused RK3
+// stage with its CUDA-graph replay.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/sam_gpu.h"
+#include "common.cuh"
+#include "diag.cuh"
+#include "fields.cuh"
+#include "passes.cuh"
+
+namespace samgpu {
+
+static char g_err[512] = "";
+
+static int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(SAM_GPU_ECUDA, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+// ---------------------------------------------------------------- FFT plans
+struct Plan {
+  FftPlan h{};
+  FftPlan* d = nullptr;
+  double2* tw64 = nullptr;
+  float2* tw32 = nullptr;
+};
+
+// Radices 8, 4, 2, 3, 5 in that order; twiddles w_{l p}^{f q} = exp(-2 pi i
+// f q / (l p)) in long double, rounded once to each working precision.
+static int build_plan(int n, Plan& P) {
+  FftPlan& pl = P.h;
+  memset(&pl, 0, sizeof(pl));
+  pl.n = n;
+  int r = n, ns = 0, fac[16];
+  while (r % 8 == 0) { fac[ns++] = 8; r /= 8; }
+  while (r % 4 == 0) { fac[ns++] = 4; r /= 4; }
+  while (r % 2 == 0) { fac[ns++] = 2; r /= 2; }
+  while (r % 3 == 0) { fac[ns++] = 3; r /= 3; }
+  while (r % 5 == 0) { fac[ns++] = 5; r /= 5; }
+  if (r != 1 || ns > 10 || n > 1024) return fail(SAM_GPU_EINVAL, "FFT length %d must be 2^a 3^b 5^c <= 1024", n);
+  pl.nst = ns;
+  int TW = 1;
+  while (TW * 8 < n) TW *= 2;
+  for (;;) {
+    bool ok = true;
+    for (int s = 0; s < ns; ++s) {
+      const int nb = n / fac[s];
+      if ((nb + TW - 1) / TW > 8 / fac[s]) ok = false;
+    }
+    if (ok) break;
+    TW *= 2;
+  }
+  if (TW > kThreads) return fail(SAM_GPU_EINVAL, "FFT length %d needs too wide a team", n);
+  pl.team = TW;
+  std::vector<double2> t64;
+  std::vector<float2> t32;
+  int l = 1, off = 0;
+  const long double two_pi = 6.283185307179586476925286766559005768L;
+  for (int s = 0; s < ns; ++s) {
+    const int p = fac[s];
+    FftStage& st = pl.st[s];
+    st.p = p;
+    st.l = l;
+    st.m = n / (l * p);
+    st.tw_off = off;
+    st.mmul = (uint32_t)(((1u << 21) + (uint32_t)st.m - 1) / (uint32_t)st.m);
+    for (int f = 0; f < l; ++f)
+      for (int q = 1; q < p; ++q) {
+        const long e = ((long)f * q) % ((long)l * p);
+        const long double a = two_pi * (long double)e / (long double)(l * p);
+        const long double c = cosl(a), sn = -sinl(a);
+        t64.push_back(make_double2((double)c, (double)sn));
+        t32.push_back(make_float2((float)c, (float)sn));
+      }
+    off += l * (p - 1);
+    l *= p;
+  }
+  pl.tw_total = off;
+  if (t64.empty()) { t64.push_back(make_double2(1, 0)); t32.push_back(make_float2(1, 0)); }
+  CK(cudaMalloc(&P.d, sizeof(FftPlan)));
+  CK(cudaMemcpy(P.d, &pl, sizeof(FftPlan), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&P.tw64, sizeof(double2) * t64.size()));
+  CK(cudaMemcpy(P.tw64, t64.data(), sizeof(double2) * t64.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&P.tw32, sizeof(float2) * t32.size()));
+  CK(cudaMemcpy(P.tw32, t32.data(), sizeof(float2) * t32.size(), cudaMemcpyHostToDevice));
+  return 0;
+}
+
+static void free_plan(Plan& P) {
+  cudaFree(P.d); cudaFree(P.tw64); cudaFree(P.tw32);
+  P.d = nullptr; P.tw64 = nullptr; P.tw32 = nullptr;
+}
+
+template <typename T> const cx_t<T>* tw_of(const Plan& P);
+template <> const double2* tw_of<double>(const Plan& P) { return P.tw64; }
+template <> const float2* tw_of<float>(const Plan& P) { return P.tw32; }
+
+// -------------------------------------------------------------- the context
+struct Scratch {
+  void* p = nullptr;
+  size_t n = 0;
+};
+
+struct Ctx {
+  sam_gpu_config cfg{};
+  Grid g{};
+  int nx2 = 0, lm = 0, k_cl = 0;
+  double gamma[4] = {0, 0, 0, 0}, zeta[4] = {0, 0, 0, 0}, adv_cfl_limit = 1.0;
+  int nrk = 1;
+  Plan px, py, pz;
+  cudaStream_t stream = nullptr, own = nullptr;
+  // resident state in the working precision: U, R (lu fields), P, and the
+  // pencil buffers S1 (A, then D), S2 (B), S3 (C)
+  void *U = nullptr, *R = nullptr, *P = nullptr, *S1 = nullptr, *S2 = nullptr, *S3 = nullptr;
+  double* partials = nullptr;
+  int partial_blocks = 0;
+  DevState* state = nullptr;
+  Scratch sc[4];
+  // tile choices
+  int ty_zi = 16, tx_yi = 16, yt_x = 8, grp_x = 9, tz_yf = 16, ty_zf = 4;
+  cudaGraphExec_t gexec = nullptr;
+  cudaStream_t graph_stream = nullptr;
+  int graph_stale = 1;
+};
+
+static Ctx* g_ctx = nullptr;
+
+static int ensure(Scratch& s, size_t bytes) {
+  if (s.n >= bytes) return 0;
+  if (s.p) cudaFree(s.p);
+  s.p = nullptr;
+  s.n = 0;
+  CK(cudaMalloc(&s.p, bytes));
+  s.n = bytes;
+  return 0;
+}
+
+static size_t csize(const Ctx& c) { return c.cfg.precision == 32 ? sizeof(float2) : sizeof(double2); }
+
+static int line_ld(int n) { return n + ((n % 2 == 0) ? 1 : 0); }
+
+// shared memory of a tile of `lines` lines of length n plus the twiddles
+static size_t tile_smem(const Plan& P, int lines, size_t es) {
+  return es * ((size_t)P.h.tw_total + (size_t)lines * line_ld(P.h.n)) + 16;
+}
+
+// dynamic shared memory budget of one CTA: the opt-in limit (227 KB on
+// GB300) less room for the kernels' static shared memory
+static size_t kSmemMax = 227 * 1024 - 2048;
+
+static int pick_tile(const Plan& P, int want, int lines_per_unit, size_t es, size_t extra = 0) {
+  int t = want;
+  while (t > 1 && tile_smem(P, t * lines_per_unit, es) + extra > kSmemMax) t /= 2;
+  return t;
+}
+
+// --------------------------------------------------------------- the passes
+template <typename T>
+static int run_z_inv(Ctx& c, const void* in, void* out, int nvar, long long in_ky, long long in_kx, long long in_n,
+                     long long out_kx, long long out_z, long long out_n) {
+  ZInvArgs<T> a{};
+  a.g = c.g;
+  a.in = (const cx_t<T>*)in;
+  a.out = (cx_t<T>*)out;
+  a.tw = tw_of<T>(c.pz);
+  a.nvar = nvar;
+  a.ty = pick_tile(c.pz, c.ty_zi, 1, sizeof(cx_t<T>));
+  a.ld = line_ld(c.g.nz);
+  a.in_ky = in_ky; a.in_kx = in_kx; a.in_n = in_n;
+  a.out_kx = out_kx; a.out_z = out_z; a.out_n = out_n;
+  launch_z_inv<T>(a, c.pz.d, tile_smem(c.pz, a.ty, sizeof(cx_t<T>)), c.stream);
+  return 0;
+}
+
+template <typename T>
+static int run_y_inv(Ctx& c, const void* in, void* out, int nvar, int in_full, long long in_kx, long long in_z,
+                     long long in_n, long long out_y, long long out_z, long long out_n) {
+  YInvArgs<T> a{};
+  a.g = c.g;
+  a.in = (const cx_t<T>*)in;
+  a.out = (cx_t<T>*)out;
+  a.tw = tw_of<T>(c.py);
+  a.nvar = nvar;
+  a.tx = pick_tile(c.py, c.tx_yi, 1, sizeof(cx_t<T>));
+  a.ld = line_ld(c.g.ny);
+  a.in_full = in_full;
+  a.in_kx = in_kx; a.in_z = in_z; a.in_n = in_n;
+  a.out_y = out_y; a.out_z = out_z; a.out_n = out_n;
+  launch_y_inv<T>(a, c.py.d, tile_smem(c.py, a.tx, sizeof(cx_t<T>)), c.stream);
+  return 0;
+}
+
+template <typename T>
+static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
+  const size_t es = sizeof(cx_t<T>);
+  const size_t red = sizeof(double) * 4 * (kThreads / 32) + 64;
+  yt = c.yt_x;
+  grp = out_mode == 2 ? c.grp_x : 0;
+  for (;;) {
+    const int lines = (nin + grp) * (yt / 2);
+    if (tile_smem(c.px, lines, es) + red <= kSmemMax) break;
+    if (grp > 1) { grp = (grp + 1) / 2; continue; }
+    if (yt > 2) { yt /= 2; continue; }
+    return fail(SAM_GPU_EINVAL, "x pass does not fit in shared memory (Nx=%d)", c.g.nx);
+  }
+  return 0;
+}
+
+template <typename T>
+static size_t x_smem(Ctx& c, int nin, int yt, int grp) {
+  return tile_smem(c.px, (nin + grp) * (yt / 2), sizeof(cx_t<T>)) + sizeof(double) * 4 * (kThreads / 32) + 64;
+}
+
+template <typename T>
+static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in, const void* in_phys,
+                      long long in_y, long long in_z, long long in_n, void* out, void* out_phys, long long out_kx,
+                      long long out_z, long long out_n, long long out_py, long long out_pz, long long out_pn,
+                      bool stats) {
+  XPassArgs<T> a{};
+  a.g = c.g;
+  a.in = (const cx_t<T>*)in;
+  a.in_phys = (const T*)in_phys;
+  a.out = (cx_t<T>*)out;
+  a.out_phys = (T*)out_phys;
+  a.tw = tw_of<T>(c.px);
+  a.in_mode = in_mode;
+  a.out_mode = out_mode;
+  a.nin = nin;
+  int rc = x_tile<T>(c, nin, out_mode, a.yt, a.group);
+  if (rc) return rc;
+  a.ld = line_ld(c.g.nx);
+  a.in_y = in_y; a.in_z = in_z; a.in_n = in_n;
+  a.out_kx = out_kx; a.out_z = out_z; a.out_n = out_n;
+  a.out_py = out_py; a.out_pz = out_pz; a.out_pn = out_pn;
+  a.partials = nullptr;
+  const int nblk = x_pass_blocks<T>(a);
+  if (stats) {
+    if (nblk > c.partial_blocks) {
+      cudaFree(c.partials);
+      c.partials = nullptr;
+      CK(cudaMalloc(&c.partials, sizeof(double) * 4 * 4 * (size_t)nblk));
+      c.partial_blocks = nblk;
+    }
+    a.partials = c.partials;
+  }
+  launch_x_pass<T>(a, c.px.d, x_smem<T>(c, nin, a.yt, a.group), c.stream);
+  if (stats)
+    launch_vel_max_finish(c.partials, nblk, c.g, c.state, c.cfg.i_cfl, c.cfg.cfl0, c.adv_cfl_limit, c.stream);
+  return 0;
+}
+
+template <typename T>
+static int run_y_fwd(Ctx& c, const void* in, void* out, int nvar, long long in_kx, long long in_z, long long in_n,
+                     long long out_ky, long long out_kx, long long out_n) {
+  YFwdArgs<T> a{};
+  a.g = c.g;
+  a.in = (const cx_t<T>*)in;
+  a.out = (cx_t<T>*)out;
+  a.tw = tw_of<T>(c.py);
+  a.nvar = nvar;
+  a.tz = pick_tile(c.py, c.tz_yf, 1, sizeof(cx_t<T>));
+  a.ld = line_ld(c.g.ny);
+  a.in_kx = in_kx; a.in_z = in_z; a.in_n = in_n;
+  a.out_ky = out_ky; a.out_kx = out_kx; a.out_n = out_n;
+  launch_y_fwd<T>(a, c.py.d, tile_smem(c.py, a.tz, sizeof(cx_t<T>)), c.stream);
+  return 0;
+}
+
+static StageConsts stage_consts(const Ctx& c, int nrk, int write_p) {
+  StageConsts s{};
+  s.nrk = nrk;
+  s.last = nrk == c.cfg.nrk_max;
+  s.i_strat = c.cfg.i_strat;
+  s.rot_sav = c.cfg.rot_sav;
+  s.i_cfl = c.cfg.i_cfl;
+  s.write_p = write_p;
+  s.gamma = c.gamma[nrk - 1];
+  s.zeta = c.zeta[nrk - 1];
+  s.vis = c.cfg.vis;
+  s.pr_inv = 1.0 / c.cfg.pr;
+  s.buoy_fac_x = c.cfg.buoy_fac_x;
+  s.buoy_fac_z = c.cfg.buoy_fac_z;
+  s.lapse = c.cfg.lapse;
+  s.cos_theta = c.cfg.cos_theta;
+  s.sin_theta = c.cfg.sin_theta;
+  s.cfl0 = c.cfg.cfl0;
+  s.adv_cfl_limit = c.adv_cfl_limit;
+  return s;
+}
+
+template <typename T>
+static int run_z_fwd(Ctx& c, ZFwdArgs<T>& a) {
+  a.g = c.g;
+  a.tw = tw_of<T>(c.pz);
+  a.ld = line_ld(c.g.nz);
+  a.ty = pick_tile(c.pz, c.ty_zf, a.nf, sizeof(cx_t<T>));
+  launch_z_fwd<T>(a, c.pz.d, tile_smem(c.pz, a.ty * a.nf, sizeof(cx_t<T>)), c.stream);
+  return 0;
+}
+
+// One fused RK stage on the resident state (sam.f:169-314).  When ev is
+// given, ev[p] is recorded before pass p and ev[5] after the last pass.
+template <typename T>
+static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr) {
+  const Grid& g = c.g;
+  const long long nzmm = (long long)g.mx * g.my * g.mz;
+  int rc;
+  if (ev) cudaEventRecord(ev[0], c.stream);
+  // z inverse: U(n, kx, ky, kz) -> A(n, z, kx, ky)
+  rc = run_z_inv<T>(c, c.U, c.S1, g.lu, g.mz, (long long)g.my * g.mz, nzmm, g.my, (long long)g.mx * g.my,
+                    (long long)g.nz * g.mx * g.my);
+  if (rc) return rc;
+  if (ev) cudaEventRecord(ev[1], c.stream);
+  // y inverse: A -> B(n, z, y, kx)
+  rc = run_y_inv<T>(c, c.S1, c.S2, g.lu, 0, g.my, (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, g.mx,
+                    (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx);
+  if (rc) return rc;
+  if (ev) cudaEventRecord(ev[2], c.stream);
+  // x pass: B -> C(m, z, kx, y) with vel_max at nrk = 1
+  rc = run_x_pass<T>(c, 0, 2, g.lu, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx, c.S3,
+                     nullptr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, 0, 0, 0, nrk == 1);
+  if (rc) return rc;
+  if (ev) cudaEventRecord(ev[3], c.stream);
+  // y forward: C -> D(m, kx, ky, z)
+  rc = run_y_fwd<T>(c, c.S3, c.S1, g.lr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, g.nz,
+                    (long long)g.my * g.nz, (long long)g.mx * g.my * g.nz);
+  if (rc) return rc;
+  if (ev) cudaEventRecord(ev[4], c.stream);
+  // z forward + rhs + RK update
+  ZFwdArgs<T> a{};
+  a.in = (cx_t<T>*)c.S1;
+  a.mode = 2;
+  a.nf = g.lr;
+  a.in_ky = g.nz; a.in_kx = (long long)g.my * g.nz; a.in_n = (long long)g.mx * g.my * g.nz;
+  a.u = (cx_t<T>*)c.U;
+  a.r = (cx_t<T>*)c.R;
+  a.p = (cx_t<T>*)c.P;
+  a.u_ky = g.mz; a.u_kx = (long long)g.my * g.mz; a.u_n = nzmm;
+  a.state = c.state;
+  a.sc = stage_consts(c, nrk, 1);
+  rc = run_z_fwd<T>(c, a);
+  if (ev) cudaEventRecord(ev[5], c.stream);
+  return rc;
+}
+
+static int stage_any(Ctx& c, int nrk, cudaEvent_t* ev = nullptr) {
+  return c.cfg.precision == 32 ? enqueue_stage<float>(c, nrk, ev) : enqueue_stage<double>(c, nrk, ev);
+}
+
+static int check_launch() {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(SAM_GPU_ECUDA, "kernel launch: %s", cudaGetErrorString(e));
+  return 0;
+}
+
+static int sync_stream(Ctx& c) {
+  CK(cudaStreamSynchronize(c.stream));
+  return check_launch();
+}
+
+static void free_ctx(Ctx* c) {
+  if (!c) return;
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  free_plan(c->px); free_plan(c->py); free_plan(c->pz);
+  cudaFree(c->U); cudaFree(c->R); cudaFree(c->P);
+  cudaFree(c->S1); cudaFree(c->S2); cudaFree(c->S3);
+  cudaFree(c->partials); cudaFree(c->state);
+  for (auto& s : c->sc) cudaFree(s.p);
+  if (c->own) cudaStreamDestroy(c->own);
+  delete c;
+}
+
+}  // namespace samgpu
+
+using namespace samgpu;
+
+#define NEED_CTX()                                                         \
+  if (!g_ctx) return fail(SAM_GPU_ENOTINIT, "sam_gpu_init has not been called"); \
+  Ctx& c = *g_ctx
+
+extern "C" {
+
+const char* sam_gpu_error_string(void) { return g_err; }
+
+int sam_gpu_init(const sam_gpu_config* cfg) {
+  if (!cfg) return fail(SAM_GPU_EINVAL, "null config");
+  if (g_ctx) { free_ctx(g_ctx); g_ctx = nullptr; }
+  if (cfg->nx < 2 || cfg->nx % 2 || cfg->ny < 1 || cfg->nz < 1)
+    return fail(SAM_GPU_EINVAL, "grid %d x %d x %d: Nx must be even and >= 2", cfg->nx, cfg->ny, cfg->nz);
+  if (cfg->precision != 64 && cfg->precision != 32) return fail(SAM_GPU_EINVAL, "precision must be 64 or 32");
+  if (cfg->nrk_max < 1 || cfg->nrk_max > 3) return fail(SAM_GPU_EINVAL, "nrk_max must be 1, 2 or 3");
+  Ctx* c = new Ctx();
+  c->cfg = *cfg;
+  Grid& g = c->g;
+  g.nx = cfg->nx; g.ny = cfg->ny; g.nz = cfg->nz; g.nze = cfg->nz;
+  // init.f:49-73
+  switch (cfg->n_dealias) {
+    case 0: g.kx = g.nx / 2 - 1; g.ky = g.ny / 2 - 1; g.kz = g.nz / 2 - 1; break;
+    case 2:
+      g.kx = g.nx / 2 - 1;
+      g.ky = (int)(((double)g.ny - 0.1) / 3.0);
+      g.kz = (int)(((double)g.nz - 0.1) / 3.0);
+      break;
+    default:
+      g.kx = (int)(((double)g.nx - 0.1) / 3.0);
+      g.ky = (int)(((double)g.ny - 0.1) / 3.0);
+      g.kz = (int)(((double)g.nz - 0.1) / 3.0);
+  }
+  if (g.ky < 0) g.ky = 0;
+  if (g.kz < 0) g.kz = 0;
+  g.mx = g.kx + 1; g.my = 2 * g.ky + 1; g.mz = 2 * g.kz + 1;
+  g.lu = cfg->i_strat ? 4 : 3;
+  g.lr = cfg->i_strat ? 9 : 6;
+  const double pi = 3.14159265358979323846;
+  g.wave_x = 2.0 * pi / cfg->xl;
+  g.wave_y = 2.0 * pi / cfg->yl;
+  g.wave_z = 2.0 * pi / cfg->zl;
+  c->nx2 = g.nx / 2;
+  const int ksq = g.kx * g.kx + g.ky * g.ky + g.kz * g.kz;
+  c->lm = (int)(sqrt((double)ksq) + 0.5) + 1;
+  c->k_cl = (int)(g.nx / 3.0);
+  // init.f:117-145
+  if (cfg->nrk_max == 1) {
+    c->gamma[0] = 1.0; c->adv_cfl_limit = 1.0;
+  } else if (cfg->nrk_max == 2) {
+    c->gamma[0] = 1.0; c->gamma[1] = 0.5; c->zeta[1] = -0.5; c->adv_cfl_limit = 1.0;
+  } else {
+    c->gamma[0] = 8.0 / 15.0; c->gamma[1] = 5.0 / 12.0; c->gamma[2] = 3.0 / 4.0;
+    c->zeta[1] = -17.0 / 60.0; c->zeta[2] = -5.0 / 12.0;
+    c->adv_cfl_limit = sqrt(3.0);
+  }
+  g_ctx = c;
+  int rc;
+  if ((rc = build_plan(g.nx, c->px)) || (rc = build_plan(g.ny, c->py)) || (rc = build_plan(g.nz, c->pz))) {
+    free_ctx(c); g_ctx = nullptr; return rc;
+  }
+  cudaError_t e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { free_ctx(c); g_ctx = nullptr; return fail(SAM_GPU_ECUDA, "stream: %s", cudaGetErrorString(e)); }
+  c->stream = c->own;
+  {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) == cudaSuccess && optin > 4096)
+      kSmemMax = (size_t)optin - 2048;
+  }
+  set_smem_limits<double>();
+  set_smem_limits<float>();
+  diag_set_smem_limits();
+  const size_t es = csize(*c);
+  const size_t nzmm = (size_t)g.mx * g.my * g.mz;
+  const size_t s1 = (size_t)g.lr * g.mx * g.my * g.nz;
+  const size_t s2 = (size_t)g.lu * g.nz * g.ny * g.mx;
+  const size_t s3 = (size_t)g.lr * g.nz * g.mx * g.ny;
+  bool ok = cudaMalloc(&c->U, es * g.lu * nzmm) == cudaSuccess && cudaMalloc(&c->R, es * g.lu * nzmm) == cudaSuccess &&
+            cudaMalloc(&c->P, es * nzmm) == cudaSuccess && cudaMalloc(&c->S1, es * s1) == cudaSuccess &&
+            cudaMalloc(&c->S2, es * s2) == cudaSuccess && cudaMalloc(&c->S3, es * s3) == cudaSuccess &&
+            cudaMalloc(&c->state, sizeof(DevState)) == cudaSuccess;
+  // vel_max partials for any x-pass tiling (at least one row per CTA), so no
+  // allocation ever happens inside a captured step
+  c->partial_blocks = g.nz * g.ny;
+  ok = ok && cudaMalloc(&c->partials, sizeof(double) * 4 * 4 * (size_t)c->partial_blocks) == cudaSuccess;
+  if (!ok) { free_ctx(c); g_ctx = nullptr; return fail(SAM_GPU_ECUDA, "device allocation failed"); }
+  cudaMemset(c->U, 0, es * g.lu * nzmm);
+  cudaMemset(c->R, 0, es * g.lu * nzmm);
+  cudaMemset(c->P, 0, es * nzmm);
+  DevState st{};
+  st.time = 0.0;
+  st.dt = cfg->dt0;
+  cudaMemcpy(c->state, &st, sizeof(st), cudaMemcpyHostToDevice);
+  e = cudaDeviceSynchronize();
+  if (e != cudaSuccess) { free_ctx(c); g_ctx = nullptr; return fail(SAM_GPU_ECUDA, "init: %s", cudaGetErrorString(e)); }
+  return 0;
+}
+
+int sam_gpu_finalize(void) {
+  if (g_ctx) { cudaStreamSynchronize(g_ctx->stream); free_ctx(g_ctx); g_ctx = nullptr; }
+  return 0;
+}
+
+int sam_gpu_dims(int* o) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  o[0] = g.mx; o[1] = g.my; o[2] = g.mz; o[3] = g.nze; o[4] = g.lu; o[5] = g.lr;
+  o[6] = g.kx; o[7] = g.ky; o[8] = g.kz; o[9] = c.lm; o[10] = c.nx2;
+  return 0;
+}
+
+int sam_gpu_set_stream(void* s) {
+  NEED_CTX();
+  c.stream = s ? (cudaStream_t)s : c.own;
+  return 0;
+}
+
+int sam_gpu_set_tstep(int nrk, double dt, double time) {
+  NEED_CTX();
+  if (nrk < 1 || nrk > c.cfg.nrk_max) return fail(SAM_GPU_EINVAL, "nrk %d out of range", nrk);
+  c.nrk = nrk;
+  DevState st;
+  CK(cudaMemcpyAsync(&st, c.state, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  st.dt = dt;
+  st.time = time;
+  CK(cudaMemcpyAsync(c.state, &st, sizeof(st), cudaMemcpyHostToDevice, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_get_stats(sam_gpu_stats* out) {
+  NEED_CTX();
+  DevState st;
+  CK(cudaMemcpyAsync(&st, c.state, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  out->time = st.time;
+  out->dt = st.dt;
+  for (int n = 0; n < 4; ++n) { out->u_avg[n] = st.u_avg[n]; out->u_var[n] = st.u_var[n]; out->u_max[n] = st.u_max[n]; }
+  out->energy = st.energy;
+  out->cfl_x = st.cfl_x; out->cfl_y = st.cfl_y; out->cfl_z = st.cfl_z;
+  out->nonfinite = st.nonfinite;
+  return 0;
+}
+
+// ------------------------------------------------------ per-routine drop-ins
+
+static bool symm_ok(const int* isymm, int n_var) {
+  if (!isymm) return true;
+  for (int n = 0; n < n_var; ++n)
+    if (isymm[n] != 0) return false;
+  return true;
+}
+
+int sam_gpu_z_trans_b(const double* u1, double* u2, int n_var, const int* isymm, double*, double*, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (n_var < 1 || !u1 || !u2) return fail(SAM_GPU_EINVAL, "z_trans_b: bad arguments");
+  if (!symm_ok(isymm, n_var)) return fail(SAM_GPU_EUNSUPPORTED, "z_trans_b: only the periodic branch (isymm=0) exists");
+  const size_t nin = (size_t)g.nze * g.my * g.mx * n_var, nout = (size_t)g.my * g.mx * g.nze * n_var;
+  int rc;
+  if ((rc = ensure(c.sc[0], nin * 16)) || (rc = ensure(c.sc[1], nout * 16))) return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u1, nin * 16, cudaMemcpyHostToDevice, c.stream));
+  rc = run_z_inv<double>(c, c.sc[0].p, c.sc[1].p, n_var, g.nze, (long long)g.my * g.nze,
+                         (long long)g.mx * g.my * g.nze, g.my, (long long)g.mx * g.my, (long long)g.nze * g.mx * g.my);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(u2, c.sc[1].p, nout * 16, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_x2z_decomp(double* u1, double* u2, int n_var, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (n_var < 1 || !u1 || !u2) return fail(SAM_GPU_EINVAL, "x2z_decomp: bad arguments");
+  const size_t nin = (size_t)g.my * g.mx * g.nze * n_var;
+  const size_t nout = (size_t)g.ny * c.nx2 * g.nz * n_var;
+  int rc;
+  if ((rc = ensure(c.sc[0], nin * 16)) || (rc = ensure(c.sc[1], nout * 16))) return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u1, nin * 16, cudaMemcpyHostToDevice, c.stream));
+  launch_x2z((const double2*)c.sc[0].p, (double2*)c.sc[1].p, g, n_var, c.nx2, c.stream);
+  // only the columns kx < Nx_min of each (z, var) plane are written back
+  CK(cudaMemcpy2DAsync(u2, (size_t)g.ny * c.nx2 * 16, c.sc[1].p, (size_t)g.ny * c.nx2 * 16, (size_t)g.ny * g.mx * 16,
+                       (size_t)g.nz * n_var, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_xy_trans_b(double* u1, double* u2, int n_var, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (n_var < 1 || !u1 || !u2) return fail(SAM_GPU_EINVAL, "xy_trans_b: bad arguments");
+  const size_t nin = (size_t)g.ny * c.nx2 * g.nz * n_var;  // complex
+  const size_t nb = (size_t)n_var * g.nz * g.ny * g.mx;    // complex
+  const size_t nout = (size_t)g.nx * g.ny * g.nz * n_var;  // real
+  int rc;
+  if ((rc = ensure(c.sc[0], nin * 16)) || (rc = ensure(c.sc[1], nb * 16)) || (rc = ensure(c.sc[2], nout * 8)))
+    return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u1, nin * 16, cudaMemcpyHostToDevice, c.stream));
+  rc = run_y_inv<double>(c, c.sc[0].p, c.sc[1].p, n_var, 1, g.ny, (long long)g.ny * c.nx2,
+                         (long long)g.ny * c.nx2 * g.nz, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx);
+  if (rc) return rc;
+  rc = run_x_pass<double>(c, 0, 0, n_var, c.sc[1].p, nullptr, g.mx, (long long)g.ny * g.mx,
+                          (long long)g.nz * g.ny * g.mx, nullptr, c.sc[2].p, 0, 0, 0, g.nx, (long long)g.nx * g.ny,
+                          (long long)g.nx * g.ny * g.nz, false);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(u2, c.sc[2].p, nout * 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_xy_trans_f(double* u1, double* u2, int n_var, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (n_var < 1 || !u1 || !u2) return fail(SAM_GPU_EINVAL, "xy_trans_f: bad arguments");
+  const size_t nin = (size_t)g.nx * g.ny * g.nz * n_var;   // real
+  const size_t nc = (size_t)n_var * g.nz * g.mx * g.ny;    // complex
+  const size_t nout = (size_t)g.nze * g.my * g.mx * n_var; // complex
+  int rc;
+  if ((rc = ensure(c.sc[0], nin * 8)) || (rc = ensure(c.sc[1], nc * 16)) || (rc = ensure(c.sc[2], nout * 16)))
+    return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u1, nin * 8, cudaMemcpyHostToDevice, c.stream));
+  rc = run_x_pass<double>(c, 1, 1, n_var, nullptr, c.sc[0].p, g.nx, (long long)g.nx * g.ny,
+                          (long long)g.nx * g.ny * g.nz, c.sc[1].p, nullptr, g.ny, (long long)g.mx * g.ny,
+                          (long long)g.nz * g.mx * g.ny, 0, 0, 0, false);
+  if (rc) return rc;
+  rc = run_y_fwd<double>(c, c.sc[1].p, c.sc[2].p, n_var, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny,
+                         g.nze, (long long)g.my * g.nze, (long long)g.mx * g.my * g.nze);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(u2, c.sc[2].p, nout * 16, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_z2x_decomp(double* u1, double* u2, int n_var, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (n_var < 1 || !u1 || !u2) return fail(SAM_GPU_EINVAL, "z2x_decomp: bad arguments");
+  // one rank: the received blocks (nzp, Ny_min, nxp, n_var) are the output layout
+  if (u1 != u2) memmove(u2, u1, (size_t)g.nze * g.my * g.mx * n_var * 16);
+  return 0;
+}
+
+int sam_gpu_z_trans_f(double* u, int n_var, const int* isymm, double*, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (n_var < 1 || !u) return fail(SAM_GPU_EINVAL, "z_trans_f: bad arguments");
+  if (!symm_ok(isymm, n_var)) return fail(SAM_GPU_EUNSUPPORTED, "z_trans_f: only the periodic branch (isymm=0) is supported");
+  const size_t n = (size_t)g.nze * g.my * g.mx * n_var;
+  int rc;
+  if ((rc = ensure(c.sc[0], n * 16))) return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u, n * 16, cudaMemcpyHostToDevice, c.stream));
+  ZFwdArgs<double> a{};
+  a.in = (double2*)c.sc[0].p;
+  a.mode = 0;
+  a.nf = n_var;
+  a.in_ky = g.nze; a.in_kx = (long long)g.my * g.nze; a.in_n = (long long)g.mx * g.my * g.nze;
+  if ((rc = run_z_fwd<double>(c, a))) return rc;
+  CK(cudaMemcpyAsync(u, c.sc[0].p, n * 16, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_vel_max(const double* u, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (!u) return fail(SAM_GPU_EINVAL, "vel_max: null array");
+  const size_t n = (size_t)g.nx * g.ny * g.nz * g.lu;
+  int rc;
+  if ((rc = ensure(c.sc[0], n * 8))) return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u, n * 8, cudaMemcpyHostToDevice, c.stream));
+  rc = run_x_pass<double>(c, 1, 3, g.lu, nullptr, c.sc[0].p, g.nx, (long long)g.nx * g.ny,
+                          (long long)g.nx * g.ny * g.nz, nullptr, nullptr, 0, 0, 0, 0, 0, 0, true);
+  if (rc) return rc;
+  return sync_stream(c);
+}
+
+int sam_gpu_rhs(double* u, double* uu, double* r, const double* u_sav, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (!uu || !r) return fail(SAM_GPU_EINVAL, "rhs: null array");
+  if (c.cfg.i_strat && !u_sav) return fail(SAM_GPU_EINVAL, "rhs: u_sav is required when stratified");
+  (void)u;  // u and uu are the same array in sam.f:244; the physical fields are read from uu
+  const size_t nphys = (size_t)g.nx * g.ny * g.nz * g.lu;
+  const size_t nc = (size_t)g.lr * g.nz * g.mx * g.ny;
+  const size_t nd = (size_t)g.lr * g.mx * g.my * g.nze;
+  const size_t nr = (size_t)(g.lu + 1) * g.mx * g.my * g.nze;
+  const size_t ns = (size_t)2 * g.mz * g.my * g.mx;
+  int rc;
+  if ((rc = ensure(c.sc[0], nphys * 8)) || (rc = ensure(c.sc[1], nc * 16)) || (rc = ensure(c.sc[2], nd * 16)) ||
+      (rc = ensure(c.sc[3], (nr + ns) * 16)))
+    return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, uu, nphys * 8, cudaMemcpyHostToDevice, c.stream));
+  double2* dr = (double2*)c.sc[3].p;
+  double2* dsav = dr + nr;
+  if (c.cfg.i_strat) CK(cudaMemcpyAsync(dsav, u_sav, ns * 16, cudaMemcpyHostToDevice, c.stream));
+  rc = run_x_pass<double>(c, 1, 2, g.lu, nullptr, c.sc[0].p, g.nx, (long long)g.nx * g.ny,
+                          (long long)g.nx * g.ny * g.nz, c.sc[1].p, nullptr, g.ny, (long long)g.mx * g.ny,
+                          (long long)g.nz * g.mx * g.ny, 0, 0, 0, c.nrk == 1);
+  if (rc) return rc;
+  rc = run_y_fwd<double>(c, c.sc[1].p, c.sc[2].p, g.lr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny,
+                         g.nze, (long long)g.my * g.nze, (long long)g.mx * g.my * g.nze);
+  if (rc) return rc;
+  ZFwdArgs<double> a{};
+  a.in = (double2*)c.sc[2].p;
+  a.mode = 1;
+  a.nf = g.lr;
+  a.in_ky = g.nze; a.in_kx = (long long)g.my * g.nze; a.in_n = (long long)g.mx * g.my * g.nze;
+  a.r = dr;
+  a.r_ky = g.nze; a.r_kx = (long long)g.my * g.nze; a.r_n = (long long)g.mx * g.my * g.nze;
+  a.usav = dsav;
+  a.sav_ky = g.mz; a.sav_kx = (long long)g.my * g.mz; a.sav_n = (long long)g.mx * g.my * g.mz;
+  a.state = c.state;
+  a.sc = stage_consts(c, c.nrk, 1);
+  if ((rc = run_z_fwd<double>(c, a))) return rc;
+  // rows 1..Nz_min of r(:,:,:,1..Lu+1)
+  CK(cudaMemcpy2DAsync(r, (size_t)g.nze * 16, dr, (size_t)g.nze * 16, (size_t)g.mz * 16,
+                       (size_t)g.my * g.mx * (g.lu + 1), cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+// ------------------------------------------------------------ resident path
+
+int sam_gpu_upload(const double* u) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (!u) return fail(SAM_GPU_EINVAL, "upload: null array");
+  const size_t nm = (size_t)g.mx * g.my * g.mz * g.lu;
+  int rc;
+  void* dst = c.U;
+  if (c.cfg.precision == 32) {
+    if ((rc = ensure(c.sc[0], nm * 16))) return rc;
+    dst = c.sc[0].p;
+  }
+  // rows 1..Nz_min of each (ky, kx, var) column of u(Nze,Ny_min,nxp,Lu)
+  CK(cudaMemcpy2DAsync(dst, (size_t)g.mz * 16, u, (size_t)g.nze * 16, (size_t)g.mz * 16, (size_t)g.my * g.mx * g.lu,
+                       cudaMemcpyHostToDevice, c.stream));
+  if (c.cfg.precision == 32) convert_in<float>((const double2*)dst, (float2*)c.U, (long long)nm, c.stream);
+  CK(cudaMemsetAsync(c.R, 0, csize(c) * nm, c.stream));
+  return sync_stream(c);
+}
+
+static int download_field(Ctx& c, const void* src, double* host, int nf, int host_field0) {
+  const Grid& g = c.g;
+  const size_t nm = (size_t)g.mx * g.my * g.mz * nf;
+  const void* s = src;
+  int rc;
+  if (c.cfg.precision == 32) {
+    if ((rc = ensure(c.sc[1], nm * 16))) return rc;
+    convert_out<float>((const float2*)src, (double2*)c.sc[1].p, (long long)nm, c.stream);
+    s = c.sc[1].p;
+  }
+  double* h = host + (size_t)2 * g.nze * g.my * g.mx * host_field0;
+  CK(cudaMemcpy2DAsync(h, (size_t)g.nze * 16, s, (size_t)g.mz * 16, (size_t)g.mz * 16, (size_t)g.my * g.mx * nf,
+                       cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_download(double* u, double* r) {
+  NEED_CTX();
+  int rc;
+  if (u && (rc = download_field(c, c.U, u, c.g.lu, 0))) return rc;
+  if (r) {
+    if ((rc = download_field(c, c.R, r, c.g.lu, 0))) return rc;
+    if ((rc = download_field(c, c.P, r, 1, c.g.lu))) return rc;
+  }
+  return 0;
+}
+
+int sam_gpu_stage(int nrk) {
+  NEED_CTX();
+  if (nrk < 1 || nrk > c.cfg.nrk_max) return fail(SAM_GPU_EINVAL, "nrk %d out of range", nrk);
+  int rc = stage_any(c, nrk);
+  if (rc) return rc;
+  c.nrk = nrk;
+  return check_launch();
+}
+
+int sam_gpu_step(int nsteps) {
+  NEED_CTX();
+  if (nsteps < 0) return fail(SAM_GPU_EINVAL, "negative step count");
+  if (!c.gexec || c.graph_stream != c.stream) {
+    if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int nrk = 1; nrk <= c.cfg.nrk_max && !rc; ++nrk) rc = stage_any(c, nrk);
+    cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(SAM_GPU_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&c.gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(SAM_GPU_ECUDA, "graph instantiate: %s", cudaGetErrorString(e));
+    c.graph_stream = c.stream;
+  }
+  for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(c.gexec, c.stream));
+  c.nrk = c.cfg.nrk_max;
+  return check_launch();
+}
+
+int sam_gpu_measure_fp64_peak(double* tflops) {
+  NEED_CTX();
+  if (!tflops) return fail(SAM_GPU_EINVAL, "measure_fp64_peak: null output");
+  *tflops = diag_fp64_peak(c.stream);
+  return check_launch();
+}
+
+int sam_gpu_profile_stage(int nrk, int reps, float* ms5) {
+  NEED_CTX();
+  if (nrk < 1 || nrk > c.cfg.nrk_max || reps < 1 || !ms5) return fail(SAM_GPU_EINVAL, "profile_stage: bad arguments");
+  cudaEvent_t ev[6];
+  for (auto& e : ev) CK(cudaEventCreate(&e));
+  for (int p = 0; p < 5; ++p) ms5[p] = 0.0f;
+  int rc = 0;
+  for (int r = 0; r < reps && !rc; ++r) {
+    rc = stage_any(c, nrk, ev);
+    if (rc) break;
+    CK(cudaEventSynchronize(ev[5]));
+    for (int p = 0; p < 5; ++p) {
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, ev[p], ev[p + 1]);
+      ms5[p] += ms / (float)reps;
+    }
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  if (rc) return rc;
+  return check_launch();
+}
+
+// ---------------------------------------------------------- initial fields
+
+static int init_finish(Ctx& c, double2* tmp) {
+  const Grid& g = c.g;
+  const size_t nm = (size_t)g.mx * g.my * g.mz * g.lu;
+  if (c.cfg.precision == 32) convert_in<float>(tmp, (float2*)c.U, (long long)nm, c.stream);
+  CK(cudaMemsetAsync(c.R, 0, csize(c) * nm, c.stream));
+  return sync_stream(c);
+}
+
+static int init_target(Ctx& c, double2** out) {
+  const Grid& g = c.g;
+  const size_t nm = (size_t)g.mx * g.my * g.mz * g.lu;
+  if (c.cfg.precision == 32) {
+    int rc = ensure(c.sc[0], nm * 16);
+    if (rc) return rc;
+    *out = (double2*)c.sc[0].p;
+  } else {
+    *out = (double2*)c.U;
+  }
+  return 0;
+}
+
+int sam_gpu_init_taylor_green(void) {
+  NEED_CTX();
+  if (c.g.kx < 1 || c.g.ky < 1 || c.g.kz < 1) return fail(SAM_GPU_EINVAL, "grid too small for Taylor-Green");
+  double2* u;
+  int rc = init_target(c, &u);
+  if (rc) return rc;
+  fields_init_tg(u, c.g, c.stream);
+  return init_finish(c, u);
+}
+
+int sam_gpu_init_random(unsigned long long seed, int kind_u, double flct_u, int kind_t, double flct_t) {
+  NEED_CTX();
+  double2* u;
+  int rc = init_target(c, &u);
+  if (rc) return rc;
+  fields_init_random(u, c.g, seed, kind_u, flct_u, kind_t, flct_t, c.stream);
+  return init_finish(c, u);
+}
+
+int sam_gpu_init_packet(unsigned long long seed, int kx0, int ky0, int kz0, double sigma, double amplitude,
+                        double noise) {
+  NEED_CTX();
+  double2* u;
+  int rc = init_target(c, &u);
+  if (rc) return rc;
+  fields_init_packet(u, c.g, seed, kx0, ky0, kz0, sigma, amplitude, noise, c.cfg.xl, c.cfg.yl, c.cfg.zl,
+                     c.cfg.buoy_fac_z, c.cfg.lapse, c.stream);
+  return init_finish(c, u);
+}
+
+// ------------------------------------------------------------- diagnostics
+
+int sam_gpu_spectra(double* out) {
+  NEED_CTX();
+  int rc = ensure(c.sc[3], sizeof(double) * ((size_t)5 * c.lm + 8) * 1024);
+  if (rc) return rc;
+  double e_cl = 0.0;
+  if (c.cfg.i_les) {
+    if ((rc = sam_gpu_cl_energy(&e_cl))) return rc;
+  }
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, e_cl, c.cfg.precision);
+  diag_spectra(d, c.U, c.R, (double*)c.sc[3].p, out, c.stream);
+  return sync_stream(c);
+}
+
+int sam_gpu_div_check(double* out4) {
+  NEED_CTX();
+  int rc = ensure(c.sc[3], sizeof(double) * 8 * 1024);
+  if (rc) return rc;
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, c.cfg.precision);
+  diag_div_check(d, c.U, (double*)c.sc[3].p, out4, c.stream);
+  return sync_stream(c);
+}
+
+int sam_gpu_cl_energy(double* e_cl) {
+  NEED_CTX();
+  int rc = ensure(c.sc[3], sizeof(double) * 8 * 1024);
+  if (rc) return rc;
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, c.cfg.precision);
+  diag_cl_energy(d, c.U, (double*)c.sc[3].p, e_cl, c.stream);
+  return sync_stream(c);
+}
+
+int sam_gpu_x_deriv(const double* u, double* du, double*) {
+  NEED_CTX();
+  if (!u || !du) return fail(SAM_GPU_EINVAL, "x_deriv: null array");
+  const size_t n = (size_t)c.g.nx * c.g.ny;
+  int rc;
+  if ((rc = ensure(c.sc[0], n * 8)) || (rc = ensure(c.sc[1], n * 8))) return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u, n * 8, cudaMemcpyHostToDevice, c.stream));
+  diag_deriv(c.g, 0, c.px.d, c.px.tw64, c.px.h, (const double*)c.sc[0].p, (double*)c.sc[1].p, c.stream);
+  CK(cudaMemcpyAsync(du, c.sc[1].p, n * 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_y_deriv(const double* u, double* du, double*) {
+  NEED_CTX();
+  if (!u || !du) return fail(SAM_GPU_EINVAL, "y_deriv: null array");
+  const size_t n = (size_t)c.g.nx * c.g.ny;
+  int rc;
+  if ((rc = ensure(c.sc[0], n * 8)) || (rc = ensure(c.sc[1], n * 8))) return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, u, n * 8, cudaMemcpyHostToDevice, c.stream));
+  diag_deriv(c.g, 1, c.py.d, c.py.tw64, c.py.h, (const double*)c.sc[0].p, (double*)c.sc[1].p, c.stream);
+  CK(cudaMemcpyAsync(du, c.sc[1].p, n * 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,295 @@
+"""Python host-side mirror of the SAM routines on the GB300 library.
+
+A thin ctypes layer over libsam_gpu.so (C ABI in include/sam_gpu.h).  Method
+names and argument meanings follow the reference's Fortran subroutines
+(z_trans_b, x2z_decomp, xy_trans_b, rhs, ...) and arrays use the reference's
+column-major layouts, so code written against the reference reads the same.
+There is no CPU path: if the library or a GPU is missing, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libsam_gpu.so")
+
+SAM_GPU_OK = 0
+ERRORS = {-1: "EINVAL", -2: "ENOTINIT", -3: "EUNSUPPORTED", -4: "ECUDA", -5: "ENONFINITE"}
+
+EXPORTS = [
+    "sam_gpu_init", "sam_gpu_finalize", "sam_gpu_dims", "sam_gpu_set_tstep", "sam_gpu_get_stats",
+    "sam_gpu_set_stream", "sam_gpu_error_string", "sam_gpu_z_trans_b", "sam_gpu_x2z_decomp",
+    "sam_gpu_xy_trans_b", "sam_gpu_xy_trans_f", "sam_gpu_z2x_decomp", "sam_gpu_z_trans_f", "sam_gpu_vel_max",
+    "sam_gpu_rhs", "sam_gpu_x_deriv", "sam_gpu_y_deriv", "sam_gpu_upload", "sam_gpu_download", "sam_gpu_stage",
+    "sam_gpu_step", "sam_gpu_spectra", "sam_gpu_div_check", "sam_gpu_cl_energy", "sam_gpu_init_taylor_green",
+    "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
+]
+
+
+class SamGpuError(RuntimeError):
+    pass
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+        ("n_dealias", C.c_int), ("i_strat", C.c_int), ("i_cfl", C.c_int),
+        ("nrk_max", C.c_int), ("rot_sav", C.c_int), ("i_les", C.c_int), ("precision", C.c_int),
+        ("xl", C.c_double), ("yl", C.c_double), ("zl", C.c_double),
+        ("vis", C.c_double), ("pr", C.c_double),
+        ("dt0", C.c_double), ("cfl0", C.c_double),
+        ("buoy_fac_x", C.c_double), ("buoy_fac_z", C.c_double), ("lapse", C.c_double),
+        ("cos_theta", C.c_double), ("sin_theta", C.c_double),
+        ("c_smag", C.c_double),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("time", C.c_double), ("dt", C.c_double),
+        ("u_avg", C.c_double * 4), ("u_var", C.c_double * 4), ("u_max", C.c_double * 4),
+        ("energy", C.c_double), ("cfl_x", C.c_double), ("cfl_y", C.c_double), ("cfl_z", C.c_double),
+        ("nonfinite", C.c_int), ("pad", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libsam_gpu.so (build it with sam_gb300.build.build())."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise SamGpuError(f"{path} is missing: run sam_gb300.build.build() (there is no CPU fallback)")
+    lib = C.CDLL(path)
+    P = C.c_void_p
+    lib.sam_gpu_init.argtypes = [C.POINTER(Config)]
+    lib.sam_gpu_dims.argtypes = [P]
+    lib.sam_gpu_set_tstep.argtypes = [C.c_int, C.c_double, C.c_double]
+    lib.sam_gpu_get_stats.argtypes = [C.POINTER(Stats)]
+    lib.sam_gpu_set_stream.argtypes = [P]
+    lib.sam_gpu_error_string.restype = C.c_char_p
+    lib.sam_gpu_z_trans_b.argtypes = [P, P, C.c_int, P, P, P, P]
+    lib.sam_gpu_x2z_decomp.argtypes = [P, P, C.c_int, P]
+    lib.sam_gpu_xy_trans_b.argtypes = [P, P, C.c_int, P]
+    lib.sam_gpu_xy_trans_f.argtypes = [P, P, C.c_int, P]
+    lib.sam_gpu_z2x_decomp.argtypes = [P, P, C.c_int, P]
+    lib.sam_gpu_z_trans_f.argtypes = [P, C.c_int, P, P, P]
+    lib.sam_gpu_vel_max.argtypes = [P, P]
+    lib.sam_gpu_rhs.argtypes = [P, P, P, P, P]
+    lib.sam_gpu_x_deriv.argtypes = [P, P, P]
+    lib.sam_gpu_y_deriv.argtypes = [P, P, P]
+    lib.sam_gpu_upload.argtypes = [P]
+    lib.sam_gpu_download.argtypes = [P, P]
+    lib.sam_gpu_stage.argtypes = [C.c_int]
+    lib.sam_gpu_step.argtypes = [C.c_int]
+    lib.sam_gpu_spectra.argtypes = [P]
+    lib.sam_gpu_div_check.argtypes = [P]
+    lib.sam_gpu_cl_energy.argtypes = [P]
+    lib.sam_gpu_init_random.argtypes = [C.c_ulonglong, C.c_int, C.c_double, C.c_int, C.c_double]
+    lib.sam_gpu_init_packet.argtypes = [C.c_ulonglong, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                        C.c_double]
+    lib.sam_gpu_profile_stage.argtypes = [C.c_int, C.c_int, P]
+    lib.sam_gpu_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    assert isinstance(a, np.ndarray)
+    assert a.flags["F_CONTIGUOUS"] or a.ndim <= 1, "arrays must be Fortran-ordered"
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def reference_config(nx, ny, nz, *, i_strat=0, n_dealias=1, i_cfl=0, nrk_max=3, xl=2 * np.pi, yl=2 * np.pi,
+                     zl=2 * np.pi, vis=0.0, pr=1.0, dt0=0.01, cfl0=0.5, grav=0.0, to=1.0, lapse0=0.0,
+                     rot_sav=0, i_les=0, precision=64, cos_theta=1.0, sin_theta=0.0, c_smag=0.01, **_):
+    """Config values derived as init.f and initial_field.f derive them:
+    buoy_fac_z = grav/To when stratified (initial_field.f:159-161) and
+    lapse = lapse0 (initial_field.f:37)."""
+    return dict(nx=nx, ny=ny, nz=nz, n_dealias=n_dealias, i_strat=i_strat, i_cfl=i_cfl, nrk_max=nrk_max,
+                rot_sav=rot_sav, i_les=i_les, precision=precision, xl=xl, yl=yl, zl=zl, vis=vis, pr=pr, dt0=dt0,
+                cfl0=cfl0, buoy_fac_x=0.0, buoy_fac_z=(grav / to if i_strat else 0.0),
+                lapse=(lapse0 if i_strat else 0.0), cos_theta=cos_theta, sin_theta=sin_theta, c_smag=c_smag)
+
+
+class SamGpu:
+    """The device context (one per process; the reference's COMMON state)."""
+
+    _live = None
+
+    def __init__(self, **cfg):
+        lib = load_library()
+        if SamGpu._live is not None:
+            SamGpu._live.close()
+        self.cfg = Config()
+        defaults = dict(n_dealias=1, i_strat=0, i_cfl=0, nrk_max=3, rot_sav=0, i_les=0, precision=64,
+                        xl=2 * np.pi, yl=2 * np.pi, zl=2 * np.pi, vis=0.0, pr=1.0, dt0=0.01, cfl0=0.5,
+                        buoy_fac_x=0.0, buoy_fac_z=0.0, lapse=0.0, cos_theta=1.0, sin_theta=0.0, c_smag=0.01)
+        defaults.update(cfg)
+        for k, v in defaults.items():
+            setattr(self.cfg, k, v)
+        self._check(lib.sam_gpu_init(C.byref(self.cfg)), "sam_gpu_init")
+        SamGpu._live = self
+        d = np.zeros(11, dtype=np.int32)
+        self._check(lib.sam_gpu_dims(d.ctypes.data_as(C.c_void_p)), "sam_gpu_dims")
+        (self.nx_min, self.ny_min, self.nz_min, self.nze, self.lu, self.lr, self.kx_max, self.ky_max,
+         self.kz_max, self.lm, self.nx2) = [int(x) for x in d]
+        self.nx, self.ny, self.nz = self.cfg.nx, self.cfg.ny, self.cfg.nz
+
+    def _check(self, rc, what):
+        if rc != SAM_GPU_OK:
+            msg = load_library().sam_gpu_error_string().decode(errors="replace")
+            raise SamGpuError(f"{what} failed ({ERRORS.get(rc, rc)}): {msg}")
+
+    def close(self):
+        if SamGpu._live is self:
+            load_library().sam_gpu_finalize()
+            SamGpu._live = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- arrays in the reference layouts
+    def wave(self, n):
+        return np.zeros((self.nze, self.ny_min, self.nx_min, n), dtype=np.complex128, order="F")
+
+    def zblocks(self, n):
+        return np.zeros((self.ny_min, self.nx_min, self.nze, n), dtype=np.complex128, order="F")
+
+    def xyplanes(self, n):
+        return np.zeros((self.ny, self.nx2, self.nz, n), dtype=np.complex128, order="F")
+
+    def phys(self, n):
+        return np.zeros((self.nx, self.ny, self.nz, n), dtype=np.float64, order="F")
+
+    # ---- state
+    def set_tstep(self, nrk, dt, time):
+        self._check(load_library().sam_gpu_set_tstep(nrk, dt, time), "set_tstep")
+
+    def stats(self):
+        s = Stats()
+        self._check(load_library().sam_gpu_get_stats(C.byref(s)), "get_stats")
+        return dict(time=s.time, dt=s.dt, u_avg=np.array(s.u_avg[:]), u_var=np.array(s.u_var[:]),
+                    u_max=np.array(s.u_max[:]), energy=s.energy, cfl_x=s.cfl_x, cfl_y=s.cfl_y, cfl_z=s.cfl_z,
+                    nonfinite=s.nonfinite)
+
+    def set_stream(self, stream_handle):
+        self._check(load_library().sam_gpu_set_stream(C.c_void_p(stream_handle)), "set_stream")
+
+    # ---- per-routine drop-ins
+    def z_trans_b(self, u1, n_var, isymm=None):
+        u2 = self.zblocks(n_var)
+        iv = np.zeros(n_var, dtype=np.int32) if isymm is None else np.asarray(isymm, dtype=np.int32)
+        self._check(load_library().sam_gpu_z_trans_b(_p(u1), _p(u2), n_var, _p(iv), None, None, None), "z_trans_b")
+        return u2
+
+    def x2z_decomp(self, u1, n_var, out=None):
+        u2 = self.xyplanes(n_var) if out is None else out
+        self._check(load_library().sam_gpu_x2z_decomp(_p(u1), _p(u2), n_var, _p(u2)), "x2z_decomp")
+        return u2
+
+    def xy_trans_b(self, u1, n_var):
+        u2 = self.phys(n_var)
+        self._check(load_library().sam_gpu_xy_trans_b(_p(u1), _p(u2), n_var, None), "xy_trans_b")
+        return u2
+
+    def xy_trans_f(self, u1, n_var):
+        u2 = self.wave(n_var)
+        self._check(load_library().sam_gpu_xy_trans_f(_p(u1), _p(u2), n_var, None), "xy_trans_f")
+        return u2
+
+    def z2x_decomp(self, u1, n_var, out=None):
+        u2 = u1 if out is None else out
+        self._check(load_library().sam_gpu_z2x_decomp(_p(u1), _p(u2), n_var, None), "z2x_decomp")
+        return u2
+
+    def z_trans_f(self, u, n_var, isymm=None):
+        iv = np.zeros(n_var, dtype=np.int32) if isymm is None else np.asarray(isymm, dtype=np.int32)
+        self._check(load_library().sam_gpu_z_trans_f(_p(u), n_var, _p(iv), None, None), "z_trans_f")
+        return u
+
+    def vel_max(self, u):
+        self._check(load_library().sam_gpu_vel_max(_p(u), None), "vel_max")
+        return self.stats()
+
+    def rhs(self, uu, u_sav=None):
+        r = self.wave(self.lr)
+        self._check(load_library().sam_gpu_rhs(_p(uu), _p(uu), _p(r), _p(u_sav), None), "rhs")
+        return r
+
+    def x_deriv(self, u):
+        du = np.zeros_like(u, order="F")
+        self._check(load_library().sam_gpu_x_deriv(_p(u), _p(du), None), "x_deriv")
+        return du
+
+    def y_deriv(self, u):
+        du = np.zeros_like(u, order="F")
+        self._check(load_library().sam_gpu_y_deriv(_p(u), _p(du), None), "y_deriv")
+        return du
+
+    # ---- resident path
+    def upload(self, u):
+        self._check(load_library().sam_gpu_upload(_p(u)), "upload")
+
+    def download(self, with_r=False, out=None):
+        u = self.wave(self.lu) if out is None else out
+        r = self.wave(self.lu + 1) if with_r else None
+        self._check(load_library().sam_gpu_download(_p(u), _p(r)), "download")
+        return (u, r) if with_r else u
+
+    def stage(self, nrk):
+        self._check(load_library().sam_gpu_stage(nrk), "stage")
+
+    def step(self, nsteps=1):
+        self._check(load_library().sam_gpu_step(nsteps), "step")
+
+    def profile_stage(self, nrk, reps):
+        """Mean ms of the five passes of stage nrk (CUDA events between them)."""
+        ms = np.zeros(5, dtype=np.float32)
+        self._check(load_library().sam_gpu_profile_stage(nrk, reps, ms.ctypes.data_as(C.c_void_p)), "profile")
+        return dict(zip(("z_inv", "y_inv", "x_pass", "y_fwd", "z_fwd"), [float(x) for x in ms]))
+
+    def fp64_peak_tflops(self):
+        t = C.c_double(0.0)
+        self._check(load_library().sam_gpu_measure_fp64_peak(C.byref(t)), "measure_fp64_peak")
+        return t.value
+
+    # ---- diagnostics
+    def spectra(self):
+        lm = self.lm
+        o = np.zeros(5 * lm + 3)
+        self._check(load_library().sam_gpu_spectra(_p(o)), "spectra")
+        return dict(ek=o[:lm], tk=o[lm:2 * lm], dk=o[2 * lm:3 * lm], vt=o[3 * lm:4 * lm],
+                    sample=o[4 * lm:5 * lm], energy_w=o[5 * lm], div_rms=o[5 * lm + 1], div_max=o[5 * lm + 2])
+
+    def div_check(self):
+        o = np.zeros(4)
+        self._check(load_library().sam_gpu_div_check(_p(o)), "div_check")
+        return dict(div_avg=o[0], div_rms=o[1], div_max=o[2], n_div=o[3])
+
+    def cl_energy(self):
+        e = C.c_double(0.0)
+        self._check(load_library().sam_gpu_cl_energy(C.byref(e)), "cl_energy")
+        return e.value
+
+    # ---- initial fields
+    def init_taylor_green(self):
+        self._check(load_library().sam_gpu_init_taylor_green(), "init_taylor_green")
+
+    def init_random(self, seed, kind_u=6, flct_u=1.0, kind_t=6, flct_t=0.1):
+        self._check(load_library().sam_gpu_init_random(seed, kind_u, flct_u, kind_t, flct_t), "init_random")
+
+    def init_packet(self, seed, k0=(8, 0, 16), sigma=np.pi / 4, amplitude=0.05, noise=0.01):
+        self._check(load_library().sam_gpu_init_packet(seed, k0[0], k0[1], k0[2], sigma, amplitude, noise),
+                    "init_packet")
