@@ -95,7 +95,19 @@ def lib():
         _lib.so_init_gw_plane.argtypes = [P, P] + [C.c_double] * 8
         _lib.so_init_packet.argtypes = [P, P, C.c_ulonglong, C.c_int, C.c_int, C.c_int,
                                         C.c_double, C.c_double, C.c_double]
+        _lib.so_fft_line.argtypes = [C.c_int, C.c_int, P]
     return _lib
+
+
+def fft_line(data: np.ndarray, kind: str) -> np.ndarray:
+    """One FFTPACK-convention transform: 'cfftf', 'cfftb' (complex input) or
+    'rfftf', 'rfftb' (real input in FFTPACK's packed layout)."""
+    k = {"cfftf": 0, "cfftb": 1, "rfftf": 2, "rfftb": 3}[kind]
+    a = np.array(data, dtype=np.complex128 if k <= 1 else np.float64, copy=True)
+    rc = lib().so_fft_line(len(a), k, a.ctypes.data_as(C.c_void_p))
+    if rc:
+        raise ValueError(f"unsupported length {len(a)}")
+    return a
 
 
 def _p(a: np.ndarray):

@@ -1106,3 +1106,25 @@ int so_init_packet(so_ctx *c, double *ud, unsigned long long seed, int kx0, int 
   enforce_symm(c, u, 0, c->lu);
   return 0;
 }
+
+/* ------------------------------------------------ raw transforms for tests */
+
+/* one FFTPACK-convention transform of a single line: kind 0 cfftf, 1 cfftb
+ * (data: n interleaved complex), 2 rfftf, 3 rfftb (data: n reals) */
+int so_fft_line(int n, int kind, double *data) {
+  so_cplx *work = (so_cplx *)malloc(sizeof(so_cplx) * (size_t)(2 * n + 4));
+  int rc = 0;
+  if (kind <= 1) {
+    so_cplan p;
+    if (so_cplan_init(&p, n)) { free(work); return -1; }
+    if (kind == 0) so_cfftf(&p, (so_cplx *)data, work); else so_cfftb(&p, (so_cplx *)data, work);
+    so_cplan_free(&p);
+  } else {
+    so_rplan p;
+    if (so_rplan_init(&p, n)) { free(work); return -1; }
+    if (kind == 2) so_rfftf(&p, data, work); else so_rfftb(&p, data, work);
+    so_rplan_free(&p);
+  }
+  free(work);
+  return rc;
+}

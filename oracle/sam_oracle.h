@@ -105,6 +105,9 @@ int so_init_gw_plane(so_ctx *c, double *u, double amplitude, double lambda_x, do
 int so_init_packet(so_ctx *c, double *u, unsigned long long seed, int kx0, int ky0, int kz0,
                    double sigma, double amplitude, double noise);
 
+/* ---- one raw FFTPACK-convention transform (0 cfftf, 1 cfftb, 2 rfftf, 3 rfftb) ---- */
+int so_fft_line(int n, int kind, double *data);
+
 #ifdef __cplusplus
 }
 #endif
