@@ -43,7 +43,8 @@ WORKLOAD = ("gravity-wave packet 256^3 stratified Boussinesq, N=2, nu=kappa=1e-4
 METRIC = "RK3 steps/s at 256^3 (FP64 drop-in; FP32 bulk reported beside it)"
 
 
-def workload_cfg(n=N, precision=64):
+def workload_cfg(n=None, precision=64):
+    n = n or N
     return dict(nx=n, ny=n, nz=n, i_strat=1, i_cfl=1, cfl0=0.5, vis=1e-4, pr=1.0, dt0=1e-3,
                 buoy_fac_z=4.0, lapse=1.0, precision=precision)
 
@@ -51,16 +52,18 @@ def workload_cfg(n=N, precision=64):
 PACKET = dict(seed=1, k0=(8, 0, 16), sigma=math.pi / 4, amplitude=0.05, noise=0.01)
 
 
-def dims(n=N, lu=4, lr=9):
+def dims(n=None, lu=4, lr=9):
+    n = n or N
     k = int((n - 0.1) / 3.0)
     mx, my, mz = k + 1, 2 * k + 1, 2 * k + 1
     return mx, my, mz
 
 
-def algorithmic_bytes_per_step(n=N, w=8, lu=4, lr=9):
+def algorithmic_bytes_per_step(n=None, w=8, lu=4, lr=9):
     """Bytes one stage must move with the transposes fused into the passes:
     z inverse, y inverse, x pass (C2R, products, R2C), y forward, z forward
     with the update (read u, r_old; write u, r, p); three stages per step."""
+    n = n or N
     mx, my, mz = dims(n)
     sz, szn, syn = mx * my * mz, mx * my * n, mx * n * n
     c = 2 * w
@@ -69,17 +72,20 @@ def algorithmic_bytes_per_step(n=N, w=8, lu=4, lr=9):
     return 3 * stage
 
 
-def x_pass_bytes(n=N, w=8, lu=4, lr=9):
+def x_pass_bytes(n=None, w=8, lu=4, lr=9):
+    n = n or N
     mx, _, _ = dims(n)
     return 2 * w * (lu + lr) * mx * n * n
 
 
-def x_pass_flops(n=N, lu=4, lr=9):
+def x_pass_flops(n=None, lu=4, lr=9):
+    n = n or N
     # 5 n log2 n per complex line; two real x-lines share one complex line
     return 5.0 * n * math.log2(n) * (lu + lr) * n * (n / 2)
 
 
-def step_flops(n=N, lu=4, lr=9):
+def step_flops(n=None, lu=4, lr=9):
+    n = n or N
     mx, my, _ = dims(n)
     f = 5.0 * n * math.log2(n)
     per_field = mx * my * f + mx * n * f + n * n * f / 2
@@ -201,7 +207,14 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--grid", type=int, default=256, help="N of the N^3 box (profiling of smaller cases)")
+    ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
+                    help="precision of the timed run (32 for profiling the FP32 bulk form)")
     args = ap.parse_args()
+    global N, WORKLOAD
+    if args.grid != N:
+        WORKLOAD = WORKLOAD.replace("256^3", f"{args.grid}^3")
+        N = args.grid
     if args.impl == "reference":
         return run_reference(args)
 
@@ -222,7 +235,7 @@ def main():
 
     K, W = args.steps, max(args.warmup, 3)
     stream = torch.cuda.Stream()
-    g = SamGpu(**workload_cfg())
+    g = SamGpu(**workload_cfg(precision=args.precision))
     g.set_stream(stream.cuda_stream)
     g.init_packet(PACKET["seed"], PACKET["k0"], PACKET["sigma"], PACKET["amplitude"], PACKET["noise"])
     u_init = g.download()
@@ -341,7 +354,7 @@ def main():
     ms_step = ms / K
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic (seeded, generated on the device)",
+            "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded, generated on the device)",
             "config": {"workload": WORKLOAD, "grid": [N, N, N], "fields": 4, "products": 9,
                        "l2": "inputs larger than L2 (state 161 MB, pencils up to 811 MB per pass)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
