@@ -128,6 +128,22 @@ int sam_gpu_profile_stage(int nrk, int reps, float* ms5);
  * roofline of the FP64 drop-in.  No counterpart in the reference. */
 int sam_gpu_measure_fp64_peak(double* tflops);
 
+/* ---- vel_max for callers that cannot allocate device memory ----
+ * No counterpart in the reference.  For callers that own all device memory
+ * through another allocator, or must not stall a step loop on cudaMalloc:
+ * same sums as vel_max.f:156-181, but u_dev (real (Nx,Ny,nzp,Lu)) and
+ * stats_dev (16 doubles: u_avg[4], u_var[4], u_max[4], energy, count of
+ * non-finite values, 2 unused) are DEVICE pointers, and the per-plane
+ * partial sums live in a 512 KB array compiled into the library (held on
+ * every GPU that loads it until exit), so the call allocates nothing and needs
+ * no sam_gpu_init.  nzp may not exceed SAM_GPU_NOALLOC_MAX_PLANES (else
+ * SAM_GPU_EINVAL); Lu is 1..4.  The first call on each device looks up that
+ * array's device address and should precede any stream capture.  Calls that
+ * overlap on the GPU share the array and race.  stream: a cudaStream_t or
+ * NULL for the default stream; the call is asynchronous on it. */
+#define SAM_GPU_NOALLOC_MAX_PLANES 4096
+int sam_gpu_vel_max_noalloc(const double* u_dev, int nx, int ny, int nzp, int lu, double* stats_dev, void* stream);
+
 /* ---- diagnostics on the resident state ---- */
 /* spectra.f:1  out[5*Lm+3]: ek tk dk vt sample, energy_w, div_rms, div_max */
 int sam_gpu_spectra(double* out);

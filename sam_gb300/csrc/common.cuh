@@ -47,4 +47,7 @@ __device__ __forceinline__ int kpos(int j, int km, int m, int n) { return j <= k
 
 constexpr int kThreads = 256;
 
+// Records the message returned by sam_gpu_error_string(); returns code.
+int set_error(int code, const char* msg);
+
 }  // namespace samgpu

@@ -30,6 +30,8 @@ static int fail(int code, const char* fmt, ...) {
   return code;
 }
 
+int set_error(int code, const char* msg) { return fail(code, "%s", msg); }
+
 #define CK(call)                                                                                   \
   do {                                                                                             \
     cudaError_t e_ = (call);                                                                       \

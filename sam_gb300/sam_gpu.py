@@ -26,6 +26,7 @@ EXPORTS = [
     "sam_gpu_rhs", "sam_gpu_x_deriv", "sam_gpu_y_deriv", "sam_gpu_upload", "sam_gpu_download", "sam_gpu_stage",
     "sam_gpu_step", "sam_gpu_spectra", "sam_gpu_div_check", "sam_gpu_cl_energy", "sam_gpu_init_taylor_green",
     "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
+    "sam_gpu_vel_max_noalloc",
 ]
 
 
@@ -96,6 +97,7 @@ def load_library(path: str = LIB_PATH):
                                         C.c_double]
     lib.sam_gpu_profile_stage.argtypes = [C.c_int, C.c_int, P]
     lib.sam_gpu_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.sam_gpu_vel_max_noalloc.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P]
     _lib = lib
     return lib
 
