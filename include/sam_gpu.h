@@ -107,6 +107,27 @@ int sam_gpu_rhs(double* u, double* uu, double* r, const double* u_sav, double* w
 int sam_gpu_x_deriv(const double* u, double* du, double* work);
 int sam_gpu_y_deriv(const double* u, double* du, double* work);
 
+/* ---- subgrid models on haloed grids (Lx,Ly,Lz) = (Nx+2,Ny+2,Nz+2) ----
+ * filter.f, sm.f and dm.f include a header the reference does not ship; the
+ * symbols it would define are fixed here: periodic halo planes 1 and N+2,
+ * ifact = (1,1,1,2,2,2), ip = (1,2,3,1,2,1), jp = (1,2,3,2,3,3),
+ * alpha_sq = 4, delta_sq = (dx dy dz)^(2/3) (init.f:28), c_smag from the
+ * configuration.  Input halos must hold the periodic images (as
+ * periodicity.f sets them); outputs get periodic halos. */
+/* filter.f:1  f_bar(Lx,Ly,n_var,3) -> f_hat(Lx,Ly,n_var) */
+int sam_gpu_filter(const double* f_bar, double* f_hat, int n_var);
+/* sm.f:1  u(Lx,Ly,Lz,3) -> vt(Lx,Ly,Lz); u_bar, s_bar are workspace (may be NULL) */
+int sam_gpu_sm(const double* u, double* u_bar, double* s_bar, double* vt);
+/* dm.f:1  u(Lx,Ly,Lz,3) -> vt(Lx,Ly,Lz); the work arrays may be NULL;
+ * c_delta_sq (may be NULL) receives the volume-averaged coefficient that
+ * dm.f:176-178 logs (times delta_sq_inv there). */
+int sam_gpu_dm(const double* u, double* u_bar, double* s_bar, double* s_mag_s, double* u_bar_u_bar, double* u_hat,
+               double* s_hat, double* L, double* M, double* vt, double* c_delta_sq);
+/* get_mean.f:1  one field u(Nze,Ny_min,nxp): horizontal-mean profile
+ * u_mean(Nze) and the linear jump; i_remove = 1 removes the jump's linear
+ * profile from the kx = ky = 0 column of u in place. i_symm must be 0. */
+int sam_gpu_get_mean(double* u, int i_symm, int i_remove, double* u_mean, double* jump, double* work);
+
 /* ---- resident fused path: state stays in HBM between steps ---- */
 /* after initial_field / read_field (sam.f:102-108): u(Nze,Ny_min,nxp,Lu) */
 int sam_gpu_upload(const double* u);

@@ -1,0 +1,16 @@
+// Subgrid-model routines and get_mean (les.cu).
+#pragma once
+#include "common.cuh"
+
+namespace samgpu {
+void les_filter(const double* f_bar, double* f_hat, int nx, int ny, int n_var, cudaStream_t s);
+// ub: 3*Nx*Ny*Nz doubles of workspace
+void les_sm(const double* u, double* ub, double* vt, int nx, int ny, int nz, double c_delta_sq, double dxi, double dyi,
+            double dzi, cudaStream_t s);
+int les_dm_blocks(int nx, int ny, int nz);
+// ub: 3*N, q: 19*N doubles (N = Nx*Ny*Nz); part: 2*les_dm_blocks; cds: 1
+void les_dm(const double* u, double* ub, double* q, double* part, double* cds, double* vt, int nx, int ny, int nz,
+            double alpha_sq, double dxi, double dyi, double dzi, cudaStream_t s);
+void les_get_mean(double2* col, int mz, int kz, int nz, int i_remove, const FftPlan* dplan, const double2* tw,
+                  const FftPlan& hplan, double* u_mean, double* jump, cudaStream_t s);
+}  // namespace samgpu

@@ -16,6 +16,7 @@
 #include "common.cuh"
 #include "diag.cuh"
 #include "fields.cuh"
+#include "les.cuh"
 #include "passes.cuh"
 
 namespace samgpu {
@@ -913,6 +914,91 @@ int sam_gpu_x_deriv(const double* u, double* du, double*) {
   CK(cudaMemcpyAsync(c.sc[0].p, u, n * 8, cudaMemcpyHostToDevice, c.stream));
   diag_deriv(c.g, 0, c.px.d, c.px.tw64, c.px.h, (const double*)c.sc[0].p, (double*)c.sc[1].p, c.stream);
   CK(cudaMemcpyAsync(du, c.sc[1].p, n * 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+// ------------------------------------------------ subgrid models, get_mean
+
+int sam_gpu_filter(const double* f_bar, double* f_hat, int n_var) {
+  NEED_CTX();
+  if (!f_bar || !f_hat || n_var < 1) return fail(SAM_GPU_EINVAL, "filter: bad arguments");
+  const size_t pl = (size_t)(c.g.nx + 2) * (c.g.ny + 2);
+  int rc;
+  if ((rc = ensure(c.sc[0], pl * n_var * 3 * 8)) || (rc = ensure(c.sc[1], pl * n_var * 8))) return rc;
+  CK(cudaMemcpyAsync(c.sc[0].p, f_bar, pl * n_var * 3 * 8, cudaMemcpyHostToDevice, c.stream));
+  les_filter((const double*)c.sc[0].p, (double*)c.sc[1].p, c.g.nx, c.g.ny, n_var, c.stream);
+  CK(cudaMemcpyAsync(f_hat, c.sc[1].p, pl * n_var * 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+static void grid_spacing(const Ctx& c, double& dxi, double& dyi, double& dzi, double& delta_sq) {
+  const double dx = c.cfg.xl / c.g.nx, dy = c.cfg.yl / c.g.ny, dz = c.cfg.zl / c.g.nz;
+  dxi = 1.0 / dx; dyi = 1.0 / dy; dzi = 1.0 / dz;
+  delta_sq = pow(dx * dy * dz, 2.0 / 3.0);  // init.f:28
+}
+
+int sam_gpu_sm(const double* u, double*, double*, double* vt) {
+  NEED_CTX();
+  if (!u || !vt) return fail(SAM_GPU_EINVAL, "sm: null array");
+  const Grid& g = c.g;
+  const size_t vol = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+  const size_t n = (size_t)g.nx * g.ny * g.nz;
+  int rc;
+  if ((rc = ensure(c.sc[0], vol * 3 * 8)) || (rc = ensure(c.sc[1], vol * 8)) || (rc = ensure(c.sc[2], n * 3 * 8)))
+    return rc;
+  double dxi, dyi, dzi, dsq;
+  grid_spacing(c, dxi, dyi, dzi, dsq);
+  CK(cudaMemcpyAsync(c.sc[0].p, u, vol * 3 * 8, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemsetAsync(c.sc[1].p, 0, vol * 8, c.stream));
+  les_sm((const double*)c.sc[0].p, (double*)c.sc[2].p, (double*)c.sc[1].p, g.nx, g.ny, g.nz, c.cfg.c_smag * dsq, dxi,
+         dyi, dzi, c.stream);
+  CK(cudaMemcpyAsync(vt, c.sc[1].p, vol * 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_dm(const double* u, double*, double*, double*, double*, double*, double*, double*, double*, double* vt,
+               double* c_delta_sq) {
+  NEED_CTX();
+  if (!u || !vt) return fail(SAM_GPU_EINVAL, "dm: null array");
+  const Grid& g = c.g;
+  const size_t vol = (size_t)(g.nx + 2) * (g.ny + 2) * (g.nz + 2);
+  const size_t n = (size_t)g.nx * g.ny * g.nz;
+  const int nb = les_dm_blocks(g.nx, g.ny, g.nz);
+  int rc;
+  if ((rc = ensure(c.sc[0], vol * 3 * 8)) || (rc = ensure(c.sc[1], vol * 8)) ||
+      (rc = ensure(c.sc[2], n * 22 * 8)) || (rc = ensure(c.sc[3], (2 * (size_t)nb + 8) * 8)))
+    return rc;
+  double dxi, dyi, dzi, dsq;
+  grid_spacing(c, dxi, dyi, dzi, dsq);
+  double* ub = (double*)c.sc[2].p;
+  double* q = ub + 3 * n;
+  double* part = (double*)c.sc[3].p;
+  double* cds = part + 2 * nb;
+  CK(cudaMemcpyAsync(c.sc[0].p, u, vol * 3 * 8, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemsetAsync(c.sc[1].p, 0, vol * 8, c.stream));
+  les_dm((const double*)c.sc[0].p, ub, q, part, cds, (double*)c.sc[1].p, g.nx, g.ny, g.nz, 4.0, dxi, dyi, dzi,
+         c.stream);
+  CK(cudaMemcpyAsync(vt, c.sc[1].p, vol * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (c_delta_sq) CK(cudaMemcpyAsync(c_delta_sq, cds, 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_get_mean(double* u, int i_symm, int i_remove, double* u_mean, double* jump, double*) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (!u || !u_mean || !jump) return fail(SAM_GPU_EINVAL, "get_mean: null array");
+  if (i_symm != 0) return fail(SAM_GPU_EUNSUPPORTED, "get_mean: only the periodic branch (i_symm=0) is supported");
+  if (g.nz < 3) return fail(SAM_GPU_EINVAL, "get_mean: Nz must be >= 3");
+  int rc;
+  if ((rc = ensure(c.sc[0], ((size_t)g.mz * 2 + (size_t)g.nz + 8) * 8))) return rc;
+  double2* col = (double2*)c.sc[0].p;
+  double* dmean = (double*)(col + g.mz);
+  double* djump = dmean + g.nz;
+  CK(cudaMemcpyAsync(col, u, (size_t)g.mz * 16, cudaMemcpyHostToDevice, c.stream));
+  les_get_mean(col, g.mz, g.kz, g.nz, i_remove, c.pz.d, c.pz.tw64, c.pz.h, dmean, djump, c.stream);
+  CK(cudaMemcpyAsync(u, col, (size_t)g.mz * 16, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(u_mean, dmean, (size_t)g.nz * 8, cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaMemcpyAsync(jump, djump, 8, cudaMemcpyDeviceToHost, c.stream));
   return sync_stream(c);
 }
 

@@ -26,7 +26,7 @@ EXPORTS = [
     "sam_gpu_rhs", "sam_gpu_x_deriv", "sam_gpu_y_deriv", "sam_gpu_upload", "sam_gpu_download", "sam_gpu_stage",
     "sam_gpu_step", "sam_gpu_spectra", "sam_gpu_div_check", "sam_gpu_cl_energy", "sam_gpu_init_taylor_green",
     "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
-    "sam_gpu_vel_max_noalloc",
+    "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
 ]
 
 
@@ -98,6 +98,10 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_profile_stage.argtypes = [C.c_int, C.c_int, P]
     lib.sam_gpu_measure_fp64_peak.argtypes = [C.POINTER(C.c_double)]
     lib.sam_gpu_vel_max_noalloc.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_int, P, P]
+    lib.sam_gpu_filter.argtypes = [P, P, C.c_int]
+    lib.sam_gpu_sm.argtypes = [P, P, P, P]
+    lib.sam_gpu_dm.argtypes = [P] * 11
+    lib.sam_gpu_get_mean.argtypes = [P, C.c_int, C.c_int, P, P, P]
     _lib = lib
     return lib
 
@@ -239,6 +243,31 @@ class SamGpu:
         du = np.zeros_like(u, order="F")
         self._check(load_library().sam_gpu_y_deriv(_p(u), _p(du), None), "y_deriv")
         return du
+
+    # ---- subgrid models (haloed grids) and get_mean
+    def filter(self, f_bar, n_var):
+        f_hat = np.zeros((self.nx + 2, self.ny + 2, n_var), order="F")
+        self._check(load_library().sam_gpu_filter(_p(f_bar), _p(f_hat), n_var), "filter")
+        return f_hat
+
+    def sm(self, u):
+        vt = np.zeros((self.nx + 2, self.ny + 2, self.nz + 2), order="F")
+        self._check(load_library().sam_gpu_sm(_p(u), None, None, _p(vt)), "sm")
+        return vt
+
+    def dm(self, u):
+        vt = np.zeros((self.nx + 2, self.ny + 2, self.nz + 2), order="F")
+        cds = np.zeros(1)
+        self._check(load_library().sam_gpu_dm(_p(u), None, None, None, None, None, None, None, None, _p(vt),
+                                              _p(cds)), "dm")
+        return vt, float(cds[0])
+
+    def get_mean(self, ufield, i_remove=0):
+        """ufield: one field (Nze, Ny_min, Nx_min), modified in place when i_remove=1."""
+        um = np.zeros(self.nze)
+        jump = np.zeros(1)
+        self._check(load_library().sam_gpu_get_mean(_p(ufield), 0, i_remove, _p(um), _p(jump), None), "get_mean")
+        return um, float(jump[0])
 
     # ---- resident path
     def upload(self, u):
