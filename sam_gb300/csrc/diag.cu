@@ -207,7 +207,7 @@ __global__ void k_deriv(Grid g, int dir, const FftPlan* __restrict__ gpl, const 
   load_plan(&pl, gpl);
   __syncthreads();
   const int n = pl.n;
-  const int ld = n + ((n % 2 == 0) ? 1 : 0);
+  const int ld = line_stride(n);
   double2* s_tw = reinterpret_cast<double2*>(smem_raw);
   double2* s_ln = s_tw + pl.tw_total;
   for (int e = threadIdx.x; e < pl.tw_total; e += blockDim.x) s_tw[e] = gtw[e];
@@ -224,7 +224,7 @@ __global__ void k_deriv(Grid g, int dir, const FftPlan* __restrict__ gpl, const 
     const int ra = 2 * (p0 + L), rb = ra + 1;
     const double a = u[ra * sline + x * selem] * ninv;
     const double b = rb < nrows ? u[rb * sline + x * selem] * ninv : 0.0;
-    s_ln[L * ld + x] = make_double2(a, b);
+    s_ln[L * ld + sidx(x)] = make_double2(a, b);
   }
   __syncthreads();
   fft_lines<-1>(s_ln, ld, np, s_tw, pl);
@@ -235,7 +235,7 @@ __global__ void k_deriv(Grid g, int dir, const FftPlan* __restrict__ gpl, const 
     const int L = e / (n / 2 + 1), k = e - L * (n / 2 + 1);
     double2* ln = s_ln + L * ld;
     const int kk = (n - k) % n;
-    const double2 z1 = ln[k], z2 = ln[kk];
+    const double2 z1 = ln[sidx(k)], z2 = ln[sidx(kk)];
     double2 o1 = make_double2(0.0, 0.0), o2 = make_double2(0.0, 0.0);
     if (k >= 1 && k <= kmax) {
       // X = (z1 + conj z2)/2, Y = (z1 - conj z2)/(2i)
@@ -248,8 +248,8 @@ __global__ void k_deriv(Grid g, int dir, const FftPlan* __restrict__ gpl, const 
       o1 = make_double2(dxr - dyi, dxi + dyr);
       o2 = make_double2(dxr + dyi, dyr - dxi);
     }
-    ln[k] = o1;
-    if (k != kk) ln[kk] = o2;
+    ln[sidx(k)] = o1;
+    if (k != kk) ln[sidx(kk)] = o2;
   }
   __syncthreads();
   fft_lines<+1>(s_ln, ld, np, s_tw, pl);
@@ -257,7 +257,7 @@ __global__ void k_deriv(Grid g, int dir, const FftPlan* __restrict__ gpl, const 
   for (int e = threadIdx.x; e < np * n; e += blockDim.x) {
     const int L = e / n, x = e - L * n;
     const int ra = 2 * (p0 + L), rb = ra + 1;
-    const double2 v = s_ln[L * ld + x];
+    const double2 v = s_ln[L * ld + sidx(x)];
     du[ra * sline + x * selem] = v.x;
     if (rb < nrows) du[rb * sline + x * selem] = v.y;
   }
@@ -339,7 +339,7 @@ void diag_cl_energy(const DiagArgs& d, const void* u, double* scratch, double* h
 void diag_deriv(const Grid& g, int dir, const FftPlan* dplan, const double2* tw, const FftPlan& hplan, const double* u,
                 double* du, cudaStream_t s) {
   const int n = hplan.n;
-  const int ld = n + ((n % 2 == 0) ? 1 : 0);
+  const int ld = line_stride(n);
   const int nrows = dir == 0 ? g.ny : g.nx;
   const int pairs = (nrows + 1) / 2;
   int per = 8;

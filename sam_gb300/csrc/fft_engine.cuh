@@ -54,6 +54,34 @@ struct FftPlan {
 
 __device__ __forceinline__ int div_m(int b, const FftStage& s) { return (int)(((uint32_t)b * s.mmul) >> 21); }
 
+// Shared-memory position of element p of a line: one pad slot after every 8
+// elements, so the stride-p accesses of the late Stockham stages and the
+// column accesses of the transposing stores fall in distinct banks.
+__host__ __device__ __forceinline__ int sidx(int p) { return p + (p >> 3); }
+// Stride between consecutive lines (odd, so lines start in rotating banks).
+__host__ __device__ __forceinline__ int line_stride(int n) {
+  const int s = n + (n >> 3) + 1;
+  return s | 1;
+}
+
+// Exact unsigned division by a runtime divisor d >= 1 for n < 2^31
+// (round-up multiplier method): q = (umulhi(n, mul) + n) >> shift.
+struct FastDiv {
+  uint32_t d, mul, shift;
+};
+inline FastDiv make_fastdiv(uint32_t d) {
+  FastDiv f;
+  f.d = d;
+  uint32_t s = 0;
+  while ((1ull << s) < d) ++s;
+  f.shift = s;
+  f.mul = (uint32_t)(((1ull << 32) * ((1ull << s) - d)) / d + 1);
+  return f;
+}
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+  return (uint32_t)(((uint64_t)__umulhi(n, f.mul) + n) >> f.shift);
+}
+
 // ---- radix-p DFT kernels on registers (in place on a[0..P-1])
 template <int SIGN, typename C> __device__ __forceinline__ void dft2(C* a) {
   C t = a[1];
@@ -168,15 +196,15 @@ __device__ __forceinline__ void fft_stage(C* line, const C* __restrict__ tw, con
       const int f = div_m(b, s);
       const int k = b - f * s.m;
       fo[i] = f; ko[i] = k;
-      const C* src = line + f * s.m * P + k;
-      a[i][0] = src[0];
+      const int src = f * s.m * P + k;
+      a[i][0] = line[sidx(src)];
       if (s.l == 1) {
 #pragma unroll
-        for (int q = 1; q < P; ++q) a[i][q] = src[s.m * q];
+        for (int q = 1; q < P; ++q) a[i][q] = line[sidx(src + s.m * q)];
       } else {
         const C* w = tw + s.tw_off + f * (P - 1);
 #pragma unroll
-        for (int q = 1; q < P; ++q) a[i][q] = ctw<SIGN>(src[s.m * q], w[q - 1]);
+        for (int q = 1; q < P; ++q) a[i][q] = ctw<SIGN>(line[sidx(src + s.m * q)], w[q - 1]);
       }
     }
   }
@@ -186,10 +214,10 @@ __device__ __forceinline__ void fft_stage(C* line, const C* __restrict__ tw, con
     const int b = tl + i * TW;
     if (b < nb) {
       dftp<P, SIGN>(a[i]);
-      C* dst = line + fo[i] * s.m + ko[i];
+      const int dst = fo[i] * s.m + ko[i];
       const int os = s.l * s.m;
 #pragma unroll
-      for (int q = 0; q < P; ++q) dst[q * os] = a[i][q];
+      for (int q = 0; q < P; ++q) line[sidx(dst + q * os)] = a[i][q];
     }
   }
   team_sync(TW);

@@ -218,7 +218,7 @@ __global__ void k_get_mean(double2* __restrict__ col, int mz, int kz, int nz, in
   __shared__ double s_jump;
   load_plan(&pl, gpl);
   __syncthreads();
-  const int ld = nz + ((nz % 2 == 0) ? 1 : 0);
+  const int ld = line_stride(nz);
   double2* s_tw = reinterpret_cast<double2*>(smem_raw);
   double2* ln = s_tw + pl.tw_total;
   for (int e = threadIdx.x; e < pl.tw_total; e += blockDim.x) s_tw[e] = gtw[e];
@@ -231,37 +231,37 @@ __global__ void k_get_mean(double2* __restrict__ col, int mz, int kz, int nz, in
       if (p == 0) v = make_double2(col[0].x, 0.0);
       else if (p <= kz) v = col[p];
       else if (p >= nz - kz) v = make_double2(col[nz - p].x, -col[nz - p].y);
-      ln[p] = v;
+      ln[sidx(p)] = v;
     }
     __syncthreads();
     fft_lines<+1>(ln, ld, 1, s_tw, pl);
     __syncthreads();
     if (threadIdx.x == 0) {
-      const double m0 = ln[0].x, m1 = ln[1 % nz].x, m2 = ln[2 % nz].x;
-      const double l0 = ln[nz - 1].x, l1 = ln[(nz - 2 + nz) % nz].x, l2 = ln[(nz - 3 + nz) % nz].x;
+      const double m0 = ln[sidx(0)].x, m1 = ln[sidx(1 % nz)].x, m2 = ln[sidx(2 % nz)].x;
+      const double l0 = ln[sidx(nz - 1)].x, l1 = ln[sidx((nz - 2 + nz) % nz)].x, l2 = ln[sidx((nz - 3 + nz) % nz)].x;
       const double u_n = 3.0 * m0 - 3.0 * m1 + m2;
       const double u_1 = 3.0 * l0 - 3.0 * l1 + l2;
       const double jmp = 0.5 * ((l0 - u_n) + (u_1 - m0));
       if (pass == 0) s_jump = jmp;
       else s_jump = s_jump - jmp;
     }
-    for (int p = threadIdx.x; p < nz; p += blockDim.x) u_mean[p] = ln[p].x;
+    for (int p = threadIdx.x; p < nz; p += blockDim.x) u_mean[p] = ln[sidx(p)].x;
     __syncthreads();
     if (pass == 1 || i_remove != 1) break;
     // the linear profile jump (k/Nz - 1/2), rfftf, and its first kz_max+1
     // packed entries scaled by 1/Nz (get_mean.f:224-231)
     const double jump = s_jump;
     __syncthreads();
-    for (int p = threadIdx.x; p < nz; p += blockDim.x) ln[p] = make_double2(jump * ((double)p * nz_inv - 0.5), 0.0);
+    for (int p = threadIdx.x; p < nz; p += blockDim.x) ln[sidx(p)] = make_double2(jump * ((double)p * nz_inv - 0.5), 0.0);
     __syncthreads();
     fft_lines<-1>(ln, ld, 1, s_tw, pl);
     __syncthreads();
     if (threadIdx.x == 0) {
       // packed r(0) = X0, r(2k-1) = Re Xk, r(2k) = Im Xk (0-based)
       auto packed = [&](int idx) {
-        if (idx == 0) return ln[0].x;
+        if (idx == 0) return ln[sidx(0)].x;
         const int k = (idx + 1) / 2;
-        return (idx % 2 == 1) ? ln[k].x : ln[k].y;
+        return (idx % 2 == 1) ? ln[sidx(k)].x : ln[sidx(k)].y;
       };
       auto scaled = [&](int idx) { return idx <= kz ? packed(idx) * nz_inv : packed(idx); };
       col[0].x -= scaled(0);
@@ -321,7 +321,7 @@ void les_dm(const double* u, double* ub, double* q, double* part, double* cds, d
 
 void les_get_mean(double2* col, int mz, int kz, int nz, int i_remove, const FftPlan* dplan, const double2* tw,
                   const FftPlan& hplan, double* u_mean, double* jump, cudaStream_t s) {
-  const int ld = nz + ((nz % 2 == 0) ? 1 : 0);
+  const int ld = line_stride(nz);
   const size_t sm = sizeof(double2) * ((size_t)hplan.tw_total + (size_t)ld) + 16;
   k_get_mean<<<1, kThreads, sm, s>>>(col, mz, kz, nz, i_remove, dplan, tw, u_mean, jump);
 }

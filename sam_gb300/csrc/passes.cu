@@ -25,11 +25,36 @@ __device__ __forceinline__ void load_twiddles(cx_t<T>* s_tw, const cx_t<T>* __re
   for (int i = threadIdx.x; i < n; i += blockDim.x) s_tw[i] = g_tw[i];
 }
 
+// Element-wise tile copy with kBatch independent loads in flight per thread:
+// v = get(e) for a batch of e, then put(e, v) for the same batch.
+constexpr int kBatch = 8;
+
+// Resident CTAs per SM the register budget is sized for: two for FP64 (the
+// FP64 pipe needs the second CTA to cover load phases), three for FP32.
+template <typename T> struct MinBlocks { static constexpr int value = 2; };
+template <> struct MinBlocks<double> { static constexpr int value = 1; };
+template <typename V, typename Get, typename Put>
+__device__ __forceinline__ void batched(int count, Get get, Put put) {
+  for (int base = threadIdx.x; base < count; base += kBatch * blockDim.x) {
+    V v[kBatch];
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = base + u * blockDim.x;
+      if (e < count) v[u] = get(e);
+    }
+#pragma unroll
+    for (int u = 0; u < kBatch; ++u) {
+      const int e = base + u * blockDim.x;
+      if (e < count) put(e, v[u]);
+    }
+  }
+}
+
 // --------------------------------------------------------------- z inverse
 // Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
 // modes; output A(n, z, kx, ky) with ky fastest.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -48,21 +73,33 @@ __global__ void __launch_bounds__(kThreads) k_z_inv(ZInvArgs<T> a, const FftPlan
   const int nl = min(a.ty, my - j0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
   const C* src = a.in + (long long)n * a.in_n + (long long)i * a.in_kx + (long long)j0 * a.in_ky;
-  for (int e = threadIdx.x; e < nl * nz; e += blockDim.x) {
-    const int t = e / nz, p = e - t * nz;
-    C v = mk<C>((T)0, (T)0);
-    if (p <= km) v = src[(long long)t * a.in_ky + p];
-    else if (p >= nz - km) v = src[(long long)t * a.in_ky + p - (nz - mz)];
-    s_ln[t * ld + p] = v;
-  }
+  batched<C>(
+      nl * nz,
+      [&](int e) {
+        const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
+        C v = mk<C>((T)0, (T)0);
+        if (p <= km) v = src[(long long)t * a.in_ky + p];
+        else if (p >= nz - km) v = src[(long long)t * a.in_ky + p - (nz - mz)];
+        return v;
+      },
+      [&](int e, C v) {
+        const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
+        s_ln[t * ld + sidx(p)] = v;
+      });
   __syncthreads();
   fft_lines<+1>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)i * a.out_kx + j0;
-  for (int e = threadIdx.x; e < nl * nz; e += blockDim.x) {
-    const int z = e / nl, t = e - z * nl;
-    dst[(long long)z * a.out_z + t] = s_ln[t * ld + z];
-  }
+  batched<C>(
+      a.ty * nz,
+      [&](int e) {
+        const int z = (int)fdiv(e, a.fd_t), t = e - z * a.ty;
+        return t < nl ? s_ln[t * ld + sidx(z)] : mk<C>((T)0, (T)0);
+      },
+      [&](int e, C v) {
+        const int z = (int)fdiv(e, a.fd_t), t = e - z * a.ty;
+        if (t < nl) dst[(long long)z * a.out_z + t] = v;
+      });
 }
 
 // --------------------------------------------------------------- y inverse
@@ -70,7 +107,7 @@ __global__ void __launch_bounds__(kThreads) k_z_inv(ZInvArgs<T> a, const FftPlan
 // hold either Ny_min compact modes (zero band inserted here, as
 // x2z_decomp.f:111-124 does) or Ny values with the band already present.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -89,26 +126,34 @@ __global__ void __launch_bounds__(kThreads) k_y_inv(YInvArgs<T> a, const FftPlan
   const int nl = min(a.tx, mx - i0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
   const C* src = a.in + (long long)n * a.in_n + (long long)z * a.in_z + (long long)i0 * a.in_kx;
-  for (int e = threadIdx.x; e < nl * ny; e += blockDim.x) {
-    const int t = e / ny, p = e - t * ny;
-    C v;
-    if (a.in_full) {
-      v = src[(long long)t * a.in_kx + p];
-    } else {
-      v = mk<C>((T)0, (T)0);
-      if (p <= km) v = src[(long long)t * a.in_kx + p];
-      else if (p >= ny - km) v = src[(long long)t * a.in_kx + p - (ny - my)];
-    }
-    s_ln[t * ld + p] = v;
-  }
+  batched<C>(
+      nl * ny,
+      [&](int e) {
+        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
+        C v = mk<C>((T)0, (T)0);
+        if (a.in_full) v = src[(long long)t * a.in_kx + p];
+        else if (p <= km) v = src[(long long)t * a.in_kx + p];
+        else if (p >= ny - km) v = src[(long long)t * a.in_kx + p - (ny - my)];
+        return v;
+      },
+      [&](int e, C v) {
+        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
+        s_ln[t * ld + sidx(p)] = v;
+      });
   __syncthreads();
   fft_lines<+1>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)z * a.out_z + i0;
-  for (int e = threadIdx.x; e < nl * ny; e += blockDim.x) {
-    const int y = e / nl, t = e - y * nl;
-    dst[(long long)y * a.out_y + t] = s_ln[t * ld + y];
-  }
+  batched<C>(
+      a.tx * ny,
+      [&](int e) {
+        const int y = (int)fdiv(e, a.fd_t), t = e - y * a.tx;
+        return t < nl ? s_ln[t * ld + sidx(y)] : mk<C>((T)0, (T)0);
+      },
+      [&](int e, C v) {
+        const int y = (int)fdiv(e, a.fd_t), t = e - y * a.tx;
+        if (t < nl) dst[(long long)y * a.out_y + t] = v;
+      });
 }
 
 // ------------------------------------------------------------------ x pass
@@ -127,7 +172,7 @@ __device__ __forceinline__ void product_pair(int m, int& a, int& b) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -152,70 +197,90 @@ __global__ void __launch_bounds__(kThreads) k_x_pass(XPassArgs<T> a, const FftPl
     // spectral rows of B(n, z, y, kx): Hermitian half spectra with kx <= kx_max
     const int nband = nx - 2 * kmx - 1;
     for (int e = threadIdx.x; e < nin * yp * nband; e += blockDim.x) {
-      const int L = e / nband, p = e - L * nband;
-      s_in[L * ld + kmx + 1 + p] = mk<C>((T)0, (T)0);
+      const int L = (int)fdiv(e, a.fd_band), p = e - L * nband;
+      s_in[L * ld + sidx(kmx + 1 + p)] = mk<C>((T)0, (T)0);
     }
-    for (int e = threadIdx.x; e < nin * yp * mx; e += blockDim.x) {
-      const int L = e / mx, kx = e - L * mx;
-      const int f = L / yp, c = L - f * yp;
-      const int ya = y0 + 2 * c, yb = ya + 1;
-      const C* src = a.in + (long long)f * a.in_n + (long long)z * a.in_z;
-      C X = mk<C>((T)0, (T)0), Yv = mk<C>((T)0, (T)0);
-      if (ya < ny) X = src[(long long)ya * a.in_y + kx];
-      if (yb < ny) Yv = src[(long long)yb * a.in_y + kx];
-      if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
-        X.y = (T)0;
-        Yv.y = (T)0;
-      }
-      s_in[L * ld + kx] = mk<C>(X.x - Yv.y, X.y + Yv.x);
-      if (kx > 0) s_in[L * ld + nx - kx] = mk<C>(X.x + Yv.y, Yv.x - X.y);
-    }
+    // element e -> line L = (f, c) and kx; loads the two rows of the pair
+    struct Pair { C x, y; };
+    batched<Pair>(
+        nin * yp * mx,
+        [&](int e) {
+          const int L = (int)fdiv(e, a.fd_mx), kx = e - L * mx;
+          const int f = (int)fdiv(L, a.fd_yp), c = L - f * yp;
+          const int ya = y0 + 2 * c, yb = ya + 1;
+          const C* src = a.in + (long long)f * a.in_n + (long long)z * a.in_z;
+          Pair q;
+          q.x = ya < ny ? src[(long long)ya * a.in_y + kx] : mk<C>((T)0, (T)0);
+          q.y = yb < ny ? src[(long long)yb * a.in_y + kx] : mk<C>((T)0, (T)0);
+          return q;
+        },
+        [&](int e, Pair q) {
+          const int L = (int)fdiv(e, a.fd_mx), kx = e - L * mx;
+          C X = q.x, Yv = q.y;
+          if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
+            X.y = (T)0;
+            Yv.y = (T)0;
+          }
+          s_in[L * ld + sidx(kx)] = mk<C>(X.x - Yv.y, X.y + Yv.x);
+          if (kx > 0) s_in[L * ld + sidx(nx - kx)] = mk<C>(X.x + Yv.y, Yv.x - X.y);
+        });
     __syncthreads();
     fft_lines<+1>(s_in, ld, nin * yp, s_tw, pl);
   } else {
     // physical rows of P(n, z, y, x)
-    for (int e = threadIdx.x; e < nin * yp * nx; e += blockDim.x) {
-      const int L = e / nx, x = e - L * nx;
-      const int f = L / yp, c = L - f * yp;
-      const int ya = y0 + 2 * c, yb = ya + 1;
-      const T* src = a.in_phys + (long long)f * a.in_n + (long long)z * a.in_z;
-      T va = (T)0, vb = (T)0;
-      if (ya < ny) va = src[(long long)ya * a.in_y + x];
-      if (yb < ny) vb = src[(long long)yb * a.in_y + x];
-      s_in[L * ld + x] = mk<C>(va, vb);
-    }
+    struct Pair { T x, y; };
+    batched<Pair>(
+        nin * yp * nx,
+        [&](int e) {
+          const int L = (int)fdiv(e, a.fd_nx), x = e - L * nx;
+          const int f = (int)fdiv(L, a.fd_yp), c = L - f * yp;
+          const int ya = y0 + 2 * c, yb = ya + 1;
+          const T* src = a.in_phys + (long long)f * a.in_n + (long long)z * a.in_z;
+          Pair q;
+          q.x = ya < ny ? src[(long long)ya * a.in_y + x] : (T)0;
+          q.y = yb < ny ? src[(long long)yb * a.in_y + x] : (T)0;
+          return q;
+        },
+        [&](int e, Pair q) {
+          const int L = (int)fdiv(e, a.fd_nx), x = e - L * nx;
+          s_in[L * ld + sidx(x)] = mk<C>(q.x, q.y);
+        });
   }
   __syncthreads();
 
   // ---- vel_max partial sums (vel_max.f:158-168), FP64, deterministic order
   if (a.partials) {
     for (int f = 0; f < a.g.lu; ++f) {
-      double s1 = 0.0, s2 = 0.0, mxv = 0.0;
+      double s1 = 0.0, s2 = 0.0;
+      T mxv = (T)0;
       int bad = 0;
       for (int e = threadIdx.x; e < yp * nx; e += blockDim.x) {
-        const int c = e / nx, x = e - c * nx;
-        const C v = s_in[(f * yp + c) * ld + x];
+        const int c = (int)fdiv(e, a.fd_nx), x = e - c * nx;
+        const C v = s_in[(f * yp + c) * ld + sidx(x)];
         if (y0 + 2 * c < ny) {
           const double d = (double)v.x;
-          s1 += d; s2 += d * d; mxv = fmax(mxv, fabs(d));
-          bad |= !isfinite(d);
+          s1 += d; s2 += d * d;
+          mxv = fmax(mxv, fabs(v.x));
+          bad |= !isfinite(v.x);
         }
         if (y0 + 2 * c + 1 < ny) {
           const double d = (double)v.y;
-          s1 += d; s2 += d * d; mxv = fmax(mxv, fabs(d));
-          bad |= !isfinite(d);
+          s1 += d; s2 += d * d;
+          mxv = fmax(mxv, fabs(v.y));
+          bad |= !isfinite(v.y);
         }
       }
       // warp reduce then CTA reduce
+      double mxd = (double)mxv;
       for (int o = 16; o > 0; o >>= 1) {
         s1 += __shfl_xor_sync(0xffffffffu, s1, o);
         s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-        mxv = fmax(mxv, __shfl_xor_sync(0xffffffffu, mxv, o));
+        mxd = fmax(mxd, __shfl_xor_sync(0xffffffffu, mxd, o));
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
       }
       const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
       if ((threadIdx.x & 31) == 0) {
-        s_red[w * 4 + 0] = s1; s_red[w * 4 + 1] = s2; s_red[w * 4 + 2] = mxv; s_red[w * 4 + 3] = (double)bad;
+        s_red[w * 4 + 0] = s1; s_red[w * 4 + 1] = s2; s_red[w * 4 + 2] = mxd; s_red[w * 4 + 3] = (double)bad;
       }
       __syncthreads();
       if (threadIdx.x == 0) {
@@ -236,10 +301,10 @@ __global__ void __launch_bounds__(kThreads) k_x_pass(XPassArgs<T> a, const FftPl
   if (a.out_mode == 0) {
     // physical rows (xy_trans_b.f:117-119)
     for (int e = threadIdx.x; e < nin * Y * nx; e += blockDim.x) {
-      const int x = e % nx, r = e / nx;
-      const int yy = r % Y, f = r / Y;
+      const int r = (int)fdiv(e, a.fd_nx), x = e - r * nx;
+      const int f = (int)fdiv(r, a.fd_y), yy = r - f * Y;
       if (yy < yv) {
-        const C v = s_in[(f * yp + (yy >> 1)) * ld + x];
+        const C v = s_in[(f * yp + (yy >> 1)) * ld + sidx(x)];
         a.out_phys[(long long)f * a.out_pn + (long long)z * a.out_pz + (long long)(y0 + yy) * a.out_py + x] =
             (yy & 1) ? v.y : v.x;
       }
@@ -259,13 +324,13 @@ __global__ void __launch_bounds__(kThreads) k_x_pass(XPassArgs<T> a, const FftPl
     } else {
       // rhs.f:46-60 products of the physical lines
       for (int e = threadIdx.x; e < gm * yp * nx; e += blockDim.x) {
-        const int L = e / nx, x = e - L * nx;
-        const int gi = L / yp, c = L - gi * yp;
+        const int L = (int)fdiv(e, a.fd_nx), x = e - L * nx;
+        const int gi = (int)fdiv(L, a.fd_yp), c = L - gi * yp;
         int fa, fb;
         product_pair(m0 + gi, fa, fb);
-        const C va = s_in[(fa * yp + c) * ld + x];
-        const C vb = s_in[(fb * yp + c) * ld + x];
-        s_pr[L * ld + x] = mk<C>(va.x * vb.x, va.y * vb.y);
+        const C va = s_in[(fa * yp + c) * ld + sidx(x)];
+        const C vb = s_in[(fb * yp + c) * ld + sidx(x)];
+        s_pr[L * ld + sidx(x)] = mk<C>(va.x * vb.x, va.y * vb.y);
       }
       lines = s_pr;
       __syncthreads();
@@ -274,12 +339,12 @@ __global__ void __launch_bounds__(kThreads) k_x_pass(XPassArgs<T> a, const FftPl
     __syncthreads();
     // split the two real transforms, keep kx <= kx_max, scale, store C(m, z, kx, y)
     for (int e = threadIdx.x; e < gm * mx * Y; e += blockDim.x) {
-      const int yy = e % Y, r = e / Y;
-      const int kx = r % mx, gi = r / mx;
+      const int r = (int)fdiv(e, a.fd_y), yy = e - r * Y;
+      const int gi = (int)fdiv(r, a.fd_mx), kx = r - gi * mx;
       if (yy < yv) {
         const C* ln = lines + (gi * yp + (yy >> 1)) * ld;
-        const C z1 = ln[kx];
-        const C z2 = ln[kx == 0 ? 0 : nx - kx];
+        const C z1 = ln[sidx(kx)];
+        const C z2 = ln[sidx(kx == 0 ? 0 : nx - kx)];
         C v;
         if ((yy & 1) == 0) v = mk<C>((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
         else v = mk<C>((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
@@ -294,7 +359,7 @@ __global__ void __launch_bounds__(kThreads) k_x_pass(XPassArgs<T> a, const FftPl
 // Tile: field m, kx column i, planes z0 .. z0+TZ-1.  Output D(m, kx, ky, z)
 // keeps |ky| <= ky_max (xy_trans_f.f:45-52).
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -313,18 +378,137 @@ __global__ void __launch_bounds__(kThreads) k_y_fwd(YFwdArgs<T> a, const FftPlan
   const int nl = min(a.tz, nz - z0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
   const C* src = a.in + (long long)m * a.in_n + (long long)i * a.in_kx + (long long)z0 * a.in_z;
-  for (int e = threadIdx.x; e < nl * ny; e += blockDim.x) {
-    const int t = e / ny, p = e - t * ny;
-    s_ln[t * ld + p] = src[(long long)t * a.in_z + p];
-  }
+  batched<C>(
+      nl * ny,
+      [&](int e) {
+        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
+        return src[(long long)t * a.in_z + p];
+      },
+      [&](int e, C v) {
+        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
+        s_ln[t * ld + sidx(p)] = v;
+      });
   __syncthreads();
   fft_lines<-1>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)m * a.out_n + (long long)i * a.out_kx + z0;
-  for (int e = threadIdx.x; e < nl * my; e += blockDim.x) {
-    const int j = e / nl, t = e - j * nl;
-    dst[(long long)j * a.out_ky + t] = s_ln[t * ld + kpos(j, km, my, ny)];
+  batched<C>(
+      a.tz * my,
+      [&](int e) {
+        const int j = (int)fdiv(e, a.fd_t), t = e - j * a.tz;
+        return t < nl ? s_ln[t * ld + sidx(kpos(j, km, my, ny))] : mk<C>((T)0, (T)0);
+      },
+      [&](int e, C v) {
+        const int j = (int)fdiv(e, a.fd_t), t = e - j * a.tz;
+        if (t < nl) dst[(long long)j * a.out_ky + t] = v;
+      });
+}
+
+__device__ __forceinline__ double wexp(double x) { return exp(x); }
+__device__ __forceinline__ float wexp(float x) { return expf(x); }
+
+// rhs.f:108-142 for one mode (kx i, ky j, kz k) in working type W, then
+// (mode 2) sam.f:210-221 and 293-314.  ln points at field 0 of this mode in
+// shared memory; field f is at ln[f * fstride].
+template <typename W, typename T>
+__device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln, int fstride, int i, int j, int k,
+                                         double dt) {
+  using C = cx_t<T>;
+  const Grid& g = a.g;
+  const StageConsts& sc = a.sc;
+  const int nf = a.nf;
+  const W rkx = (W)(g.wave_x * (double)i);
+  const W rky = (W)(g.wave_y * (double)kwave(j, g.ky, g.my));
+  const W rkz = (W)(g.wave_z * (double)kwave(k, g.kz, g.mz));
+  const W rk_sq_raw = rkx * rkx + rky * rky + rkz * rkz;
+  const W rk_sq = rk_sq_raw > (W)1.0e-10 ? rk_sq_raw : (W)1.0e-10;
+  const W nz_inv = (W)(1.0 / (double)g.nz);
+  W tr[9], ti[9];
+#pragma unroll
+  for (int f = 0; f < 9; ++f) {
+    if (f < nf) {
+      const C v = ln[f * fstride];
+      tr[f] = (W)v.x * nz_inv;
+      ti[f] = (W)v.y * nz_inv;
+    } else {
+      tr[f] = (W)0; ti[f] = (W)0;
+    }
   }
+  // -i (a + i b) = b - i a
+  const W s1r = rkx * tr[0] + rky * tr[1] + rkz * tr[3], s1i = rkx * ti[0] + rky * ti[1] + rkz * ti[3];
+  const W s2r = rkx * tr[1] + rky * tr[2] + rkz * tr[4], s2i = rkx * ti[1] + rky * ti[2] + rkz * ti[4];
+  const W s3r = rkx * tr[3] + rky * tr[4] + rkz * tr[5], s3i = rkx * ti[3] + rky * ti[4] + rkz * ti[5];
+  W r1r = s1i, r1i = -s1r, r2r = s2i, r2i = -s2r, r3r = s3i, r3i = -s3r, r4r = (W)0, r4i = (W)0;
+  W u_r[4] = {0, 0, 0, 0}, u_i[4] = {0, 0, 0, 0};
+  const long long uidx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
+  if (a.mode == 2) {
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+      if (f < g.lu) {
+        const C v = a.u[(long long)f * a.u_n + uidx];
+        u_r[f] = (W)v.x;
+        u_i[f] = (W)v.y;
+      }
+  }
+  if (sc.i_strat) {
+    W wr, wi, thr, thi;
+    if (a.mode == 2) {
+      wr = u_r[2]; wi = u_i[2];
+      if (sc.rot_sav) {  // sam.f:180-181
+        wr = (W)sc.cos_theta * u_r[2] - (W)sc.sin_theta * u_r[0];
+        wi = (W)sc.cos_theta * u_i[2] - (W)sc.sin_theta * u_i[0];
+      }
+      thr = u_r[3]; thi = u_i[3];
+    } else {
+      const long long s = (long long)i * a.sav_kx + (long long)j * a.sav_ky + k;
+      const C w = a.usav[s];
+      const C th = a.usav[a.sav_n + s];
+      wr = (W)w.x; wi = (W)w.y; thr = (W)th.x; thi = (W)th.y;
+    }
+    r1r += (W)sc.buoy_fac_x * thr; r1i += (W)sc.buoy_fac_x * thi;
+    r3r += (W)sc.buoy_fac_z * thr; r3i += (W)sc.buoy_fac_z * thi;
+    const W s4r = rkx * tr[6] + rky * tr[7] + rkz * tr[8];
+    const W s4i = rkx * ti[6] + rky * ti[7] + rkz * ti[8];
+    r4r = s4i - (W)sc.lapse * wr;
+    r4i = -s4r - (W)sc.lapse * wi;
+  }
+  // p = -i (k . R) / k^2 ;  R -= i k p   (rhs.f:134-139)
+  const W qr = rkx * r1r + rky * r2r + rkz * r3r, qi = rkx * r1i + rky * r2i + rkz * r3i;
+  const W pr = qi / rk_sq, pim = -qr / rk_sq;
+  // -i rk p = rk * (p.i, -p.r)
+  r1r += rkx * pim; r1i -= rkx * pr;
+  r2r += rky * pim; r2i -= rky * pr;
+  r3r += rkz * pim; r3i -= rkz * pr;
+  const W rr[4] = {r1r, r2r, r3r, r4r}, ri[4] = {r1i, r2i, r3i, r4i};
+  if (a.mode == 1) {
+    const long long ridx = (long long)i * a.r_kx + (long long)j * a.r_ky + k;
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+      if (f < g.lu) a.r[(long long)f * a.r_n + ridx] = mk<C>((T)rr[f], (T)ri[f]);
+    a.r[(long long)g.lu * a.r_n + ridx] = mk<C>((T)pr, (T)pim);
+    return;
+  }
+  const W dt_fac1 = (W)(sc.gamma * dt), dt_fac2 = (W)(sc.zeta * dt);
+  const W vis_f = (W)(sc.vis * (sc.gamma * dt + sc.zeta * dt));
+  const long long ridx = uidx;
+  const W ef = wexp(-vis_f * rk_sq_raw);
+  const W et = sc.pr_inv == 1.0 ? ef : wexp(-(vis_f * (W)sc.pr_inv) * rk_sq_raw);
+#pragma unroll
+  for (int f = 0; f < 4; ++f)
+    if (f < g.lu) {
+      W ur = u_r[f], ui = u_i[f];
+      if (sc.nrk > 1) {  // sam.f:211-221
+        const C ro = a.r[(long long)f * a.u_n + ridx];
+        ur = ur + dt_fac2 * (W)ro.x;
+        ui = ui + dt_fac2 * (W)ro.y;
+      }
+      const W vf = f == 3 ? et : ef;  // sam.f:297
+      ur = (ur + dt_fac1 * rr[f]) * vf;
+      ui = (ui + dt_fac1 * ri[f]) * vf;
+      a.u[(long long)f * a.u_n + uidx] = mk<C>((T)ur, (T)ui);
+      a.r[(long long)f * a.u_n + ridx] = mk<C>((T)rr[f], (T)ri[f]);
+    }
+  if (sc.write_p) a.p[ridx] = mk<C>((T)pr, (T)pim);
 }
 
 // --------------------------------------------------------------- z forward
@@ -334,7 +518,7 @@ __global__ void __launch_bounds__(kThreads) k_y_fwd(YFwdArgs<T> a, const FftPlan
 //   mode 1: rhs epilogue (rhs.f:108-142) into r with u_sav from memory,
 //   mode 2: full stage epilogue: rhs, then sam.f:210-221 and 293-314.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -351,132 +535,47 @@ __global__ void __launch_bounds__(kThreads) k_z_fwd(ZFwdArgs<T> a, const FftPlan
   const int j0 = jt * a.ty;
   const int nl = min(a.ty, my - j0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
-  for (int e = threadIdx.x; e < nf * nl * nz; e += blockDim.x) {
-    const int p = e % nz, r = e / nz;
-    const int t = r % nl, f = r / nl;
-    s_ln[(f * nl + t) * ld + p] =
-        a.in[(long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky + p];
-  }
+  // lines of all nf fields for the nl rows of this tile, packed as f * nl + t
+  batched<C>(
+      nf * a.ty * nz,
+      [&](int e) {
+        const int r = (int)fdiv(e, a.fd_n), p = e - r * nz;
+        const int f = (int)fdiv(r, a.fd_t), t = r - f * a.ty;
+        return t < nl ? a.in[(long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky + p]
+                      : mk<C>((T)0, (T)0);
+      },
+      [&](int e, C v) {
+        const int r = (int)fdiv(e, a.fd_n), p = e - r * nz;
+        const int f = (int)fdiv(r, a.fd_t), t = r - f * a.ty;
+        if (t < nl) s_ln[(f * nl + t) * ld + sidx(p)] = v;
+      });
   __syncthreads();
   fft_lines<-1>(s_ln, ld, nf * nl, s_tw, pl);
   __syncthreads();
   const T nz_inv = (T)(1.0 / (double)nz);
   if (a.mode == 0) {
-    for (int e = threadIdx.x; e < nf * nl * mz; e += blockDim.x) {
-      const int k = e % mz, r = e / mz;
-      const int t = r % nl, f = r / nl;
-      C v = s_ln[(f * nl + t) * ld + kpos(k, km, mz, nz)];
+    for (int e = threadIdx.x; e < nf * a.ty * mz; e += blockDim.x) {
+      const int r = (int)fdiv(e, a.fd_m), k = e - r * mz;
+      const int f = (int)fdiv(r, a.fd_t), t = r - f * a.ty;
+      if (t >= nl) continue;
+      C v = s_ln[(f * nl + t) * ld + sidx(kpos(k, km, mz, nz))];
       v.x *= nz_inv;
       v.y *= nz_inv;
       a.in[(long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky + k] = v;
     }
     return;
   }
-  const StageConsts& sc = a.sc;
-  const double rkx = g.wave_x * (double)i;
-  const double rkx2 = rkx * rkx;
-  double dt = 0.0, dt_fac1 = 0.0, dt_fac2 = 0.0, vis_f = 0.0;
-  if (a.mode == 2) {
-    dt = a.state->dt;
-    dt_fac1 = sc.gamma * dt;
-    dt_fac2 = sc.zeta * dt;
-    vis_f = sc.vis * (dt_fac1 + dt_fac2);
-  }
+  double dt = 0.0;
+  if (a.mode == 2) dt = a.state->dt;
   for (int e = threadIdx.x; e < nl * mz; e += blockDim.x) {
-    const int k = e % mz, t = e / mz;
+    const int t = (int)fdiv(e, a.fd_m), k = e - t * mz;
     const int j = j0 + t;
-    const double rky = g.wave_y * (double)kwave(j, g.ky, my);
-    const double rk_sq2 = rkx2 + rky * rky;
-    const double rkz = g.wave_z * (double)kwave(k, km, mz);
-    const double rk_sq_raw = rk_sq2 + rkz * rkz;
-    const double rk_sq = fmax(rk_sq_raw, 1.0e-10);
-    const int pos = kpos(k, km, mz, nz);
-    double tr[9], ti[9];
-#pragma unroll
-    for (int f = 0; f < 9; ++f) {
-      if (f < nf) {
-        const C v = s_ln[(f * nl + t) * ld + pos];
-        tr[f] = (double)v.x * (double)nz_inv;
-        ti[f] = (double)v.y * (double)nz_inv;
-      } else {
-        tr[f] = 0.0; ti[f] = 0.0;
-      }
-    }
-    // -i (a + i b) = b - i a
-    double s1r = rkx * tr[0] + rky * tr[1] + rkz * tr[3], s1i = rkx * ti[0] + rky * ti[1] + rkz * ti[3];
-    double s2r = rkx * tr[1] + rky * tr[2] + rkz * tr[4], s2i = rkx * ti[1] + rky * ti[2] + rkz * ti[4];
-    double s3r = rkx * tr[3] + rky * tr[4] + rkz * tr[5], s3i = rkx * ti[3] + rky * ti[4] + rkz * ti[5];
-    double r1r = s1i, r1i = -s1r, r2r = s2i, r2i = -s2r, r3r = s3i, r3i = -s3r, r4r = 0.0, r4i = 0.0;
-    double u_r[4] = {0, 0, 0, 0}, u_i[4] = {0, 0, 0, 0};
-    const long long uidx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
-    if (a.mode == 2) {
-#pragma unroll
-      for (int f = 0; f < 4; ++f)
-        if (f < g.lu) {
-          const C v = a.u[(long long)f * a.u_n + uidx];
-          u_r[f] = (double)v.x;
-          u_i[f] = (double)v.y;
-        }
-    }
-    if (sc.i_strat) {
-      double wr, wi, thr, thi;
-      if (a.mode == 2) {
-        wr = u_r[2]; wi = u_i[2];
-        if (sc.rot_sav) {  // sam.f:180-181
-          wr = sc.cos_theta * u_r[2] - sc.sin_theta * u_r[0];
-          wi = sc.cos_theta * u_i[2] - sc.sin_theta * u_i[0];
-        }
-        thr = u_r[3]; thi = u_i[3];
-      } else {
-        const long long sidx = (long long)i * a.sav_kx + (long long)j * a.sav_ky + k;
-        const C w = a.usav[sidx];
-        const C th = a.usav[a.sav_n + sidx];
-        wr = (double)w.x; wi = (double)w.y; thr = (double)th.x; thi = (double)th.y;
-      }
-      r1r += sc.buoy_fac_x * thr; r1i += sc.buoy_fac_x * thi;
-      r3r += sc.buoy_fac_z * thr; r3i += sc.buoy_fac_z * thi;
-      const double s4r = rkx * tr[6] + rky * tr[7] + rkz * tr[8];
-      const double s4i = rkx * ti[6] + rky * ti[7] + rkz * ti[8];
-      r4r = s4i - sc.lapse * wr;
-      r4i = -s4r - sc.lapse * wi;
-    }
-    // p = -i (k . R) / k^2 ;  R -= i k p   (rhs.f:134-139)
-    const double qr = rkx * r1r + rky * r2r + rkz * r3r, qi = rkx * r1i + rky * r2i + rkz * r3i;
-    const double pr = qi / rk_sq, pim = -qr / rk_sq;
-    // -i rk p = rk * (p.i, -p.r)
-    r1r += rkx * pim; r1i -= rkx * pr;
-    r2r += rky * pim; r2i -= rky * pr;
-    r3r += rkz * pim; r3i -= rkz * pr;
-    const double rr[4] = {r1r, r2r, r3r, r4r}, ri[4] = {r1i, r2i, r3i, r4i};
-    if (a.mode == 1) {
-      const long long ridx = (long long)i * a.r_kx + (long long)j * a.r_ky + k;
-#pragma unroll
-      for (int f = 0; f < 4; ++f)
-        if (f < g.lu) a.r[(long long)f * a.r_n + ridx] = mk<C>((T)rr[f], (T)ri[f]);
-      a.r[(long long)g.lu * a.r_n + ridx] = mk<C>((T)pr, (T)pim);
-    } else {
-      const long long ridx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
-      const double ef = exp(-vis_f * rk_sq_raw);
-      const double et = sc.pr_inv == 1.0 ? ef : exp(-(vis_f * sc.pr_inv) * rk_sq_raw);
-#pragma unroll
-      for (int f = 0; f < 4; ++f)
-        if (f < g.lu) {
-          double ur = u_r[f], ui = u_i[f];
-          if (sc.nrk > 1) {  // sam.f:211-221
-            const C ro = a.r[(long long)f * a.u_n + ridx];
-            ur = ur + dt_fac2 * (double)ro.x;
-            ui = ui + dt_fac2 * (double)ro.y;
-          }
-          const double vf = f == 3 ? et : ef;  // sam.f:297
-          ur = (ur + dt_fac1 * rr[f]) * vf;
-          ui = (ui + dt_fac1 * ri[f]) * vf;
-          a.u[(long long)f * a.u_n + uidx] = mk<C>((T)ur, (T)ui);
-          a.r[(long long)f * a.u_n + ridx] = mk<C>((T)rr[f], (T)ri[f]);
-        }
-      if (sc.write_p) a.p[ridx] = mk<C>((T)pr, (T)pim);
-    }
+    const C* ln = s_ln + t * ld + sidx(kpos(k, km, mz, nz));
+    // the FP32 form keeps the mean (k = 0) mode in FP64
+    if (sizeof(T) == 4 && i == 0 && j == 0 && k == 0) epi_mode<double, T>(a, ln, nl * ld, i, j, k, dt);
+    else epi_mode<T, T>(a, ln, nl * ld, i, j, k, dt);
   }
-  if (a.mode == 2 && sc.last && blockIdx.x == 0 && threadIdx.x == 0) {
+  if (a.mode == 2 && a.sc.last && blockIdx.x == 0 && threadIdx.x == 0) {
     // sam.f:318 time = time + dt, once per step (no CTA of this launch reads
     // time, and none writes dt)
     a.state->time = a.state->time + dt;
@@ -555,13 +654,19 @@ __global__ void k_x2z(const double2* __restrict__ in, double2* __restrict__ out,
 
 // ------------------------------------------------------------ instantiation
 template <typename T>
-void launch_z_inv(const ZInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  ZInvArgs<T> a = a0;
+  a.fd_n = make_fastdiv(a.g.nz);
+  a.fd_t = make_fastdiv(a.ty);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.nvar * a.g.mx * nty;
   k_z_inv<T><<<grid, kThreads, smem, s>>>(a, pl);
 }
 template <typename T>
-void launch_y_inv(const YInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  YInvArgs<T> a = a0;
+  a.fd_n = make_fastdiv(a.g.ny);
+  a.fd_t = make_fastdiv(a.tx);
   const int ntx = (a.g.mx + a.tx - 1) / a.tx;
   const int grid = a.nvar * a.g.nz * ntx;
   k_y_inv<T><<<grid, kThreads, smem, s>>>(a, pl);
@@ -571,17 +676,31 @@ int x_pass_blocks(const XPassArgs<T>& a) {
   return a.g.nz * ((a.g.ny + a.yt - 1) / a.yt);
 }
 template <typename T>
-void launch_x_pass(const XPassArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  XPassArgs<T> a = a0;
+  const int nband = a.g.nx - 2 * a.g.kx - 1;
+  a.fd_band = make_fastdiv(nband > 0 ? nband : 1);
+  a.fd_mx = make_fastdiv(a.g.mx);
+  a.fd_yp = make_fastdiv(a.yt / 2);
+  a.fd_nx = make_fastdiv(a.g.nx);
+  a.fd_y = make_fastdiv(a.yt);
   k_x_pass<T><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
 }
 template <typename T>
-void launch_y_fwd(const YFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  YFwdArgs<T> a = a0;
+  a.fd_n = make_fastdiv(a.g.ny);
+  a.fd_t = make_fastdiv(a.tz);
   const int ntz = (a.g.nz + a.tz - 1) / a.tz;
   const int grid = a.nvar * a.g.mx * ntz;
   k_y_fwd<T><<<grid, kThreads, smem, s>>>(a, pl);
 }
 template <typename T>
-void launch_z_fwd(const ZFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s) {
+void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  ZFwdArgs<T> a = a0;
+  a.fd_n = make_fastdiv(a.g.nz);
+  a.fd_t = make_fastdiv(a.ty);
+  a.fd_m = make_fastdiv(a.g.mz);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.g.mx * nty;
   k_z_fwd<T><<<grid, kThreads, smem, s>>>(a, pl);

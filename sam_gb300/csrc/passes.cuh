@@ -14,6 +14,7 @@ struct ZInvArgs {
   int nvar, ty, ld;
   long long in_ky, in_kx, in_n;
   long long out_kx, out_z, out_n;
+  FastDiv fd_n, fd_t;  // filled by the launcher: Nz, ty
 };
 
 template <typename T>
@@ -25,6 +26,7 @@ struct YInvArgs {
   int nvar, tx, ld, in_full;
   long long in_kx, in_z, in_n;
   long long out_y, out_z, out_n;
+  FastDiv fd_n, fd_t;  // filled by the launcher: Ny, tx
 };
 
 template <typename T>
@@ -40,6 +42,7 @@ struct XPassArgs {
   long long in_y, in_z, in_n;
   long long out_kx, out_z, out_n;
   long long out_py, out_pz, out_pn;
+  FastDiv fd_band, fd_mx, fd_yp, fd_nx, fd_y;  // filled by the launcher
 };
 
 template <typename T>
@@ -51,6 +54,7 @@ struct YFwdArgs {
   int nvar, tz, ld;
   long long in_kx, in_z, in_n;
   long long out_ky, out_kx, out_n;
+  FastDiv fd_n, fd_t;  // filled by the launcher: Ny, tz
 };
 
 template <typename T>
@@ -71,6 +75,7 @@ struct ZFwdArgs {
   long long u_ky, u_kx, u_n;
   DevState* state;
   StageConsts sc;
+  FastDiv fd_n, fd_t, fd_m;  // filled by the launcher: Nz, ty, Nz_min
 };
 
 template <typename T> void launch_z_inv(const ZInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);

@@ -159,7 +159,7 @@ static int ensure(Scratch& s, size_t bytes) {
 
 static size_t csize(const Ctx& c) { return c.cfg.precision == 32 ? sizeof(float2) : sizeof(double2); }
 
-static int line_ld(int n) { return n + ((n % 2 == 0) ? 1 : 0); }
+static int line_ld(int n) { return line_stride(n); }
 
 // shared memory of a tile of `lines` lines of length n plus the twiddles
 static size_t tile_smem(const Plan& P, int lines, size_t es) {
@@ -218,9 +218,12 @@ static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
   const size_t red = sizeof(double) * 4 * (kThreads / 32) + 64;
   yt = c.yt_x;
   grp = out_mode == 2 ? c.grp_x : 0;
+  // FP32 tiles leave room for two CTAs per SM; FP64 CTAs are register-bound
+  // to one per SM and take the whole budget
+  const size_t budget = sizeof(T) == 4 ? kSmemMax / 2 - 1024 : kSmemMax;
   for (;;) {
     const int lines = (nin + grp) * (yt / 2);
-    if (tile_smem(c.px, lines, es) + red <= kSmemMax) break;
+    if (tile_smem(c.px, lines, es) + red <= budget) break;
     if (grp > 1) { grp = (grp + 1) / 2; continue; }
     if (yt > 2) { yt /= 2; continue; }
     return fail(SAM_GPU_EINVAL, "x pass does not fit in shared memory (Nx=%d)", c.g.nx);
