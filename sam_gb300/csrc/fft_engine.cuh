@@ -48,9 +48,17 @@ struct FftPlan {
   int n;
   int nst;
   int tw_total;
-  int team;  // lanes per line
+  int team;     // threads per line in FP64 (at most 8 values per thread)
+  int team_sp;  // threads per line in FP32 (at most 16 values per thread)
   FftStage st[10];
 };
+
+// Values a thread holds per stage (8 complex: 16 in FP32 spills registers
+// with five radices compiled into each stage loop).
+template <typename C> struct Emax { static constexpr int value = 8; };
+template <typename C> __device__ __forceinline__ int team_of(const FftPlan& pl) {
+  return sizeof(C) <= 8 ? pl.team_sp : pl.team;
+}
 
 __device__ __forceinline__ int div_m(int b, const FftStage& s) { return (int)(((uint32_t)b * s.mmul) >> 21); }
 
@@ -181,10 +189,16 @@ __device__ __forceinline__ void team_sync(int TW) {
   }
 }
 
-template <int P, int SIGN, typename C>
+// Reads element idx of the line being transformed (the stage's input).
+template <typename C> struct LineLoad {
+  const C* line;
+  __device__ __forceinline__ C operator()(int idx) const { return line[sidx(idx)]; }
+};
+
+template <int P, int SIGN, typename C, typename Ld>
 __device__ __forceinline__ void fft_stage(C* line, const C* __restrict__ tw, const FftStage& s, int n, int tl,
-                                          int TW) {
-  constexpr int MAXB = 8 / P;
+                                          int TW, Ld load) {
+  constexpr int MAXB = Emax<C>::value / P;
   const int nb = n / P;
   C a[MAXB][P];
   int fo[MAXB], ko[MAXB];
@@ -197,14 +211,14 @@ __device__ __forceinline__ void fft_stage(C* line, const C* __restrict__ tw, con
       const int k = b - f * s.m;
       fo[i] = f; ko[i] = k;
       const int src = f * s.m * P + k;
-      a[i][0] = line[sidx(src)];
+      a[i][0] = load(src);
       if (s.l == 1) {
 #pragma unroll
-        for (int q = 1; q < P; ++q) a[i][q] = line[sidx(src + s.m * q)];
+        for (int q = 1; q < P; ++q) a[i][q] = load(src + s.m * q);
       } else {
         const C* w = tw + s.tw_off + f * (P - 1);
 #pragma unroll
-        for (int q = 1; q < P; ++q) a[i][q] = ctw<SIGN>(line[sidx(src + s.m * q)], w[q - 1]);
+        for (int q = 1; q < P; ++q) a[i][q] = ctw<SIGN>(load(src + s.m * q), w[q - 1]);
       }
     }
   }
@@ -225,21 +239,38 @@ __device__ __forceinline__ void fft_stage(C* line, const C* __restrict__ tw, con
 
 // Full transform of one line (all threads of the team call this together;
 // a team with no line passes active=false and still synchronises).
+template <int SIGN, typename C, typename Ld>
+__device__ __forceinline__ void fft_stage_p(C* line, const C* __restrict__ tw, const FftStage& st, int n, int tl,
+                                            int TW, Ld load) {
+  switch (st.p) {
+    case 8: fft_stage<8, SIGN>(line, tw, st, n, tl, TW, load); break;
+    case 4: fft_stage<4, SIGN>(line, tw, st, n, tl, TW, load); break;
+    case 2: fft_stage<2, SIGN>(line, tw, st, n, tl, TW, load); break;
+    case 3: fft_stage<3, SIGN>(line, tw, st, n, tl, TW, load); break;
+    default: fft_stage<5, SIGN>(line, tw, st, n, tl, TW, load); break;
+  }
+}
+
+// Full transform of one line (all threads of the team call this together;
+// a team with no line passes active=false and still synchronises).
 template <int SIGN, typename C>
 __device__ __forceinline__ void fft_line(C* line, const C* __restrict__ tw, const FftPlan& pl, int tl, bool active) {
   const int n = pl.n;
-  const int TW = pl.team;
-  for (int s = 0; s < pl.nst; ++s) {
-    const FftStage& st = pl.st[s];
-    const int tla = active ? tl : (1 << 20);  // inactive lanes own no butterfly
-    switch (st.p) {
-      case 8: fft_stage<8, SIGN>(line, tw, st, n, tla, TW); break;
-      case 4: fft_stage<4, SIGN>(line, tw, st, n, tla, TW); break;
-      case 2: fft_stage<2, SIGN>(line, tw, st, n, tla, TW); break;
-      case 3: fft_stage<3, SIGN>(line, tw, st, n, tla, TW); break;
-      default: fft_stage<5, SIGN>(line, tw, st, n, tla, TW); break;
-    }
-  }
+  const int TW = team_of<C>(pl);
+  const int tla = active ? tl : (1 << 20);  // inactive lanes own no butterfly
+  for (int s = 0; s < pl.nst; ++s) fft_stage_p<SIGN>(line, tw, pl.st[s], n, tla, TW, LineLoad<C>{line});
+}
+
+// As fft_line, but the first stage reads its inputs through first(idx), so a
+// caller can form the line on the fly (e.g. the product of two other lines).
+template <int SIGN, typename C, typename First>
+__device__ __forceinline__ void fft_line_from(C* line, const C* __restrict__ tw, const FftPlan& pl, int tl,
+                                              bool active, First first) {
+  const int n = pl.n;
+  const int TW = team_of<C>(pl);
+  const int tla = active ? tl : (1 << 20);
+  fft_stage_p<SIGN>(line, tw, pl.st[0], n, tla, TW, first);
+  for (int s = 1; s < pl.nst; ++s) fft_stage_p<SIGN>(line, tw, pl.st[s], n, tla, TW, LineLoad<C>{line});
 }
 
 // Transform `nlines` lines of a CTA's shared-memory tile.  Line L starts at
@@ -247,7 +278,7 @@ __device__ __forceinline__ void fft_line(C* line, const C* __restrict__ tw, cons
 template <int SIGN, typename C>
 __device__ __forceinline__ void fft_lines(C* base, int ld, int nlines, const C* __restrict__ tw, const FftPlan& pl) {
   if (pl.n == 1) return;
-  const int TW = pl.team;
+  const int TW = team_of<C>(pl);
   const int nteams = blockDim.x / TW;
   const int team = threadIdx.x / TW;
   const int tl = threadIdx.x - team * TW;
@@ -256,6 +287,29 @@ __device__ __forceinline__ void fft_lines(C* base, int ld, int nlines, const C* 
     const int L = r * nteams + team;
     const bool active = L < nlines;
     fft_line<SIGN>(base + (active ? L : 0) * ld, tw, pl, tl, active);
+  }
+}
+
+// As fft_lines, with the first stage of line L reading through the loader
+// first(L) returns (a functor idx -> value).  A length-1 transform is the
+// identity: the inputs are only copied into place.
+template <int SIGN, typename C, typename First>
+__device__ __forceinline__ void fft_lines_from(C* base, int ld, int nlines, const C* __restrict__ tw,
+                                               const FftPlan& pl, First first) {
+  if (pl.n == 1 || pl.nst == 0) {
+    for (int L = threadIdx.x; L < nlines; L += blockDim.x) base[L * ld] = first(L)(0);
+    return;
+  }
+  const int TW = team_of<C>(pl);
+  const int nteams = blockDim.x / TW;
+  const int team = threadIdx.x / TW;
+  const int tl = threadIdx.x - team * TW;
+  const int rounds = (nlines + nteams - 1) / nteams;
+  for (int r = 0; r < rounds; ++r) {
+    const int L = r * nteams + team;
+    const bool active = L < nlines;
+    const int Lc = active ? L : 0;
+    fft_line_from<SIGN>(base + Lc * ld, tw, pl, tl, active, first(Lc));
   }
 }
 

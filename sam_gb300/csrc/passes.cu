@@ -156,6 +156,30 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_y_inv(YInvArg
       });
 }
 
+// Two adjacent complex values in one store (one 16-byte store in FP32, two in
+// FP64); o must be aligned to twice the element size.
+__device__ __forceinline__ void store_pair(float2* o, float2 a, float2 b) {
+  *reinterpret_cast<float4*>(o) = make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ void store_pair(double2* o, double2 a, double2 b) {
+  o[0] = a;
+  o[1] = b;
+}
+
+// First-stage loader of the forward x transform: element idx of line a, or,
+// when b is given, of line a times line b component by component (the two
+// real rows of a pair multiply separately), i.e. a product line of rhs.f.
+template <typename C> struct ProductLoad {
+  const C* a;
+  const C* b;
+  __device__ __forceinline__ C operator()(int idx) const {
+    const C va = a[sidx(idx)];
+    if (!b) return va;
+    const C vb = b[sidx(idx)];
+    return mk<C>(va.x * vb.x, va.y * vb.y);
+  }
+};
+
 // ------------------------------------------------------------------ x pass
 // Tile: plane z, rows y0 .. y0+Y-1 (Y even).  Two real x-lines (rows y0+2c
 // and y0+2c+1 of the same field) share one complex line: x + i y.
@@ -318,37 +342,39 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_x_pass(XPassA
   const int gstep = a.out_mode == 1 ? nin : max(a.group, 1);
   for (int m0 = 0; m0 < nout; m0 += gstep) {
     const int gm = min(gstep, nout - m0);
-    C* lines;
-    if (a.out_mode == 1) {
-      lines = s_in + m0 * yp * ld;
-    } else {
-      // rhs.f:46-60 products of the physical lines
-      for (int e = threadIdx.x; e < gm * yp * nx; e += blockDim.x) {
-        const int L = (int)fdiv(e, a.fd_nx), x = e - L * nx;
-        const int gi = (int)fdiv(L, a.fd_yp), c = L - gi * yp;
-        int fa, fb;
-        product_pair(m0 + gi, fa, fb);
-        const C va = s_in[(fa * yp + c) * ld + sidx(x)];
-        const C vb = s_in[(fb * yp + c) * ld + sidx(x)];
-        s_pr[L * ld + sidx(x)] = mk<C>(va.x * vb.x, va.y * vb.y);
-      }
-      lines = s_pr;
-      __syncthreads();
-    }
-    fft_lines<-1>(lines, ld, gm * yp, s_tw, pl);
+    // out_mode 1: the input lines in place; out_mode 2 (rhs.f:46-60): the
+    // products of the physical lines, formed while the first FFT stage loads
+    // them, straight into the product lines
+    C* lines = a.out_mode == 1 ? s_in + m0 * yp * ld : s_pr;
+    fft_lines_from<-1>(lines, ld, gm * yp, s_tw, pl, [&](int L) {
+      if (a.out_mode == 1) return ProductLoad<C>{lines + L * ld, nullptr};
+      const int gi = L / yp, c = L - gi * yp;
+      int fa, fb;
+      product_pair(m0 + gi, fa, fb);
+      return ProductLoad<C>{s_in + (fa * yp + c) * ld, s_in + (fb * yp + c) * ld};
+    });
     __syncthreads();
-    // split the two real transforms, keep kx <= kx_max, scale, store C(m, z, kx, y)
-    for (int e = threadIdx.x; e < gm * mx * Y; e += blockDim.x) {
-      const int r = (int)fdiv(e, a.fd_y), yy = e - r * Y;
+    // split the two real transforms, keep kx <= kx_max, scale, store
+    // C(m, z, kx, y): one thread writes the two rows y0+2c, y0+2c+1 of a pair
+    C* out_z = a.out + (long long)z * a.out_z + y0;
+    for (int e = threadIdx.x; e < gm * mx * yp; e += blockDim.x) {
+      const int r = (int)fdiv(e, a.fd_yp), c = e - r * yp;
       const int gi = (int)fdiv(r, a.fd_mx), kx = r - gi * mx;
-      if (yy < yv) {
-        const C* ln = lines + (gi * yp + (yy >> 1)) * ld;
-        const C z1 = ln[sidx(kx)];
-        const C z2 = ln[sidx(kx == 0 ? 0 : nx - kx)];
-        C v;
-        if ((yy & 1) == 0) v = mk<C>((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
-        else v = mk<C>((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
-        a.out[(long long)(m0 + gi) * a.out_n + (long long)z * a.out_z + (long long)kx * a.out_kx + y0 + yy] = v;
+      const C* ln = lines + (gi * yp + c) * ld;
+      const C z1 = ln[sidx(kx)];
+      const C z2 = ln[sidx(kx == 0 ? 0 : nx - kx)];
+      const C ve = mk<C>((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
+      const C vo = mk<C>((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
+      C* o = out_z + (long long)(m0 + gi) * a.out_n + (unsigned)kx * (unsigned)a.out_kx + 2 * c;
+      if (2 * c + 1 < yv) {
+        if ((reinterpret_cast<uintptr_t>(o) & (2 * sizeof(C) - 1)) == 0) {
+          store_pair(o, ve, vo);
+        } else {  // odd Ny: the pair straddles a vector boundary
+          o[0] = ve;
+          o[1] = vo;
+        }
+      } else if (2 * c < yv) {
+        o[0] = ve;
       }
     }
     __syncthreads();

@@ -61,19 +61,24 @@ static int build_plan(int n, Plan& P) {
   while (r % 5 == 0) { fac[ns++] = 5; r /= 5; }
   if (r != 1 || ns > 10 || n > 1024) return fail(SAM_GPU_EINVAL, "FFT length %d must be 2^a 3^b 5^c <= 1024", n);
   pl.nst = ns;
-  int TW = 1;
-  while (TW * 8 < n) TW *= 2;
-  for (;;) {
-    bool ok = true;
-    for (int s = 0; s < ns; ++s) {
-      const int nb = n / fac[s];
-      if ((nb + TW - 1) / TW > 8 / fac[s]) ok = false;
+  // team width: a power of two such that no thread holds more than emax
+  // values in any stage (Emax in fft_engine.cuh)
+  auto team_for = [&](int emax) {
+    int TW = 1;
+    while (TW * emax < n) TW *= 2;
+    for (;;) {
+      bool ok = true;
+      for (int s = 0; s < ns; ++s) {
+        const int nb = n / fac[s];
+        if ((nb + TW - 1) / TW > emax / fac[s]) ok = false;
+      }
+      if (ok) return TW;
+      TW *= 2;
     }
-    if (ok) break;
-    TW *= 2;
-  }
-  if (TW > kThreads) return fail(SAM_GPU_EINVAL, "FFT length %d needs too wide a team", n);
-  pl.team = TW;
+  };
+  pl.team = team_for(8);
+  pl.team_sp = team_for(8);
+  if (pl.team > kThreads) return fail(SAM_GPU_EINVAL, "FFT length %d needs too wide a team", n);
   std::vector<double2> t64;
   std::vector<float2> t32;
   int l = 1, off = 0;
