@@ -173,6 +173,21 @@ int sam_gpu_div_check(double* out4);
 /* cl_energy.f:1 */
 int sam_gpu_cl_energy(double* e_cl);
 
+/* force.f:1  rescale the shells 1..k_force+1 of the resident velocity back
+ * to the initial shell energies ek_0 (spectra's ek of step 0) */
+int sam_gpu_force(const double* ek_0, int k_force);
+
+/* ---- restart files of the resident state ---- */
+/* write_field.f:1 / read_field.f:1  vel.NNNNNN: Lu*Nx_min records of
+ * Nz_min x Ny_min complex128; read_field rejects a file of the wrong size */
+int sam_gpu_write_field(const char* fname);
+int sam_gpu_read_field(const char* fname);
+/* write_header.f:1 / read_header.f:1  header.NNNNNN: "label value" lines;
+ * reading checks the restart-fixed parameters (box, grid, i_strat) against
+ * the configuration, restores time and dt, and returns nt */
+int sam_gpu_write_header(const char* fname, int nt);
+int sam_gpu_read_header(const char* fname, int* nt);
+
 /* ---- initial fields on the device (written to the resident state) ---- */
 int sam_gpu_init_taylor_green(void);
 int sam_gpu_init_random(unsigned long long seed, int kind_u, double flct_u, int kind_t, double flct_t);

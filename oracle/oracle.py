@@ -96,6 +96,9 @@ def lib():
         _lib.so_init_packet.argtypes = [P, P, C.c_ulonglong, C.c_int, C.c_int, C.c_int,
                                         C.c_double, C.c_double, C.c_double]
         _lib.so_fft_line.argtypes = [C.c_int, C.c_int, P]
+        _lib.so_force.argtypes = [P, P, P, C.c_int]
+        _lib.so_write_field.argtypes = [P, C.c_char_p, P]
+        _lib.so_read_field.argtypes = [P, C.c_char_p, P]
     return _lib
 
 
@@ -283,6 +286,19 @@ class Oracle:
         vt = np.zeros((d.nx + 2, d.ny + 2, d.nz + 2), order="F")
         cds = lib().so_dm(self.h, _p(u), _p(vt))
         return vt, cds
+
+    # ---- forcing and restart files
+    def force(self, u, ek_0, k_force):
+        lib().so_force(self.h, _p(u), _p(np.ascontiguousarray(ek_0, dtype=np.float64)), k_force)
+        return u
+
+    def write_field(self, fname, u):
+        assert lib().so_write_field(self.h, fname.encode(), _p(u)) == 0
+
+    def read_field(self, fname):
+        u = self.wave(self.d.lu)
+        rc = lib().so_read_field(self.h, fname.encode(), _p(u))
+        return u if rc == 0 else rc
 
     # ---- initial fields
     def init_taylor_green(self):

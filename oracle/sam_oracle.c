@@ -16,6 +16,7 @@
 
 #include <math.h>
 #include <stdint.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -1127,4 +1128,83 @@ int so_fft_line(int n, int kind, double *data) {
   }
   free(work);
   return rc;
+}
+
+/* ------------------------------------------------------ forcing and restart */
+
+/* force.f:12-63 */
+int so_force(so_ctx *c, double *ud, const double *ek_0, int k_force) {
+  so_cplx *u = (so_cplx *)ud;
+  double *work = (double *)calloc((size_t)k_force + 2, sizeof(double));
+  for (int i = 0; i < c->nx_min; ++i) {
+    int kx2 = c->k_x[i] * c->k_x[i];
+    for (int j = 0; j < c->ny_min; ++j) {
+      int k_sq2 = kx2 + c->k_y[j] * c->k_y[j];
+      for (int k = 0; k < c->nz_min; ++k) {
+        double factor = (i == 0 || i == c->nx2) ? 1.0 : 2.0;
+        int k_sq = k_sq2 + c->k_z[k] * c->k_z[k];
+        int is = (int)(sqrt((double)k_sq) + 0.5);
+        if (is <= k_force) {
+          double u_sq = 0.0;
+          for (int n = 0; n < 3; ++n) {
+            so_cplx v = u[W_IDX(c, k, j, i, n)];
+            u_sq += creal(v * conj(v));
+          }
+          work[is] += factor * u_sq;
+        }
+      }
+    }
+  }
+  double *fac = (double *)calloc((size_t)k_force + 2, sizeof(double));
+  fac[0] = 1.0;
+  for (int is = 1; is <= k_force; ++is) fac[is] = sqrt(ek_0[is] / work[is]);
+  for (int i = 0; i < c->nx_min; ++i) {
+    int kx2 = c->k_x[i] * c->k_x[i];
+    for (int j = 0; j < c->ny_min; ++j) {
+      int k_sq2 = kx2 + c->k_y[j] * c->k_y[j];
+      for (int k = 0; k < c->nz_min; ++k) {
+        int is = (int)(sqrt((double)(k_sq2 + c->k_z[k] * c->k_z[k])) + 0.5);
+        if (is <= k_force)
+          for (int n = 0; n < 3; ++n) u[W_IDX(c, k, j, i, n)] *= fac[is];
+      }
+    }
+  }
+  free(work);
+  free(fac);
+  return 0;
+}
+
+/* write_field.f:12-30: record ((n-1) Nx_min + ii-1) holds u(1:Nz_min,1:Ny_min,ii,n) */
+int so_write_field(so_ctx *c, const char *fname, const double *ud) {
+  const so_cplx *u = (const so_cplx *)ud;
+  FILE *f = fopen(fname, "wb");
+  if (!f) return -1;
+  for (int n = 0; n < c->lu; ++n)
+    for (int i = 0; i < c->nx_min; ++i)
+      for (int j = 0; j < c->ny_min; ++j) fwrite(u + W_IDX(c, 0, j, i, n), sizeof(so_cplx), (size_t)c->nz_min, f);
+  fclose(f);
+  return 0;
+}
+
+/* read_field.f:61-100: size check, then the records; rows above Nz_min zeroed */
+int so_read_field(so_ctx *c, const char *fname, double *ud) {
+  so_cplx *u = (so_cplx *)ud;
+  FILE *f = fopen(fname, "rb");
+  if (!f) return -1;
+  fseek(f, 0, SEEK_END);
+  long found = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  long expect = (long)sizeof(so_cplx) * c->nz_min * c->ny_min * c->nx_min * c->lu;
+  if (found != expect) { fclose(f); return -2; }
+  for (int n = 0; n < c->lu; ++n)
+    for (int i = 0; i < c->nx_min; ++i)
+      for (int j = 0; j < c->ny_min; ++j) {
+        if (fread(u + W_IDX(c, 0, j, i, n), sizeof(so_cplx), (size_t)c->nz_min, f) != (size_t)c->nz_min) {
+          fclose(f);
+          return -3;
+        }
+        for (int k = c->nz_min; k < c->nze; ++k) u[W_IDX(c, k, j, i, n)] = 0;
+      }
+  fclose(f);
+  return 0;
 }

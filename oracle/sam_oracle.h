@@ -105,6 +105,12 @@ int so_init_gw_plane(so_ctx *c, double *u, double amplitude, double lambda_x, do
 int so_init_packet(so_ctx *c, double *u, unsigned long long seed, int kx0, int ky0, int kz0,
                    double sigma, double amplitude, double noise);
 
+/* ---- forcing and restart files ---- */
+int so_force(so_ctx *c, double *u, const double *ek_0, int k_force);
+int so_write_field(so_ctx *c, const char *fname, const double *u);
+/* 0 ok, -1 open, -2 wrong size (read_field.f:74-80), -3 short read */
+int so_read_field(so_ctx *c, const char *fname, double *u);
+
 /* ---- one raw FFTPACK-convention transform (0 cfftf, 1 cfftb, 2 rfftf, 3 rfftb) ---- */
 int so_fft_line(int n, int kind, double *data);
 

@@ -263,6 +263,68 @@ __global__ void k_deriv(Grid g, int dir, const FftPlan* __restrict__ gpl, const 
   }
 }
 
+// force.f:12-63: shells 1..k_force+1 (1-based) keep the energy ek0 they had
+// initially.  The forced modes lie in the box |kx|,|ky|,|kz| <= k_force, which
+// one thread visits in the reference's loop order (kx, then ky, then kz in
+// storage order), so the shell sums are summed as force.f sums them.
+template <typename T>
+__global__ void k_force_shells(DiagArgs d, void* uv, const double* __restrict__ ek0, int k_force) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  using C = cx_t<T>;
+  C* u = reinterpret_cast<C*>(uv);
+  const Grid& g = d.g;
+  const long long nm = (long long)g.mx * g.my * g.mz;
+  double work[64], fac[64];
+  const int ns = k_force + 1;
+  for (int s = 0; s < ns; ++s) work[s] = 0.0;
+  const int ix_end = min(k_force, g.mx - 1);
+  for (int i = 0; i <= ix_end; ++i) {
+    const double factor = (i == 0 || i == d.nx2) ? 1.0 : 2.0;
+    for (int j = 0; j < g.my; ++j) {
+      const int iy = kwave(j, g.ky, g.my);
+      if (iy > k_force || iy < -k_force) continue;
+      for (int k = 0; k < g.mz; ++k) {
+        const int iz = kwave(k, g.kz, g.mz);
+        if (iz > k_force || iz < -k_force) continue;
+        const int is = (int)(sqrt((double)(i * i + iy * iy + iz * iz)) + 0.5);
+        if (is > k_force) continue;
+        const long long e = ((long long)i * g.my + j) * g.mz + k;
+        double usq = 0.0;
+        for (int n = 0; n < 3; ++n) {
+          const C v = u[n * nm + e];
+          usq += (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+        }
+        work[is] += factor * usq;
+      }
+    }
+  }
+  fac[0] = 1.0;
+  for (int s = 1; s < ns; ++s) fac[s] = sqrt(ek0[s] / work[s]);
+  for (int i = 0; i <= ix_end; ++i)
+    for (int j = 0; j < g.my; ++j) {
+      const int iy = kwave(j, g.ky, g.my);
+      if (iy > k_force || iy < -k_force) continue;
+      for (int k = 0; k < g.mz; ++k) {
+        const int iz = kwave(k, g.kz, g.mz);
+        if (iz > k_force || iz < -k_force) continue;
+        const int is = (int)(sqrt((double)(i * i + iy * iy + iz * iz)) + 0.5);
+        if (is > k_force) continue;
+        const long long e = ((long long)i * g.my + j) * g.mz + k;
+        for (int n = 0; n < 3; ++n) {
+          C v = u[n * nm + e];
+          v.x = (T)((double)v.x * fac[is]);
+          v.y = (T)((double)v.y * fac[is]);
+          u[n * nm + e] = v;
+        }
+      }
+    }
+}
+
+void diag_force(const DiagArgs& d, void* u, const double* ek0_dev, int k_force, cudaStream_t s) {
+  if (d.precision == 32) k_force_shells<float><<<1, 32, 0, s>>>(d, u, ek0_dev, k_force);
+  else k_force_shells<double><<<1, 32, 0, s>>>(d, u, ek0_dev, k_force);
+}
+
 // FP64 FMA throughput probe: 8 independent dependency chains per thread.
 __global__ void k_dfma(double* out, int iters, double a, double b) {
   double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3, x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6,

@@ -10,6 +10,9 @@ struct DiagArgs {
 };
 DiagArgs diag_args(const Grid& g, int lm, int nx2, int k_cl, double vis, int i_les, double e_cl, int precision);
 void diag_set_smem_limits();
+// force.f on the resident state: ek0_dev holds the initial shell energies
+// (spectra's ek), k_force + 1 <= 64 shells
+void diag_force(const DiagArgs& d, void* u, const double* ek0_dev, int k_force, cudaStream_t s);
 // measured FP64 FMA throughput of this GPU in TFLOP/s
 double diag_fp64_peak(cudaStream_t s);
 // scratch must hold (5*Lm+2)*Nx_min + 5*Lm + 3 doubles

@@ -913,6 +913,140 @@ int sam_gpu_cl_energy(double* e_cl) {
   return sync_stream(c);
 }
 
+int sam_gpu_force(const double* ek_0, int k_force) {
+  NEED_CTX();
+  if (!ek_0 || k_force < 1 || k_force >= 64 || k_force >= c.lm)
+    return fail(SAM_GPU_EINVAL, "force: k_force must be in 1..min(63, Lm-1)");
+  int rc = ensure(c.sc[3], sizeof(double) * 64);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c.sc[3].p, ek_0, sizeof(double) * (k_force + 1), cudaMemcpyHostToDevice, c.stream));
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, c.cfg.precision);
+  diag_force(d, c.U, (const double*)c.sc[3].p, k_force, c.stream);
+  return sync_stream(c);
+}
+
+// ------------------------------------------------------------- restart files
+// vel.NNNNNN (write_field.f:12-30): for each field n and kx index ii a record
+// of Nz_min x Ny_min complex128 at offset ((n-1) Nx_min + ii-1) * record, i.e.
+// the fields in exactly the resident (field, kx, ky, kz) order.
+
+static int resident_fp64(Ctx& c, const double2** out) {
+  const size_t nm = (size_t)c.g.mx * c.g.my * c.g.mz * c.g.lu;
+  if (c.cfg.precision == 64) {
+    *out = (const double2*)c.U;
+    return 0;
+  }
+  int rc = ensure(c.sc[1], nm * 16);
+  if (rc) return rc;
+  convert_out<float>((const float2*)c.U, (double2*)c.sc[1].p, (long long)nm, c.stream);
+  *out = (const double2*)c.sc[1].p;
+  return 0;
+}
+
+int sam_gpu_write_field(const char* fname) {
+  NEED_CTX();
+  if (!fname) return fail(SAM_GPU_EINVAL, "write_field: null file name");
+  const size_t bytes = (size_t)c.g.mx * c.g.my * c.g.mz * c.g.lu * 16;
+  const double2* src;
+  int rc = resident_fp64(c, &src);
+  if (rc) return rc;
+  std::vector<char> host(bytes);
+  CK(cudaMemcpyAsync(host.data(), src, bytes, cudaMemcpyDeviceToHost, c.stream));
+  if ((rc = sync_stream(c))) return rc;
+  FILE* f = fopen(fname, "wb");
+  if (!f) return fail(SAM_GPU_EINVAL, "write_field: cannot open %s", fname);
+  const size_t w = fwrite(host.data(), 1, bytes, f);
+  fclose(f);
+  if (w != bytes) return fail(SAM_GPU_EINVAL, "write_field: short write to %s", fname);
+  return 0;
+}
+
+int sam_gpu_read_field(const char* fname) {
+  NEED_CTX();
+  if (!fname) return fail(SAM_GPU_EINVAL, "read_field: null file name");
+  const size_t nm = (size_t)c.g.mx * c.g.my * c.g.mz * c.g.lu;
+  const size_t expect = nm * 16;
+  FILE* f = fopen(fname, "rb");
+  if (!f) return fail(SAM_GPU_EINVAL, "read_field: cannot open %s", fname);
+  fseek(f, 0, SEEK_END);
+  const long found = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  if (found < 0 || (size_t)found != expect) {  // read_field.f:74-80
+    fclose(f);
+    return fail(SAM_GPU_EINVAL, "read_field: vel file is not of correct size (expect %zu, found %ld)", expect, found);
+  }
+  std::vector<char> host(expect);
+  const size_t r = fread(host.data(), 1, expect, f);
+  fclose(f);
+  if (r != expect) return fail(SAM_GPU_EINVAL, "read_field: short read from %s", fname);
+  int rc;
+  void* dst = c.U;
+  if (c.cfg.precision == 32) {
+    if ((rc = ensure(c.sc[0], expect))) return rc;
+    dst = c.sc[0].p;
+  }
+  CK(cudaMemcpyAsync(dst, host.data(), expect, cudaMemcpyHostToDevice, c.stream));
+  if (c.cfg.precision == 32) convert_in<float>((const double2*)dst, (float2*)c.U, (long long)nm, c.stream);
+  CK(cudaMemsetAsync(c.R, 0, csize(c) * nm, c.stream));
+  return sync_stream(c);
+}
+
+// header.NNNNNN (write_header.f:27-31): one "label value" line per
+// parameter; the restart-fixed ones (set_labels.f:29-57: box and grid, the
+// stratification switch) must agree on reading (read_header.f:25-38), and
+// time and dt are restored (assign_run_time.f).
+int sam_gpu_write_header(const char* fname, int nt) {
+  NEED_CTX();
+  DevState st;
+  CK(cudaMemcpyAsync(&st, c.state, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  FILE* f = fopen(fname, "w");
+  if (!f) return fail(SAM_GPU_EINVAL, "write_header: cannot open %s", fname);
+  const sam_gpu_config& k = c.cfg;
+  fprintf(f, " xL %.17g\n yL %.17g\n zL %.17g\n c_smag %.17g\n dt0 %.17g\n cfl0 %.17g\n vis %.17g\n pr %.17g\n",
+          k.xl, k.yl, k.zl, k.c_smag, k.dt0, k.cfl0, k.vis, k.pr);
+  fprintf(f, " Nx %d\n Ny %d\n Nz %d\n i_strat %d\n i_les %d\n i_cfl %d\n nrk_max %d\n n_dealias %d\n", k.nx, k.ny,
+          k.nz, k.i_strat, k.i_les, k.i_cfl, k.nrk_max, k.n_dealias);
+  fprintf(f, " time %.17g\n dt %.17g\n t_stat %.17g\n nt %d\n n_frame_p %d\n n_hist %d\n", st.time, st.dt, 0.0, nt, 0,
+          0);
+  fclose(f);
+  return 0;
+}
+
+int sam_gpu_read_header(const char* fname, int* nt) {
+  NEED_CTX();
+  FILE* f = fopen(fname, "r");
+  if (!f) return fail(SAM_GPU_EINVAL, "read_header: cannot open %s", fname);
+  char label[64];
+  double v;
+  double time = 0.0, dt = c.cfg.dt0;
+  int got_nt = 0, bad = 0;
+  char which[64] = "";
+  const sam_gpu_config& k = c.cfg;
+  while (fscanf(f, "%63s %lf", label, &v) == 2) {
+    std::string s(label);
+    for (auto& ch : s) ch = (char)tolower(ch);
+    auto fixed = [&](const char* nm, double have) {
+      if (s == nm && fabs(v - have) > 1.0e-12) { bad = 1; snprintf(which, sizeof(which), "%s", nm); }
+    };
+    fixed("xl", k.xl); fixed("yl", k.yl); fixed("zl", k.zl);
+    fixed("nx", k.nx); fixed("ny", k.ny); fixed("nz", k.nz); fixed("i_strat", k.i_strat);
+    if (s == "time") time = v;
+    else if (s == "dt") dt = v;
+    else if (s == "nt") got_nt = (int)v;
+  }
+  fclose(f);
+  if (bad) return fail(SAM_GPU_EINVAL, "read_header: parameter %s differs between the header and the configuration", which);
+  if (nt) *nt = got_nt;
+  DevState st;
+  CK(cudaMemcpyAsync(&st, c.state, sizeof(st), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  st.time = time;
+  st.dt = dt;
+  CK(cudaMemcpyAsync(c.state, &st, sizeof(st), cudaMemcpyHostToDevice, c.stream));
+  return sync_stream(c);
+}
+
 int sam_gpu_x_deriv(const double* u, double* du, double*) {
   NEED_CTX();
   if (!u || !du) return fail(SAM_GPU_EINVAL, "x_deriv: null array");

@@ -27,6 +27,7 @@ EXPORTS = [
     "sam_gpu_step", "sam_gpu_spectra", "sam_gpu_div_check", "sam_gpu_cl_energy", "sam_gpu_init_taylor_green",
     "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
     "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
+    "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
 ]
 
 
@@ -102,6 +103,11 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_sm.argtypes = [P, P, P, P]
     lib.sam_gpu_dm.argtypes = [P] * 11
     lib.sam_gpu_get_mean.argtypes = [P, C.c_int, C.c_int, P, P, P]
+    lib.sam_gpu_force.argtypes = [P, C.c_int]
+    lib.sam_gpu_write_field.argtypes = [C.c_char_p]
+    lib.sam_gpu_read_field.argtypes = [C.c_char_p]
+    lib.sam_gpu_write_header.argtypes = [C.c_char_p, C.c_int]
+    lib.sam_gpu_read_header.argtypes = [C.c_char_p, C.POINTER(C.c_int)]
     _lib = lib
     return lib
 
@@ -313,6 +319,25 @@ class SamGpu:
         e = C.c_double(0.0)
         self._check(load_library().sam_gpu_cl_energy(C.byref(e)), "cl_energy")
         return e.value
+
+    # ---- forcing and restart files
+    def force(self, ek_0, k_force):
+        self._check(load_library().sam_gpu_force(_p(np.ascontiguousarray(ek_0, dtype=np.float64)), k_force),
+                    "force")
+
+    def write_field(self, fname):
+        self._check(load_library().sam_gpu_write_field(fname.encode()), "write_field")
+
+    def read_field(self, fname):
+        self._check(load_library().sam_gpu_read_field(fname.encode()), "read_field")
+
+    def write_header(self, fname, nt):
+        self._check(load_library().sam_gpu_write_header(fname.encode(), nt), "write_header")
+
+    def read_header(self, fname):
+        nt = C.c_int(0)
+        self._check(load_library().sam_gpu_read_header(fname.encode(), C.byref(nt)), "read_header")
+        return nt.value
 
     # ---- initial fields
     def init_taylor_green(self):
