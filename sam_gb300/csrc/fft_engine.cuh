@@ -49,7 +49,8 @@ struct FftPlan {
   int nst;
   int tw_total;
   int team;     // threads per line in FP64 (at most 8 values per thread)
-  int team_sp;  // threads per line in FP32 (at most 16 values per thread)
+  int team_sp;  // threads per line in FP32 (at most 8 values per thread)
+  int tw16_off; // n == 256: offset of the 16 x 16 table w_256^{f q} (else -1)
   FftStage st[10];
 };
 
@@ -62,13 +63,13 @@ template <typename C> __device__ __forceinline__ int team_of(const FftPlan& pl) 
 
 __device__ __forceinline__ int div_m(int b, const FftStage& s) { return (int)(((uint32_t)b * s.mmul) >> 21); }
 
-// Shared-memory position of element p of a line: one pad slot after every 8
-// elements, so the stride-p accesses of the late Stockham stages and the
-// column accesses of the transposing stores fall in distinct banks.
-__host__ __device__ __forceinline__ int sidx(int p) { return p + (p >> 3); }
+// Shared-memory position of element p of a line: one pad slot after every 16
+// elements, so the stride-16 row reads of the 16 x 16 path (and the strided
+// reads of late Stockham stages) fall in distinct banks.
+__host__ __device__ __forceinline__ int sidx(int p) { return p + (p >> 4); }
 // Stride between consecutive lines (odd, so lines start in rotating banks).
 __host__ __device__ __forceinline__ int line_stride(int n) {
-  const int s = n + (n >> 3) + 1;
+  const int s = n + (n >> 4) + 1;
   return s | 1;
 }
 
@@ -168,6 +169,42 @@ template <int SIGN, typename C> __device__ __forceinline__ void dft5(C* a) {
   a[4] = csub(m1, n1);
   a[2] = cadd(m2, n2);
   a[3] = csub(m2, n2);
+}
+
+// 16-point DFT in registers as 4 x 4: DFT4 over n1 of x[4 n1 + n2], the
+// twiddles w16^{n2 k1}, DFT4 over n2; output k1 + 4 k2 in place.
+template <int SIGN, typename C> __device__ __forceinline__ void dft16(C* a) {
+  using T = decltype(C::x);
+  const T c1 = (T)0.92387953251128675612818318939678828682;  // cos(pi/8)
+  const T s1 = (T)0.38268343236508977172845998403039886676;  // sin(pi/8)
+  const T h = (T)0.70710678118654752440084436210484903928;   // sqrt(2)/2
+  C b[4][4];
+#pragma unroll
+  for (int n2 = 0; n2 < 4; ++n2) {
+    C t[4] = {a[n2], a[4 + n2], a[8 + n2], a[12 + n2]};
+    dft4<SIGN>(t);
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) b[n2][k1] = t[k1];
+  }
+  // w16^j = (cos(2 pi j/16), SIGN sin(2 pi j/16)) for j = n2 k1
+  auto rot = [&](C v, T cr, T si) { return mk<C>(v.x * cr - v.y * si, v.x * si + v.y * cr); };
+  const T sg = (T)SIGN;
+  b[1][1] = rot(b[1][1], c1, sg * s1);   // j = 1
+  b[1][2] = rot(b[1][2], h, sg * h);     // j = 2
+  b[1][3] = rot(b[1][3], s1, sg * c1);   // j = 3
+  b[2][1] = rot(b[2][1], h, sg * h);     // j = 2
+  b[2][2] = cmul_si<SIGN>(b[2][2]);      // j = 4
+  b[2][3] = rot(b[2][3], -h, sg * h);    // j = 6
+  b[3][1] = rot(b[3][1], s1, sg * c1);   // j = 3
+  b[3][2] = rot(b[3][2], -h, sg * h);    // j = 6
+  b[3][3] = rot(b[3][3], -c1, -sg * s1); // j = 9
+#pragma unroll
+  for (int k1 = 0; k1 < 4; ++k1) {
+    C t[4] = {b[0][k1], b[1][k1], b[2][k1], b[3][k1]};
+    dft4<SIGN>(t);
+#pragma unroll
+    for (int k2 = 0; k2 < 4; ++k2) a[k1 + 4 * k2] = t[k2];
+  }
 }
 
 template <int P, int SIGN, typename C> __device__ __forceinline__ void dftp(C* a) {
@@ -273,11 +310,60 @@ __device__ __forceinline__ void fft_line_from(C* line, const C* __restrict__ tw,
   for (int s = 1; s < pl.nst; ++s) fft_stage_p<SIGN>(line, tw, pl.st[s], n, tla, TW, LineLoad<C>{line});
 }
 
+// n = 256 as 16 x 16 in registers: a team of 16 threads per line, two lines
+// per warp.  Thread k first transforms the column x[k + 16 q] (the l = 1
+// Stockham stage of radix 16) and writes it back; thread f then reads row
+// 16 f + q, applies w_256^{f q} and transforms it (the l = 16 stage).  One
+// shared-memory exchange and four warp barriers per line.
+template <int SIGN, typename C, typename First>
+__device__ __forceinline__ void fft256_lines(C* base, int ld, int nlines, const C* __restrict__ tw,
+                                             const FftPlan& pl, First first) {
+  const int team = threadIdx.x >> 4;
+  const int k = threadIdx.x & 15;
+  const int nteams = blockDim.x >> 4;
+  const int rounds = (nlines + nteams - 1) / nteams;
+  const C* w = tw + pl.tw16_off + k;  // w[16 q] = w_256^{k q}
+  for (int r = 0; r < rounds; ++r) {
+    const int L = r * nteams + team;
+    const bool active = L < nlines;
+    C* line = base + (active ? L : 0) * ld;
+    C a[16];
+    if (active) {
+      const auto ld0 = first(L);
+#pragma unroll
+      for (int q = 0; q < 16; ++q) a[q] = ld0(k + 16 * q);
+      dft16<SIGN>(a);
+    }
+    __syncwarp();
+    if (active) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s) line[sidx(16 * s + k)] = a[s];
+    }
+    __syncwarp();
+    if (active) {
+      a[0] = line[sidx(16 * k)];
+#pragma unroll
+      for (int q = 1; q < 16; ++q) a[q] = ctw<SIGN>(line[sidx(16 * k + q)], w[16 * q]);
+      dft16<SIGN>(a);
+    }
+    __syncwarp();
+    if (active) {
+#pragma unroll
+      for (int s = 0; s < 16; ++s) line[sidx(k + 16 * s)] = a[s];
+    }
+    __syncwarp();
+  }
+}
+
 // Transform `nlines` lines of a CTA's shared-memory tile.  Line L starts at
 // base + L*ld.  Every thread of the CTA must call this with the same plan.
 template <int SIGN, typename C>
 __device__ __forceinline__ void fft_lines(C* base, int ld, int nlines, const C* __restrict__ tw, const FftPlan& pl) {
   if (pl.n == 1) return;
+  if (pl.tw16_off >= 0) {
+    fft256_lines<SIGN>(base, ld, nlines, tw, pl, [&](int L) { return LineLoad<C>{base + L * ld}; });
+    return;
+  }
   const int TW = team_of<C>(pl);
   const int nteams = blockDim.x / TW;
   const int team = threadIdx.x / TW;
@@ -298,6 +384,10 @@ __device__ __forceinline__ void fft_lines_from(C* base, int ld, int nlines, cons
                                                const FftPlan& pl, First first) {
   if (pl.n == 1 || pl.nst == 0) {
     for (int L = threadIdx.x; L < nlines; L += blockDim.x) base[L * ld] = first(L)(0);
+    return;
+  }
+  if (pl.tw16_off >= 0) {
+    fft256_lines<SIGN>(base, ld, nlines, tw, pl, first);
     return;
   }
   const int TW = team_of<C>(pl);

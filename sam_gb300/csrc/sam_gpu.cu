@@ -102,6 +102,20 @@ static int build_plan(int n, Plan& P) {
     off += l * (p - 1);
     l *= p;
   }
+  pl.tw16_off = -1;
+  if (n == 256) {
+    // the 16 x 16 register path (fft256_lines): w_256^{f q}, f, q in [0, 16),
+    // stored q-major so the 16 threads of a team read 16 consecutive entries
+    pl.tw16_off = off;
+    for (int q = 0; q < 16; ++q)
+      for (int f = 0; f < 16; ++f) {
+        const long double a = two_pi * (long double)((f * q) % 256) / 256.0L;
+        const long double c = cosl(a), sn = -sinl(a);
+        t64.push_back(make_double2((double)c, (double)sn));
+        t32.push_back(make_float2((float)c, (float)sn));
+      }
+    off += 256;
+  }
   pl.tw_total = off;
   if (t64.empty()) { t64.push_back(make_double2(1, 0)); t32.push_back(make_float2(1, 0)); }
   CK(cudaMalloc(&P.d, sizeof(FftPlan)));

@@ -26,6 +26,9 @@ GRIDS = [
     dict(nx=72, ny=1, nz=24, i_strat=1, xl=3.0, yl=0.05, zl=1.0),
     dict(nx=32, ny=32, nz=32, i_strat=0),
     dict(nx=48, ny=20, nz=96, i_strat=1),
+    # length-256 lines take the 16 x 16 register path: x and y, then z
+    dict(nx=256, ny=256, nz=12, i_strat=1),
+    dict(nx=16, ny=20, nz=256, i_strat=1),
 ]
 
 
@@ -74,7 +77,7 @@ def test_forward_transforms(gpu_lib, grid):
     assert relerr(zg[: d.nz_min], zo[: d.nz_min]) < TOL_ROUTINE
 
 
-@pytest.mark.parametrize("grid", GRIDS[:4])
+@pytest.mark.parametrize("grid", GRIDS[:4] + GRIDS[5:])
 @pytest.mark.parametrize("nrk", [1, 2])
 def test_rhs_and_vel_max(gpu_lib, grid, nrk):
     g, o = pair(i_cfl=1, cfl0=0.5, **grid)
