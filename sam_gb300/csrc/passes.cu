@@ -433,29 +433,85 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_y_fwd(YFwdArg
 __device__ __forceinline__ double wexp(double x) { return exp(x); }
 __device__ __forceinline__ float wexp(float x) { return expf(x); }
 
+// Per-launch constants of the epilogue in working type W, formed once per
+// thread: the FP32 form then touches no FP64 arithmetic per mode.
+template <typename W> struct EpiConst {
+  W wave_x, wave_y, wave_z, nz_inv, dt_fac1, dt_fac2, mvis_f, mvis_t, bx, bz, lapse, cth, sth;
+  bool same_t;
+};
+
+template <typename W, typename T>
+__device__ __forceinline__ EpiConst<W> epi_const(const ZFwdArgs<T>& a, double dt) {
+  const StageConsts& sc = a.sc;
+  EpiConst<W> e;
+  e.wave_x = (W)a.g.wave_x; e.wave_y = (W)a.g.wave_y; e.wave_z = (W)a.g.wave_z;
+  e.nz_inv = (W)(1.0 / (double)a.g.nz);
+  e.dt_fac1 = (W)(sc.gamma * dt);
+  e.dt_fac2 = (W)(sc.zeta * dt);
+  const double vis_f = sc.vis * (sc.gamma * dt + sc.zeta * dt);  // sam.f:293-295
+  e.mvis_f = (W)(-vis_f);
+  e.mvis_t = (W)(-(vis_f * sc.pr_inv));                           // sam.f:297
+  e.same_t = sc.pr_inv == 1.0;
+  e.bx = (W)sc.buoy_fac_x; e.bz = (W)sc.buoy_fac_z; e.lapse = (W)sc.lapse;
+  e.cth = (W)sc.cos_theta; e.sth = (W)sc.sin_theta;
+  return e;
+}
+
+// u and r_old of one mode (mode 2) or u_sav (mode 1), loaded ahead of use.
+template <typename W> struct EpiIn {
+  W ur[4], ui[4], rr[4], ri[4];
+};
+
+template <typename W, typename T>
+__device__ __forceinline__ void epi_load(const ZFwdArgs<T>& a, int i, int j, int k, EpiIn<W>& in) {
+  using C = cx_t<T>;
+  const Grid& g = a.g;
+#pragma unroll
+  for (int f = 0; f < 4; ++f) {
+    in.ur[f] = in.ui[f] = in.rr[f] = in.ri[f] = (W)0;
+  }
+  if (a.mode == 2) {
+    const long long uidx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+      if (f < g.lu) {
+        const C v = a.u[(long long)f * a.u_n + uidx];
+        in.ur[f] = (W)v.x; in.ui[f] = (W)v.y;
+        if (a.sc.nrk > 1) {
+          const C ro = a.r[(long long)f * a.u_n + uidx];
+          in.rr[f] = (W)ro.x; in.ri[f] = (W)ro.y;
+        }
+      }
+  } else if (a.sc.i_strat) {  // mode 1: (w, T) of u_sav in slots 2, 3
+    const long long s = (long long)i * a.sav_kx + (long long)j * a.sav_ky + k;
+    const C w = a.usav[s];
+    const C th = a.usav[a.sav_n + s];
+    in.ur[2] = (W)w.x; in.ui[2] = (W)w.y; in.ur[3] = (W)th.x; in.ui[3] = (W)th.y;
+  }
+}
+
 // rhs.f:108-142 for one mode (kx i, ky j, kz k) in working type W, then
 // (mode 2) sam.f:210-221 and 293-314.  ln points at field 0 of this mode in
 // shared memory; field f is at ln[f * fstride].
 template <typename W, typename T>
 __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln, int fstride, int i, int j, int k,
-                                         double dt) {
+                                         const EpiConst<W>& c, const EpiIn<W>& in) {
   using C = cx_t<T>;
   const Grid& g = a.g;
   const StageConsts& sc = a.sc;
   const int nf = a.nf;
-  const W rkx = (W)(g.wave_x * (double)i);
-  const W rky = (W)(g.wave_y * (double)kwave(j, g.ky, g.my));
-  const W rkz = (W)(g.wave_z * (double)kwave(k, g.kz, g.mz));
+  const W rkx = c.wave_x * (W)i;
+  const W rky = c.wave_y * (W)kwave(j, g.ky, g.my);
+  const W rkz = c.wave_z * (W)kwave(k, g.kz, g.mz);
   const W rk_sq_raw = rkx * rkx + rky * rky + rkz * rkz;
   const W rk_sq = rk_sq_raw > (W)1.0e-10 ? rk_sq_raw : (W)1.0e-10;
-  const W nz_inv = (W)(1.0 / (double)g.nz);
   W tr[9], ti[9];
 #pragma unroll
   for (int f = 0; f < 9; ++f) {
     if (f < nf) {
       const C v = ln[f * fstride];
-      tr[f] = (W)v.x * nz_inv;
-      ti[f] = (W)v.y * nz_inv;
+      tr[f] = (W)v.x * c.nz_inv;
+      ti[f] = (W)v.y * c.nz_inv;
     } else {
       tr[f] = (W)0; ti[f] = (W)0;
     }
@@ -465,38 +521,19 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
   const W s2r = rkx * tr[1] + rky * tr[2] + rkz * tr[4], s2i = rkx * ti[1] + rky * ti[2] + rkz * ti[4];
   const W s3r = rkx * tr[3] + rky * tr[4] + rkz * tr[5], s3i = rkx * ti[3] + rky * ti[4] + rkz * ti[5];
   W r1r = s1i, r1i = -s1r, r2r = s2i, r2i = -s2r, r3r = s3i, r3i = -s3r, r4r = (W)0, r4i = (W)0;
-  W u_r[4] = {0, 0, 0, 0}, u_i[4] = {0, 0, 0, 0};
-  const long long uidx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
-  if (a.mode == 2) {
-#pragma unroll
-    for (int f = 0; f < 4; ++f)
-      if (f < g.lu) {
-        const C v = a.u[(long long)f * a.u_n + uidx];
-        u_r[f] = (W)v.x;
-        u_i[f] = (W)v.y;
-      }
-  }
   if (sc.i_strat) {
-    W wr, wi, thr, thi;
-    if (a.mode == 2) {
-      wr = u_r[2]; wi = u_i[2];
-      if (sc.rot_sav) {  // sam.f:180-181
-        wr = (W)sc.cos_theta * u_r[2] - (W)sc.sin_theta * u_r[0];
-        wi = (W)sc.cos_theta * u_i[2] - (W)sc.sin_theta * u_i[0];
-      }
-      thr = u_r[3]; thi = u_i[3];
-    } else {
-      const long long s = (long long)i * a.sav_kx + (long long)j * a.sav_ky + k;
-      const C w = a.usav[s];
-      const C th = a.usav[a.sav_n + s];
-      wr = (W)w.x; wi = (W)w.y; thr = (W)th.x; thi = (W)th.y;
+    W wr = in.ur[2], wi = in.ui[2];
+    if (a.mode == 2 && sc.rot_sav) {  // sam.f:180-181
+      wr = c.cth * in.ur[2] - c.sth * in.ur[0];
+      wi = c.cth * in.ui[2] - c.sth * in.ui[0];
     }
-    r1r += (W)sc.buoy_fac_x * thr; r1i += (W)sc.buoy_fac_x * thi;
-    r3r += (W)sc.buoy_fac_z * thr; r3i += (W)sc.buoy_fac_z * thi;
+    const W thr = in.ur[3], thi = in.ui[3];
+    r1r += c.bx * thr; r1i += c.bx * thi;
+    r3r += c.bz * thr; r3i += c.bz * thi;
     const W s4r = rkx * tr[6] + rky * tr[7] + rkz * tr[8];
     const W s4i = rkx * ti[6] + rky * ti[7] + rkz * ti[8];
-    r4r = s4i - (W)sc.lapse * wr;
-    r4i = -s4r - (W)sc.lapse * wi;
+    r4r = s4i - c.lapse * wr;
+    r4i = -s4r - c.lapse * wi;
   }
   // p = -i (k . R) / k^2 ;  R -= i k p   (rhs.f:134-139)
   const W qr = rkx * r1r + rky * r2r + rkz * r3r, qi = rkx * r1i + rky * r2i + rkz * r3i;
@@ -514,27 +551,24 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
     a.r[(long long)g.lu * a.r_n + ridx] = mk<C>((T)pr, (T)pim);
     return;
   }
-  const W dt_fac1 = (W)(sc.gamma * dt), dt_fac2 = (W)(sc.zeta * dt);
-  const W vis_f = (W)(sc.vis * (sc.gamma * dt + sc.zeta * dt));
-  const long long ridx = uidx;
-  const W ef = wexp(-vis_f * rk_sq_raw);
-  const W et = sc.pr_inv == 1.0 ? ef : wexp(-(vis_f * (W)sc.pr_inv) * rk_sq_raw);
+  const long long uidx = (long long)i * a.u_kx + (long long)j * a.u_ky + k;
+  const W ef = wexp(c.mvis_f * rk_sq_raw);
+  const W et = c.same_t ? ef : wexp(c.mvis_t * rk_sq_raw);
 #pragma unroll
   for (int f = 0; f < 4; ++f)
     if (f < g.lu) {
-      W ur = u_r[f], ui = u_i[f];
+      W ur = in.ur[f], ui = in.ui[f];
       if (sc.nrk > 1) {  // sam.f:211-221
-        const C ro = a.r[(long long)f * a.u_n + ridx];
-        ur = ur + dt_fac2 * (W)ro.x;
-        ui = ui + dt_fac2 * (W)ro.y;
+        ur = ur + c.dt_fac2 * in.rr[f];
+        ui = ui + c.dt_fac2 * in.ri[f];
       }
       const W vf = f == 3 ? et : ef;  // sam.f:297
-      ur = (ur + dt_fac1 * rr[f]) * vf;
-      ui = (ui + dt_fac1 * ri[f]) * vf;
+      ur = (ur + c.dt_fac1 * rr[f]) * vf;
+      ui = (ui + c.dt_fac1 * ri[f]) * vf;
       a.u[(long long)f * a.u_n + uidx] = mk<C>((T)ur, (T)ui);
-      a.r[(long long)f * a.u_n + ridx] = mk<C>((T)rr[f], (T)ri[f]);
+      a.r[(long long)f * a.u_n + uidx] = mk<C>((T)rr[f], (T)ri[f]);
     }
-  if (sc.write_p) a.p[ridx] = mk<C>((T)pr, (T)pim);
+  if (sc.write_p) a.p[uidx] = mk<C>((T)pr, (T)pim);
 }
 
 // --------------------------------------------------------------- z forward
@@ -593,13 +627,29 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_z_fwd(ZFwdArg
   }
   double dt = 0.0;
   if (a.mode == 2) dt = a.state->dt;
-  for (int e = threadIdx.x; e < nl * mz; e += blockDim.x) {
-    const int t = (int)fdiv(e, a.fd_m), k = e - t * mz;
-    const int j = j0 + t;
-    const C* ln = s_ln + t * ld + sidx(kpos(k, km, mz, nz));
-    // the FP32 form keeps the mean (k = 0) mode in FP64
-    if (sizeof(T) == 4 && i == 0 && j == 0 && k == 0) epi_mode<double, T>(a, ln, nl * ld, i, j, k, dt);
-    else epi_mode<T, T>(a, ln, nl * ld, i, j, k, dt);
+  const EpiConst<T> cw = epi_const<T>(a, dt);
+  // two modes per iteration: their global loads are issued together
+  for (int e0 = threadIdx.x; e0 < nl * mz; e0 += 2 * blockDim.x) {
+    const int e1 = e0 + blockDim.x;
+    const bool has1 = e1 < nl * mz;
+    const int t0 = (int)fdiv(e0, a.fd_m), k0 = e0 - t0 * mz;
+    const int t1 = has1 ? (int)fdiv(e1, a.fd_m) : t0, k1 = has1 ? e1 - t1 * mz : k0;
+    EpiIn<T> in0, in1;
+    epi_load<T>(a, i, j0 + t0, k0, in0);
+    if (has1) epi_load<T>(a, i, j0 + t1, k1, in1);
+    for (int h = 0; h < 2; ++h) {
+      if (h == 1 && !has1) break;
+      const int t = h ? t1 : t0, k = h ? k1 : k0, j = j0 + t;
+      const C* ln = s_ln + t * ld + sidx(kpos(k, km, mz, nz));
+      if (sizeof(T) == 4 && i == 0 && j == 0 && k == 0) {
+        // the FP32 form keeps the mean (k = 0) mode in FP64
+        EpiIn<double> ind;
+        epi_load<double>(a, i, j, k, ind);
+        epi_mode<double, T>(a, ln, nl * ld, i, j, k, epi_const<double>(a, dt), ind);
+      } else {
+        epi_mode<T, T>(a, ln, nl * ld, i, j, k, cw, h ? in1 : in0);
+      }
+    }
   }
   if (a.mode == 2 && a.sc.last && blockIdx.x == 0 && threadIdx.x == 0) {
     // sam.f:318 time = time + dt, once per step (no CTA of this launch reads

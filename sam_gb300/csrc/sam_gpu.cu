@@ -9,6 +9,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <initializer_list>
 #include <string>
 #include <vector>
 
@@ -343,33 +344,43 @@ static int run_z_fwd(Ctx& c, ZFwdArgs<T>& a) {
 }
 
 // One fused RK stage on the resident state (sam.f:169-314).  When ev is
-// given, ev[p] is recorded before pass p and ev[5] after the last pass.
+// given, ev[p] is recorded before pass p and ev[5] after the last pass; when
+// only >= 0, just pass `only` (0..4) runs (used by the autotuner).
 template <typename T>
-static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr) {
+static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = -1) {
   const Grid& g = c.g;
   const long long nzmm = (long long)g.mx * g.my * g.mz;
-  int rc;
+  int rc = 0;
+  auto run = [&](int p) { return only < 0 || only == p; };
   if (ev) cudaEventRecord(ev[0], c.stream);
   // z inverse: U(n, kx, ky, kz) -> A(n, z, kx, ky)
-  rc = run_z_inv<T>(c, c.U, c.S1, g.lu, g.mz, (long long)g.my * g.mz, nzmm, g.my, (long long)g.mx * g.my,
-                    (long long)g.nz * g.mx * g.my);
+  if (run(0))
+    rc = run_z_inv<T>(c, c.U, c.S1, g.lu, g.mz, (long long)g.my * g.mz, nzmm, g.my, (long long)g.mx * g.my,
+                      (long long)g.nz * g.mx * g.my);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[1], c.stream);
   // y inverse: A -> B(n, z, y, kx)
-  rc = run_y_inv<T>(c, c.S1, c.S2, g.lu, 0, g.my, (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, g.mx,
-                    (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx);
+  if (run(1))
+    rc = run_y_inv<T>(c, c.S1, c.S2, g.lu, 0, g.my, (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, g.mx,
+                      (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[2], c.stream);
   // x pass: B -> C(m, z, kx, y) with vel_max at nrk = 1
-  rc = run_x_pass<T>(c, 0, 2, g.lu, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx, c.S3,
-                     nullptr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, 0, 0, 0, nrk == 1);
+  if (run(2))
+    rc = run_x_pass<T>(c, 0, 2, g.lu, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
+                       c.S3, nullptr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, 0, 0, 0, nrk == 1);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[3], c.stream);
   // y forward: C -> D(m, kx, ky, z)
-  rc = run_y_fwd<T>(c, c.S3, c.S1, g.lr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, g.nz,
-                    (long long)g.my * g.nz, (long long)g.mx * g.my * g.nz);
+  if (run(3))
+    rc = run_y_fwd<T>(c, c.S3, c.S1, g.lr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, g.nz,
+                      (long long)g.my * g.nz, (long long)g.mx * g.my * g.nz);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[4], c.stream);
+  if (!run(4)) {
+    if (ev) cudaEventRecord(ev[5], c.stream);
+    return 0;
+  }
   // z forward + rhs + RK update
   ZFwdArgs<T> a{};
   a.in = (cx_t<T>*)c.S1;
@@ -387,8 +398,8 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr) {
   return rc;
 }
 
-static int stage_any(Ctx& c, int nrk, cudaEvent_t* ev = nullptr) {
-  return c.cfg.precision == 32 ? enqueue_stage<float>(c, nrk, ev) : enqueue_stage<double>(c, nrk, ev);
+static int stage_any(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = -1) {
+  return c.cfg.precision == 32 ? enqueue_stage<float>(c, nrk, ev, only) : enqueue_stage<double>(c, nrk, ev, only);
 }
 
 static int check_launch() {
@@ -817,6 +828,71 @@ int sam_gpu_measure_fp64_peak(double* tflops) {
   if (!tflops) return fail(SAM_GPU_EINVAL, "measure_fp64_peak: null output");
   *tflops = diag_fp64_peak(c.stream);
   return check_launch();
+}
+
+// Tile autotuner: each pass is timed (CUDA events, best of `reps`) with each
+// candidate tiling on the resident state and the fastest is kept.  The z
+// forward pass updates u and r, so both are saved first and restored after.
+int sam_gpu_autotune(int reps) {
+  NEED_CTX();
+  if (reps < 1) reps = 1;
+  const size_t nm = (size_t)c.g.mx * c.g.my * c.g.mz * c.g.lu;
+  const size_t bytes = nm * csize(c);
+  void *su = nullptr, *sr = nullptr;
+  CK(cudaMalloc(&su, bytes));
+  CK(cudaMalloc(&sr, bytes));
+  CK(cudaMemcpyAsync(su, c.U, bytes, cudaMemcpyDeviceToDevice, c.stream));
+  CK(cudaMemcpyAsync(sr, c.R, bytes, cudaMemcpyDeviceToDevice, c.stream));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  auto time_pass = [&](int p) {
+    float best = 1e30f;
+    for (int r = 0; r < reps + 1; ++r) {
+      cudaEventRecord(e0, c.stream);
+      if (stage_any(c, 2, nullptr, p)) return 1e30f;
+      cudaEventRecord(e1, c.stream);
+      cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (r > 0 && ms < best) best = ms;  // the first run warms up
+    }
+    return best;
+  };
+  auto tune = [&](int p, int* field, std::initializer_list<int> cands) {
+    int best_v = *field;
+    float best_t = time_pass(p);
+    for (int v : cands) {
+      if (v == best_v) continue;
+      const int keep = *field;
+      *field = v;
+      const float t = time_pass(p);
+      if (t < best_t) { best_t = t; best_v = v; }
+      else *field = keep;
+    }
+    *field = best_v;
+  };
+  tune(0, &c.ty_zi, {4, 8, 16, 32});
+  tune(1, &c.tx_yi, {4, 8, 16, 32});
+  tune(2, &c.yt_x, {2, 4, 8, 16});
+  tune(2, &c.grp_x, {1, 2, 3, 5, 9});
+  tune(3, &c.tz_yf, {4, 8, 16, 32});
+  tune(4, &c.ty_zf, {1, 2, 4, 8});
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaMemcpyAsync(c.U, su, bytes, cudaMemcpyDeviceToDevice, c.stream));
+  CK(cudaMemcpyAsync(c.R, sr, bytes, cudaMemcpyDeviceToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  cudaFree(su);
+  cudaFree(sr);
+  if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }  // recapture with the new tiles
+  return check_launch();
+}
+
+int sam_gpu_tiles(int* out6) {
+  NEED_CTX();
+  out6[0] = c.ty_zi; out6[1] = c.tx_yi; out6[2] = c.yt_x; out6[3] = c.grp_x; out6[4] = c.tz_yf; out6[5] = c.ty_zf;
+  return 0;
 }
 
 int sam_gpu_profile_stage(int nrk, int reps, float* ms5) {

@@ -28,6 +28,7 @@ EXPORTS = [
     "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
     "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
     "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
+    "sam_gpu_autotune", "sam_gpu_tiles",
 ]
 
 
@@ -103,6 +104,8 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_sm.argtypes = [P, P, P, P]
     lib.sam_gpu_dm.argtypes = [P] * 11
     lib.sam_gpu_get_mean.argtypes = [P, C.c_int, C.c_int, P, P, P]
+    lib.sam_gpu_autotune.argtypes = [C.c_int]
+    lib.sam_gpu_tiles.argtypes = [P]
     lib.sam_gpu_force.argtypes = [P, C.c_int]
     lib.sam_gpu_write_field.argtypes = [C.c_char_p]
     lib.sam_gpu_read_field.argtypes = [C.c_char_p]
@@ -296,6 +299,14 @@ class SamGpu:
         ms = np.zeros(5, dtype=np.float32)
         self._check(load_library().sam_gpu_profile_stage(nrk, reps, ms.ctypes.data_as(C.c_void_p)), "profile")
         return dict(zip(("z_inv", "y_inv", "x_pass", "y_fwd", "z_fwd"), [float(x) for x in ms]))
+
+    def autotune(self, reps=3):
+        """Pick the fastest tiling of each pass on the resident state."""
+        self._check(load_library().sam_gpu_autotune(reps), "autotune")
+        t = np.zeros(6, dtype=np.int32)
+        self._check(load_library().sam_gpu_tiles(t.ctypes.data_as(C.c_void_p)), "tiles")
+        return dict(zip(("z_inv_rows", "y_inv_cols", "x_rows", "x_group", "y_fwd_planes", "z_fwd_rows"),
+                        [int(x) for x in t]))
 
     def fp64_peak_tflops(self):
         t = C.c_double(0.0)
