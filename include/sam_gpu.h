@@ -186,6 +186,23 @@ int sam_gpu_cl_energy(double* e_cl);
  * to the initial shell energies ek_0 (spectra's ek of step 0) */
 int sam_gpu_force(const double* ek_0, int k_force);
 
+/* ---- planes output of the resident state ----
+ * sam.f:145-166 + write_planes.f:1  at an output step (before stage 1), the
+ * fields uu = u, v, w, [T], p, du/dz, dv/dz, [dT/dz] (p is the pressure the
+ * last stage left, r(Lu+1)) cut into planes in write_planes' record order:
+ *   xy(Nx,Ny,2Lu,n_xy)  all 2Lu fields at z = k_xy(m)      (write_planes.f:34-45)
+ *   xz(Nx,Nz,2Lu,n_xz)  u..p at y = j_xz(m), then y_deriv of the fields
+ *                       n = 1,3,[4]                          (write_planes.f:56-89)
+ *   yz(Ny,Nz,2Lu,n_yz)  u..p at x = i_yz(m), then x_deriv of the fields
+ *                       n = 2,3,[4]                          (write_planes.f:105-131)
+ *   mean(Nz,Lu)         get_mean (i_remove = 0) of each u field (sam.f:161-165)
+ * Plane indices are 1-based as in the input deck; at most
+ * SAM_GPU_MAX_PLANES of each kind; an array may be NULL when its count is 0
+ * (mean may be NULL).  The resident state is not modified. */
+#define SAM_GPU_MAX_PLANES 16
+int sam_gpu_planes(const int* k_xy, int n_xy, const int* j_xz, int n_xz, const int* i_yz, int n_yz, double* xy,
+                   double* xz, double* yz, double* mean);
+
 /* ---- restart files of the resident state ---- */
 /* write_field.f:1 / read_field.f:1  vel.NNNNNN: Lu*Nx_min records of
  * Nz_min x Ny_min complex128; read_field rejects a file of the wrong size */

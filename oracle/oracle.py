@@ -97,6 +97,7 @@ def lib():
                                         C.c_double, C.c_double, C.c_double]
         _lib.so_fft_line.argtypes = [C.c_int, C.c_int, P]
         _lib.so_force.argtypes = [P, P, P, C.c_int]
+        _lib.so_planes.argtypes = [P, P, P, P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
         _lib.so_write_field.argtypes = [P, C.c_char_p, P]
         _lib.so_read_field.argtypes = [P, C.c_char_p, P]
     return _lib
@@ -268,6 +269,25 @@ class Oracle:
         du = np.zeros_like(u, order="F")
         lib().so_y_deriv(self.h, _p(u), _p(du))
         return du
+
+    def planes(self, u, p, k_xy=(), j_xz=(), i_yz=()):
+        """Planes output of sam.f:145-166 / write_planes.f (1-based plane
+        indices): xy (Nx,Ny,2Lu,n_xy), xz (Nx,Nz,2Lu,n_xz), yz (Ny,Nz,2Lu,n_yz),
+        mean (Nz,Lu); p is the pressure field r(Lu+1) in wave space."""
+        d = self.d
+        n_out = 2 * d.lu
+        ia = [np.ascontiguousarray(x, dtype=np.int32) for x in (k_xy, j_xz, i_yz)]
+        xy = np.zeros((d.nx, d.ny, n_out, max(len(ia[0]), 1)), order="F")
+        xz = np.zeros((d.nx, d.nz, n_out, max(len(ia[1]), 1)), order="F")
+        yz = np.zeros((d.ny, d.nz, n_out, max(len(ia[2]), 1)), order="F")
+        mean = np.zeros((d.nz, d.lu), order="F")
+        u = np.asfortranarray(u)
+        p = np.asfortranarray(p)
+        rc = lib().so_planes(self.h, _p(u), _p(p), _p(ia[0]), len(ia[0]), _p(ia[1]), len(ia[1]), _p(ia[2]),
+                             len(ia[2]), _p(xy), _p(xz), _p(yz), _p(mean))
+        if rc:
+            raise ValueError("so_planes: plane index out of range")
+        return dict(xy=xy[..., :len(ia[0])], xz=xz[..., :len(ia[1])], yz=yz[..., :len(ia[2])], mean=mean)
 
     def filter(self, f_bar, n_var):
         d = self.d

@@ -1208,3 +1208,93 @@ int so_read_field(so_ctx *c, const char *fname, double *ud) {
   fclose(f);
   return 0;
 }
+
+/* ------------------------------------------------------------ planes output
+ * The output-step branch of sam.f:145-166 and 225-239 plus write_planes.f:
+ * r(Lu+1) = p, r(Lu+2) = i kz u, r(Lu+3) = i kz v, r(Lu+4) = i kz T (stratified),
+ * all transformed with u through z_trans_b, x2z_decomp and xy_trans_b into
+ * uu(Nx,Ny,Nz,2 Lu) = u, v, w, [T], p, du/dz, dv/dz, [dT/dz]; the mean profile
+ * of each u field (get_mean with i_remove = 0); the xy planes of all 2 Lu
+ * fields (write_planes.f:34-45); the xz planes of u..p plus y_deriv of the
+ * fields n != 2 (write_planes.f:56-89); the yz planes of u..p plus x_deriv of
+ * the fields n != 1 (write_planes.f:105-131).  Plane indices are 1-based as
+ * in the input deck.  Outputs: xy(Nx,Ny,2Lu,n_xy), xz(Nx,Nz,2Lu,n_xz),
+ * yz(Ny,Nz,2Lu,n_yz), mean(Nz,Lu). */
+int so_planes(so_ctx *c, const double *ud, const double *pd, const int *k_xy, int n_xy, const int *j_xz,
+              int n_xz, const int *i_yz, int n_yz, double *xy, double *xz, double *yz, double *mean) {
+  const so_cplx *u = (const so_cplx *)ud, *p = (const so_cplx *)pd;
+  const int lu = c->lu, nu = lu, nx = c->nx, ny = c->ny, nz = c->nz, n_out = 2 * lu;
+  for (int m = 0; m < n_xy; ++m) if (k_xy[m] < 1 || k_xy[m] > nz) return -1;
+  for (int m = 0; m < n_xz; ++m) if (j_xz[m] < 1 || j_xz[m] > ny) return -1;
+  for (int m = 0; m < n_yz; ++m) if (i_yz[m] < 1 || i_yz[m] > nx) return -1;
+  const size_t nw = (size_t)c->nze * c->ny_min * c->nx_min;
+  const size_t nxy = (size_t)ny * c->nx2 * nz;
+  const size_t npl = (size_t)nx * ny * nz;
+  so_cplx *r2 = (so_cplx *)calloc(nw * nu, sizeof(so_cplx));
+  so_cplx *zb = (so_cplx *)calloc((size_t)c->ny_min * c->nx_min * c->nze * 2 * nu, sizeof(so_cplx));
+  so_cplx *xyb = (so_cplx *)calloc(nxy * 2 * nu, sizeof(so_cplx));
+  double *uu = (double *)malloc(sizeof(double) * npl * n_out);
+  const int dz_src[3] = {0, 1, 3};
+  memcpy(r2, p, sizeof(so_cplx) * nw);
+  for (int f = 1; f < nu; ++f) {
+    const int n = dz_src[f - 1];
+    for (int i = 0; i < c->nx_min; ++i)
+      for (int j = 0; j < c->ny_min; ++j)
+        for (int k = 0; k < c->nz_min; ++k) {
+          const double b = c->wave_z * (double)c->k_z[k];
+          const so_cplx v = u[W_IDX(c, k, j, i, n)];
+          r2[W_IDX(c, k, j, i, f)] = -b * cimag(v) + b * creal(v) * I;
+        }
+  }
+  /* z_trans_b of u into blocks 0..Nu-1 and of r2 into blocks Nu..2Nu-1 */
+  const size_t nzb = (size_t)c->ny_min * c->nx_min * c->nze;
+  so_z_trans_b(c, (const double *)u, (double *)zb, nu);
+  so_z_trans_b(c, (const double *)r2, (double *)(zb + nzb * nu), nu);
+  so_x2z_decomp(c, (const double *)zb, (double *)xyb, 2 * nu);
+  so_xy_trans_b(c, (double *)xyb, uu, 2 * nu);
+  for (int n = 0; n < lu; ++n) {
+    so_cplx *col = (so_cplx *)malloc(sizeof(so_cplx) * (size_t)c->nze);
+    memcpy(col, u + W_IDX(c, 0, 0, 0, n), sizeof(so_cplx) * (size_t)c->nze);
+    so_get_mean(c, (double *)col, 0, mean + (size_t)nz * n);
+    free(col);
+  }
+  for (int m = 0; m < n_xy; ++m)
+    for (int n = 0; n < n_out; ++n)
+      memcpy(xy + (size_t)nx * ny * (n + (size_t)n_out * m), uu + P_IDX(c, 0, 0, k_xy[m] - 1, n),
+             sizeof(double) * nx * ny);
+  double *du = (double *)malloc(sizeof(double) * (size_t)nx * ny);
+  for (int m = 0; m < n_xz; ++m) {
+    const int j = j_xz[m] - 1;
+    double *o = xz + (size_t)nx * nz * n_out * m;
+    for (int n = 0; n <= lu; ++n)
+      for (int k = 0; k < nz; ++k)
+        for (int i = 0; i < nx; ++i) o[i + (size_t)nx * (k + (size_t)nz * n)] = uu[P_IDX(c, i, j, k, n)];
+    for (int k = 0; k < nz; ++k) {
+      int L = 1;
+      for (int n = 0; n < lu; ++n) {
+        if (n == 1) continue;
+        ++L;
+        so_y_deriv(c, uu + P_IDX(c, 0, 0, k, n), du);
+        for (int i = 0; i < nx; ++i) o[i + (size_t)nx * (k + (size_t)nz * (lu + L - 1))] = du[i + (size_t)nx * j];
+      }
+    }
+  }
+  for (int m = 0; m < n_yz; ++m) {
+    const int i = i_yz[m] - 1;
+    double *o = yz + (size_t)ny * nz * n_out * m;
+    for (int n = 0; n <= lu; ++n)
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j) o[j + (size_t)ny * (k + (size_t)nz * n)] = uu[P_IDX(c, i, j, k, n)];
+    for (int k = 0; k < nz; ++k) {
+      int L = 1;
+      for (int n = 0; n < lu; ++n) {
+        if (n == 0) continue;
+        ++L;
+        so_x_deriv(c, uu + P_IDX(c, 0, 0, k, n), du);
+        for (int j = 0; j < ny; ++j) o[j + (size_t)ny * (k + (size_t)nz * (lu + L - 1))] = du[i + (size_t)nx * j];
+      }
+    }
+  }
+  free(du); free(uu); free(xyb); free(zb); free(r2);
+  return 0;
+}

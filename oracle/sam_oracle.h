@@ -111,6 +111,12 @@ int so_write_field(so_ctx *c, const char *fname, const double *u);
 /* 0 ok, -1 open, -2 wrong size (read_field.f:74-80), -3 short read */
 int so_read_field(so_ctx *c, const char *fname, double *u);
 
+/* ---- planes output (sam.f:145-166, write_planes.f): u and p = r(Lu+1) in
+ * wave space; 1-based plane indices; xy(Nx,Ny,2Lu,n_xy), xz(Nx,Nz,2Lu,n_xz),
+ * yz(Ny,Nz,2Lu,n_yz), mean(Nz,Lu); -1 on an index out of range ---- */
+int so_planes(so_ctx *c, const double *u, const double *p, const int *k_xy, int n_xy, const int *j_xz,
+              int n_xz, const int *i_yz, int n_yz, double *xy, double *xz, double *yz, double *mean);
+
 /* ---- one raw FFTPACK-convention transform (0 cfftf, 1 cfftb, 2 rfftf, 3 rfftb) ---- */
 int so_fft_line(int n, int kind, double *data);
 

@@ -29,10 +29,17 @@ __device__ __forceinline__ void load_twiddles(cx_t<T>* s_tw, const cx_t<T>* __re
 // v = get(e) for a batch of e, then put(e, v) for the same batch.
 constexpr int kBatch = 8;
 
-// Resident CTAs per SM the register budget is sized for: two for FP64 (the
-// FP64 pipe needs the second CTA to cover load phases), three for FP32.
-template <typename T> struct MinBlocks { static constexpr int value = 2; };
-template <> struct MinBlocks<double> { static constexpr int value = 1; };
+// Resident CTAs per SM each kernel's register budget is sized for (measured
+// at 256^3): the transpose passes gain from a third FP32 / second FP64 CTA to
+// cover their load phases; the x pass and the FP32 z_fwd epilogue lose more
+// to the tighter register cap than they gain.
+enum PassKind { kPassZInv, kPassYInv, kPassX, kPassYFwd, kPassZFwd };
+template <typename T, int K> struct MinBlocks {
+  static constexpr int value = (K == kPassX || K == kPassZFwd) ? 2 : 3;
+};
+template <int K> struct MinBlocks<double, K> {
+  static constexpr int value = (K == kPassX) ? 1 : 2;
+};
 template <typename V, typename Get, typename Put>
 __device__ __forceinline__ void batched(int count, Get get, Put put) {
   for (int base = threadIdx.x; base < count; base += kBatch * blockDim.x) {
@@ -54,7 +61,7 @@ __device__ __forceinline__ void batched(int count, Get get, Put put) {
 // Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
 // modes; output A(n, z, kx, ky) with ky fastest.
 template <typename T>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -107,7 +114,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_z_inv(ZInvArg
 // hold either Ny_min compact modes (zero band inserted here, as
 // x2z_decomp.f:111-124 does) or Ny values with the band already present.
 template <typename T>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv>::value) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -196,7 +203,7 @@ __device__ __forceinline__ void product_pair(int m, int& a, int& b) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -385,7 +392,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_x_pass(XPassA
 // Tile: field m, kx column i, planes z0 .. z0+TZ-1.  Output D(m, kx, ky, z)
 // keeps |ky| <= ky_max (xy_trans_f.f:45-52).
 template <typename T>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd>::value) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -578,7 +585,7 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
 //   mode 1: rhs epilogue (rhs.f:108-142) into r with u_sav from memory,
 //   mode 2: full stage epilogue: rhs, then sam.f:210-221 and 293-314.
 template <typename T>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T>::value) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;

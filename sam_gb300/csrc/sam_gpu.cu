@@ -19,6 +19,7 @@
 #include "fields.cuh"
 #include "les.cuh"
 #include "passes.cuh"
+#include "planes.cuh"
 
 namespace samgpu {
 
@@ -423,6 +424,89 @@ static void free_ctx(Ctx* c) {
   for (auto& s : c->sc) cudaFree(s.p);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
+}
+
+// Planes output (sam.f:145-166, write_planes.f) on the resident state: the
+// batch u, p, i kz (u, v, [T]), then i ky (u, w, [T]) when xz planes are asked
+// for and i kx (v, w, [T]) when yz planes are, through the inverse passes into
+// physical space, then the plane cuts.  Scratch: sc[0] holds the wave batch,
+// then the physical batch; sc[1] the z-inverse blocks, then the planes; sc[2]
+// the y-inverse blocks; sc[3] the mean columns.
+template <typename T>
+static int planes_impl(Ctx& c, const PlaneSel& sel0, double* xy, double* xz, double* yz, double* mean) {
+  using Cx = cx_t<T>;
+  const Grid& g = c.g;
+  const int lu = g.lu;
+  PlaneFields pf{};
+  PlaneSel sel = sel0;
+  int nf = 0;
+  auto add = [&](int src, int op) {
+    pf.src[nf] = src;
+    pf.op[nf] = op;
+    return nf++;
+  };
+  // the fields write_planes differentiates: z (sam.f:152-157), y (write_planes.f:79-86: n != 2),
+  // x (write_planes.f:119-126: n != 1), as 0-based field numbers
+  const int dz_src[3] = {0, 1, 3}, dy_src[3] = {0, 2, 3}, dx_src[3] = {1, 2, 3};
+  for (int n = 0; n < lu; ++n) add(n, 0);
+  add(-1, 0);
+  for (int m = 0; m < lu - 1; ++m) add(dz_src[m], 1);
+  for (int s = 0; s < 2 * lu; ++s) sel.fxy[s] = s;
+  if (sel.n_xz > 0) {
+    for (int s = 0; s <= lu; ++s) sel.fxz[s] = s;
+    for (int m = 0; m < lu - 1; ++m) sel.fxz[lu + 1 + m] = add(dy_src[m], 2);
+  }
+  if (sel.n_yz > 0) {
+    for (int s = 0; s <= lu; ++s) sel.fyz[s] = s;
+    for (int m = 0; m < lu - 1; ++m) sel.fyz[lu + 1 + m] = add(dx_src[m], 3);
+  }
+  pf.nf = nf;
+  sel.n_out = 2 * lu;
+  const size_t nm = (size_t)g.mx * g.my * g.mz;
+  const size_t vol = (size_t)g.nx * g.ny * g.nz;
+  const size_t n_planes = ((size_t)sel.n_xy * g.nx * g.ny + (size_t)sel.n_xz * g.nx * g.nz +
+                           (size_t)sel.n_yz * g.ny * g.nz) * sel.n_out;
+  const size_t w_bytes = nm * nf * sizeof(Cx), ph_bytes = vol * nf * sizeof(T);
+  const size_t a_bytes = (size_t)nf * g.nz * g.mx * g.my * sizeof(Cx);
+  const size_t b_bytes = (size_t)nf * g.nz * g.ny * g.mx * sizeof(Cx);
+  int rc;
+  if ((rc = ensure(c.sc[0], w_bytes > ph_bytes ? w_bytes : ph_bytes)) ||
+      (rc = ensure(c.sc[1], a_bytes > n_planes * 8 ? a_bytes : n_planes * 8)) || (rc = ensure(c.sc[2], b_bytes)) ||
+      (rc = ensure(c.sc[3], ((size_t)g.mz * 2 + (size_t)g.nz * lu + 8) * 8)))
+    return rc;
+  planes_fields<T>(g, pf, (const Cx*)c.U, (const Cx*)c.P, (Cx*)c.sc[0].p, c.stream);
+  if ((rc = run_z_inv<T>(c, c.sc[0].p, c.sc[1].p, nf, g.mz, (long long)g.my * g.mz, (long long)nm, g.my,
+                         (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my)))
+    return rc;
+  if ((rc = run_y_inv<T>(c, c.sc[1].p, c.sc[2].p, nf, 0, g.my, (long long)g.mx * g.my,
+                         (long long)g.nz * g.mx * g.my, g.mx, (long long)g.ny * g.mx,
+                         (long long)g.nz * g.ny * g.mx)))
+    return rc;
+  if ((rc = run_x_pass<T>(c, 0, 0, nf, c.sc[2].p, nullptr, g.mx, (long long)g.ny * g.mx,
+                          (long long)g.nz * g.ny * g.mx, nullptr, c.sc[0].p, 0, 0, 0, g.nx, (long long)g.nx * g.ny,
+                          (long long)vol, false)))
+    return rc;
+  double* d_xy = (double*)c.sc[1].p;
+  double* d_xz = d_xy + (size_t)sel.n_xy * sel.n_out * g.nx * g.ny;
+  double* d_yz = d_xz + (size_t)sel.n_xz * sel.n_out * g.nx * g.nz;
+  planes_gather<T>(g, sel, (const T*)c.sc[0].p, d_xy, d_xz, d_yz, c.stream);
+  if (mean) {
+    double2* col = (double2*)c.sc[3].p;
+    double* dmean = (double*)(col + g.mz);
+    double* djump = dmean + (size_t)g.nz * lu;
+    for (int n = 0; n < lu; ++n) {
+      convert_out<T>((const Cx*)c.U + (size_t)n * nm, col, g.mz, c.stream);
+      les_get_mean(col, g.mz, g.kz, g.nz, 0, c.pz.d, c.pz.tw64, c.pz.h, dmean + (size_t)n * g.nz, djump, c.stream);
+    }
+    CK(cudaMemcpyAsync(mean, dmean, (size_t)g.nz * lu * 8, cudaMemcpyDeviceToHost, c.stream));
+  }
+  if (sel.n_xy)
+    CK(cudaMemcpyAsync(xy, d_xy, (size_t)sel.n_xy * sel.n_out * g.nx * g.ny * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (sel.n_xz)
+    CK(cudaMemcpyAsync(xz, d_xz, (size_t)sel.n_xz * sel.n_out * g.nx * g.nz * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (sel.n_yz)
+    CK(cudaMemcpyAsync(yz, d_yz, (size_t)sel.n_yz * sel.n_out * g.ny * g.nz * 8, cudaMemcpyDeviceToHost, c.stream));
+  return 0;
 }
 
 }  // namespace samgpu
@@ -1231,6 +1315,36 @@ int sam_gpu_get_mean(double* u, int i_symm, int i_remove, double* u_mean, double
   CK(cudaMemcpyAsync(u, col, (size_t)g.mz * 16, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(u_mean, dmean, (size_t)g.nz * 8, cudaMemcpyDeviceToHost, c.stream));
   CK(cudaMemcpyAsync(jump, djump, 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+int sam_gpu_planes(const int* k_xy, int n_xy, const int* j_xz, int n_xz, const int* i_yz, int n_yz, double* xy,
+                   double* xz, double* yz, double* mean) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (n_xy < 0 || n_xz < 0 || n_yz < 0 || n_xy > SAM_GPU_MAX_PLANES || n_xz > SAM_GPU_MAX_PLANES ||
+      n_yz > SAM_GPU_MAX_PLANES)
+    return fail(SAM_GPU_EINVAL, "planes: plane counts must be 0..%d", SAM_GPU_MAX_PLANES);
+  if ((n_xy && (!k_xy || !xy)) || (n_xz && (!j_xz || !xz)) || (n_yz && (!i_yz || !yz)))
+    return fail(SAM_GPU_EINVAL, "planes: null plane list or output array");
+  if (g.nz < 3) return fail(SAM_GPU_EINVAL, "planes: Nz must be >= 3 (get_mean)");
+  PlaneSel sel{};
+  sel.n_xy = n_xy; sel.n_xz = n_xz; sel.n_yz = n_yz;
+  for (int m = 0; m < n_xy; ++m) {
+    if (k_xy[m] < 1 || k_xy[m] > g.nz) return fail(SAM_GPU_EINVAL, "planes: k_xy(%d) = %d outside 1..%d", m + 1, k_xy[m], g.nz);
+    sel.k_xy[m] = k_xy[m] - 1;
+  }
+  for (int m = 0; m < n_xz; ++m) {
+    if (j_xz[m] < 1 || j_xz[m] > g.ny) return fail(SAM_GPU_EINVAL, "planes: j_xz(%d) = %d outside 1..%d", m + 1, j_xz[m], g.ny);
+    sel.j_xz[m] = j_xz[m] - 1;
+  }
+  for (int m = 0; m < n_yz; ++m) {
+    if (i_yz[m] < 1 || i_yz[m] > g.nx) return fail(SAM_GPU_EINVAL, "planes: i_yz(%d) = %d outside 1..%d", m + 1, i_yz[m], g.nx);
+    sel.i_yz[m] = i_yz[m] - 1;
+  }
+  const int rc = c.cfg.precision == 32 ? planes_impl<float>(c, sel, xy, xz, yz, mean)
+                                       : planes_impl<double>(c, sel, xy, xz, yz, mean);
+  if (rc) return rc;
   return sync_stream(c);
 }
 

@@ -14,7 +14,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_lib", "libsam_gpu.so")
+# SAM_GPU_LIB selects another build of the same library (e.g. a tuning variant)
+LIB_PATH = os.environ.get("SAM_GPU_LIB", os.path.join(HERE, "_lib", "libsam_gpu.so"))
 
 SAM_GPU_OK = 0
 ERRORS = {-1: "EINVAL", -2: "ENOTINIT", -3: "EUNSUPPORTED", -4: "ECUDA", -5: "ENONFINITE"}
@@ -28,7 +29,7 @@ EXPORTS = [
     "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
     "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
     "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
-    "sam_gpu_autotune", "sam_gpu_tiles",
+    "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_planes",
 ]
 
 
@@ -106,6 +107,7 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_get_mean.argtypes = [P, C.c_int, C.c_int, P, P, P]
     lib.sam_gpu_autotune.argtypes = [C.c_int]
     lib.sam_gpu_tiles.argtypes = [P]
+    lib.sam_gpu_planes.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
     lib.sam_gpu_force.argtypes = [P, C.c_int]
     lib.sam_gpu_write_field.argtypes = [C.c_char_p]
     lib.sam_gpu_read_field.argtypes = [C.c_char_p]
@@ -320,6 +322,22 @@ class SamGpu:
         self._check(load_library().sam_gpu_spectra(_p(o)), "spectra")
         return dict(ek=o[:lm], tk=o[lm:2 * lm], dk=o[2 * lm:3 * lm], vt=o[3 * lm:4 * lm],
                     sample=o[4 * lm:5 * lm], energy_w=o[5 * lm], div_rms=o[5 * lm + 1], div_max=o[5 * lm + 2])
+
+    def planes(self, k_xy=(), j_xz=(), i_yz=()):
+        """Planes output of the resident state (sam.f:145-166, write_planes.f),
+        1-based plane indices: xy (Nx,Ny,2Lu,n_xy), xz (Nx,Nz,2Lu,n_xz),
+        yz (Ny,Nz,2Lu,n_yz) and the mean profiles (Nz,Lu)."""
+        lu = self.lu
+        ia = [np.ascontiguousarray(x, dtype=np.int32) for x in (k_xy, j_xz, i_yz)]
+        xy = np.zeros((self.nx, self.ny, 2 * lu, len(ia[0])), order="F")
+        xz = np.zeros((self.nx, self.nz, 2 * lu, len(ia[1])), order="F")
+        yz = np.zeros((self.ny, self.nz, 2 * lu, len(ia[2])), order="F")
+        mean = np.zeros((self.nz, lu), order="F")
+        self._check(load_library().sam_gpu_planes(
+            _p(ia[0]) if len(ia[0]) else None, len(ia[0]), _p(ia[1]) if len(ia[1]) else None, len(ia[1]),
+            _p(ia[2]) if len(ia[2]) else None, len(ia[2]), _p(xy) if len(ia[0]) else None,
+            _p(xz) if len(ia[1]) else None, _p(yz) if len(ia[2]) else None, _p(mean)), "planes")
+        return dict(xy=xy, xz=xz, yz=yz, mean=mean)
 
     def div_check(self):
         o = np.zeros(4)

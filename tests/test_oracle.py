@@ -177,3 +177,52 @@ def test_sm_dm_constant_strain():
     assert np.isfinite(vt).all() and vt.max() > 0
     vt2, cds = o.dm(u)
     assert np.isfinite(vt2).all() and np.isfinite(cds)
+
+
+def _np_phys(o, w, op=None):
+    """numpy synthesis of one wave field (Nze,Ny_min,Nx_min), optionally times
+    i k along axis op ('x', 'y', 'z'), as physical (Nx,Ny,Nz)."""
+    d = o.d
+    nx, ny, nz = d.nx, d.ny, d.nz
+    spec = np.zeros((nz, ny, nx // 2 + 1), complex)
+    for i in range(d.nx_min):
+        for j in range(d.ny_min):
+            ky = j if j <= d.ky_max else j - d.ny_min
+            for k in range(d.nz_min):
+                kz = k if k <= d.kz_max else k - d.nz_min
+                f = {None: 1.0, "x": 1j * i, "y": 1j * ky, "z": 1j * kz}[op]
+                spec[kz % nz, ky % ny, i] = w[k, j, i] * f
+    return np.transpose(np.fft.irfftn(spec, s=(nz, ny, nx), axes=(0, 1, 2), norm="forward"), (2, 1, 0))
+
+
+@pytest.mark.parametrize("strat", [0, 1])
+def test_planes_match_numpy(strat):
+    """sam.f:145-166 + write_planes.f: the oracle's plane cuts, z derivatives,
+    y_deriv / x_deriv columns and mean profiles equal numpy's spectral synthesis."""
+    nx, ny, nz = 16, 12, 20
+    o = O.Oracle(nx=nx, ny=ny, nz=nz, i_strat=strat)
+    d = o.d
+    lu = d.lu
+    u = o.init_random(3)
+    p = o.init_random(11)[..., :1].copy(order="F")
+    k_xy, j_xz, i_yz = [1, 7, 20], [2, 12], [1, 9]
+    r = o.planes(u, p, k_xy, j_xz, i_yz)
+    fields = [_np_phys(o, u[..., n]) for n in range(lu)] + [_np_phys(o, p[..., 0])]
+    dz = [0, 1, 3][: lu - 1]
+    fields += [_np_phys(o, u[..., n], "z") for n in dz]
+    dy = [_np_phys(o, u[..., n], "y") for n in [0, 2, 3][: lu - 1]]
+    dx = [_np_phys(o, u[..., n], "x") for n in [1, 2, 3][: lu - 1]]
+    tol = 1e-13 * max(np.abs(f).max() for f in fields)
+    for m, k in enumerate(k_xy):
+        for s in range(2 * lu):
+            np.testing.assert_allclose(r["xy"][:, :, s, m], fields[s][:, :, k - 1], rtol=0, atol=tol)
+    for m, j in enumerate(j_xz):
+        for s in range(2 * lu):
+            ref = fields[s][:, j - 1, :] if s <= lu else dy[s - lu - 1][:, j - 1, :]
+            np.testing.assert_allclose(r["xz"][:, :, s, m], ref, rtol=0, atol=tol)
+    for m, i in enumerate(i_yz):
+        for s in range(2 * lu):
+            ref = fields[s][i - 1, :, :] if s <= lu else dx[s - lu - 1][i - 1, :, :]
+            np.testing.assert_allclose(r["yz"][:, :, s, m], ref, rtol=0, atol=tol)
+    for n in range(lu):
+        np.testing.assert_allclose(r["mean"][:, n], fields[n].mean(axis=(0, 1)), rtol=0, atol=tol)
