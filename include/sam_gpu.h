@@ -203,6 +203,17 @@ int sam_gpu_force(const double* ek_0, int k_force);
 int sam_gpu_planes(const int* k_xy, int n_xy, const int* j_xz, int n_xz, const int* i_yz, int n_yz, double* xy,
                    double* xz, double* yz, double* mean);
 
+/* Ornstein-Uhlenbeck forcing (no reference counterpart; force.f only clamps
+ * shell energies): the stored modes with 0 < |k| <= k_f (in units of the
+ * box's fundamental wave numbers) carry three complex amplitudes each with
+ * stationary rms sigma per component and correlation time t_l, advanced
+ * exactly (rho = exp(-dt/t_l)) from a splitmix64 counter RNG keyed by seed;
+ * every sam_gpu_step ends with u += dt P(k) a (P the solenoidal projection).
+ * sam_gpu_stage does not force.  k_f <= 0 or sigma = 0 switches it off;
+ * a new call restarts the amplitudes from step 0.  n_modes (may be NULL)
+ * receives the number of forced modes (at most 128). */
+int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, double t_l, int* n_modes);
+
 /* ---- restart files of the resident state ---- */
 /* write_field.f:1 / read_field.f:1  vel.NNNNNN: Lu*Nx_min records of
  * Nz_min x Ny_min complex128; read_field rejects a file of the wrong size */

@@ -97,6 +97,7 @@ def lib():
                                         C.c_double, C.c_double, C.c_double]
         _lib.so_fft_line.argtypes = [C.c_int, C.c_int, P]
         _lib.so_force.argtypes = [P, P, P, C.c_int]
+        _lib.so_set_forcing.argtypes = [P, C.c_ulonglong, C.c_double, C.c_double, C.c_double]
         _lib.so_planes.argtypes = [P, P, P, P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
         _lib.so_write_field.argtypes = [P, C.c_char_p, P]
         _lib.so_read_field.argtypes = [P, C.c_char_p, P]
@@ -269,6 +270,12 @@ class Oracle:
         du = np.zeros_like(u, order="F")
         lib().so_y_deriv(self.h, _p(u), _p(du))
         return du
+
+    def set_forcing(self, seed, k_f=2.5, sigma=0.1, t_l=1.0):
+        n = lib().so_set_forcing(self.h, seed, k_f, sigma, t_l)
+        if n < 0:
+            raise ValueError("too many forced modes")
+        return n
 
     def planes(self, u, p, k_xy=(), j_xz=(), i_yz=()):
         """Planes output of sam.f:145-166 / write_planes.f (1-based plane

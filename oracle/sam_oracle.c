@@ -42,6 +42,13 @@ struct so_ctx {
   so_cplx *zb;   /* z_trans_b output, also x2z temp */
   double *uu;    /* physical fields (Nx,Ny,Nz,Lr) */
   so_cplx *usav; /* (Nz_min,Ny_min,Nx_min,2) */
+  /* Ornstein-Uhlenbeck forcing (so_set_forcing) */
+  int ou_n;
+  long long ou_step;
+  uint64_t ou_seed;
+  double ou_sigma, ou_tl;
+  int ou_k[128][3];
+  so_cplx ou_a[128][3];
 };
 
 static const double SO_PI = 3.14159265358979323846;
@@ -481,10 +488,13 @@ int so_stage(so_ctx *c, double *ud, double *rd, int nrk) {
   return 0;
 }
 
+static void so_ou_apply(so_ctx *c, double *ud);
+
 int so_steps(so_ctx *c, double *u, double *r, int nsteps) {
   for (int s = 0; s < nsteps; ++s) {
     for (int nrk = 1; nrk <= c->cfg.nrk_max; ++nrk) so_stage(c, u, r, nrk);
     c->time += c->dt; /* sam.f:318 */
+    if (c->ou_n > 0) so_ou_apply(c, u);
   }
   return 0;
 }
@@ -1297,4 +1307,78 @@ int so_planes(so_ctx *c, const double *ud, const double *pd, const int *k_xy, in
   }
   free(du); free(uu); free(xyb); free(zb); free(r2);
   return 0;
+}
+
+/* ------------------------------------------------ Ornstein-Uhlenbeck forcing
+ * Not in the reference (force.f only clamps shell energies).  The stored
+ * modes with 0 < |k| <= k_f, kx = 0 modes only in the half ky > 0 or
+ * (ky = 0, kz > 0), in the order kx, ky, kz ascending; per mode three complex
+ * amplitudes a with a(0) = sigma xi(0) and, after each step n,
+ * u += dt P(k) a (mirror mode of kx = 0 gets the conjugate), then
+ * a <- rho a + sigma sqrt(1 - rho^2) xi(n), rho = exp(-dt / T_L),
+ * xi = (g1 + i g2)/sqrt(2), g1 + i g2 = sqrt(-2 ln(1 - u1)) e^{2 pi i u2}
+ * (Box-Muller) with u1, u2 splitmix64 uniforms keyed by (seed, n, mode, q). */
+static double so_ou_uniform(uint64_t seed, long long step, int mode, int q) {
+  uint64_t ctr = ((uint64_t)step << 20) ^ ((uint64_t)mode << 4) ^ (uint64_t)q;
+  uint64_t x = so_mix64(seed ^ so_mix64(ctr ^ 0xA5A5A5A5A5A5A5A5ULL));
+  return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+
+static so_cplx so_ou_xi(uint64_t seed, long long step, int mode, int comp) {
+  double u1 = 1.0 - so_ou_uniform(seed, step, mode, 2 * comp);
+  double u2 = so_ou_uniform(seed, step, mode, 2 * comp + 1);
+  double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+  return rad * cos(2.0 * SO_PI * u2) + rad * sin(2.0 * SO_PI * u2) * I;
+}
+
+int so_set_forcing(so_ctx *c, unsigned long long seed, double k_f, double sigma, double t_l) {
+  c->ou_n = 0;
+  if (k_f <= 0.0 || sigma == 0.0) return 0;
+  int kk = (int)floor(k_f);
+  for (int kx = 0; kx <= kk; ++kx)
+    for (int ky = -kk; ky <= kk; ++ky)
+      for (int kz = -kk; kz <= kk; ++kz) {
+        double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
+        if (k2 == 0.0 || k2 > k_f * k_f) continue;
+        if (kx == 0 && !(ky > 0 || (ky == 0 && kz > 0))) continue;
+        if (kx > c->kx_max || abs(ky) > c->ky_max || abs(kz) > c->kz_max) continue;
+        if (c->ou_n >= 128) return -1;
+        c->ou_k[c->ou_n][0] = kx; c->ou_k[c->ou_n][1] = ky; c->ou_k[c->ou_n][2] = kz;
+        ++c->ou_n;
+      }
+  c->ou_seed = seed; c->ou_sigma = sigma; c->ou_tl = t_l; c->ou_step = 0;
+  for (int m = 0; m < c->ou_n; ++m)
+    for (int q = 0; q < 3; ++q) c->ou_a[m][q] = sigma * so_ou_xi(seed, 0, m, q);
+  return c->ou_n;
+}
+
+static void so_ou_apply(so_ctx *c, double *ud) {
+  so_cplx *u = (so_cplx *)ud;
+  const long long step = c->ou_step + 1;
+  const double dt = c->dt;
+  const double rho = exp(-dt / c->ou_tl), amp = c->ou_sigma * sqrt(1.0 - rho * rho);
+  for (int m = 0; m < c->ou_n; ++m) {
+    int kx = c->ou_k[m][0], ky = c->ou_k[m][1], kz = c->ou_k[m][2];
+    double kv[3] = {c->wave_x * kx, c->wave_y * ky, c->wave_z * kz};
+    double k2 = kv[0] * kv[0] + kv[1] * kv[1] + kv[2] * kv[2];
+    so_cplx *a = c->ou_a[m];
+    double dr = (kv[0] * creal(a[0]) + kv[1] * creal(a[1]) + kv[2] * creal(a[2])) / k2;
+    double di = (kv[0] * cimag(a[0]) + kv[1] * cimag(a[1]) + kv[2] * cimag(a[2])) / k2;
+    int j = ky >= 0 ? ky : ky + c->ny_min, k = kz >= 0 ? kz : kz + c->nz_min;
+    int jm = ky > 0 ? c->ny_min - ky : -ky, km = kz > 0 ? c->nz_min - kz : -kz;
+    for (int q = 0; q < 3; ++q) {
+      double fr = (creal(a[q]) - kv[q] * dr) * dt, fi = (cimag(a[q]) - kv[q] * di) * dt;
+      so_cplx *p = &u[W_IDX(c, k, j, kx, q)];
+      *p = (creal(*p) + fr) + (cimag(*p) + fi) * I;
+      if (kx == 0) {
+        so_cplx *pm = &u[W_IDX(c, km, jm, 0, q)];
+        *pm = (creal(*pm) + fr) + (cimag(*pm) - fi) * I;
+      }
+    }
+    for (int q = 0; q < 3; ++q) {
+      so_cplx xi = so_ou_xi(c->ou_seed, step, m, q);
+      a[q] = (rho * creal(a[q]) + amp * creal(xi)) + (rho * cimag(a[q]) + amp * cimag(xi)) * I;
+    }
+  }
+  c->ou_step = step;
 }

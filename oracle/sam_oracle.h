@@ -107,6 +107,9 @@ int so_init_packet(so_ctx *c, double *u, unsigned long long seed, int kx0, int k
 
 /* ---- forcing and restart files ---- */
 int so_force(so_ctx *c, double *u, const double *ek_0, int k_force);
+/* Ornstein-Uhlenbeck forcing of 0 < |k| <= k_f applied by so_steps after
+ * every step; returns the number of forced modes, -1 above 128 */
+int so_set_forcing(so_ctx *c, unsigned long long seed, double k_f, double sigma, double t_l);
 int so_write_field(so_ctx *c, const char *fname, const double *u);
 /* 0 ok, -1 open, -2 wrong size (read_field.f:74-80), -3 short read */
 int so_read_field(so_ctx *c, const char *fname, double *u);

@@ -262,6 +262,106 @@ template <typename T>
 void convert_out(const cx_t<T>* src, double2* dst, long long n, cudaStream_t s) {
   k_convert_out<T><<<grid_for(n), kThreads, 0, s>>>(src, dst, n);
 }
+// ------------------------------------------------ Ornstein-Uhlenbeck forcing
+// Low-wavenumber stochastic forcing: every stored mode with 0 < |k| <= k_f
+// (kx = 0 modes only in the half ky > 0 or ky = 0, kz > 0; their mirror images
+// get the conjugate) carries three complex amplitudes a that follow an exact
+// OU discretisation a <- rho a + sigma sqrt(1 - rho^2) xi, rho = exp(-dt/T_L),
+// xi = (g1 + i g2)/sqrt(2) with g from Box-Muller on two splitmix64 uniforms
+// keyed by (seed, step, mode, component).  After each step the velocity gets
+// u += dt P(k) a (P the solenoidal projection), then a advances one step.
+
+__device__ __forceinline__ double ou_uniform(uint64_t seed, long long step, int mode, int q) {
+  const uint64_t ctr = ((uint64_t)step << 20) ^ ((uint64_t)mode << 4) ^ (uint64_t)q;
+  const uint64_t x = mix64(seed ^ mix64(ctr ^ 0xA5A5A5A5A5A5A5A5ULL));
+  return (double)(x >> 11) * (1.0 / 9007199254740992.0);
+}
+
+__device__ __forceinline__ double2 ou_xi(uint64_t seed, long long step, int mode, int comp) {
+  const double u1 = 1.0 - ou_uniform(seed, step, mode, 2 * comp);  // (0, 1]
+  const double u2 = ou_uniform(seed, step, mode, 2 * comp + 1);
+  const double rad = sqrt(-2.0 * log(u1)) * 0.70710678118654752440;
+  double sn, cs;
+  sincospi(2.0 * u2, &sn, &cs);
+  return make_double2(rad * cs, rad * sn);
+}
+
+__global__ void k_ou_init(OuForcing* f) {
+  const int m = threadIdx.x;
+  if (m >= f->n_modes) return;
+  for (int c = 0; c < 3; ++c) {
+    const double2 xi = ou_xi(f->seed, 0, m, c);
+    f->a[m][c] = make_double2(f->sigma * xi.x, f->sigma * xi.y);
+  }
+  if (m == 0) f->step = 0;
+}
+
+template <typename T>
+__global__ void k_ou_apply(cx_t<T>* u, Grid g, OuForcing* f, const DevState* st) {
+  using C = cx_t<T>;
+  const int m = threadIdx.x;
+  const long long step = f->step + 1;
+  if (m < f->n_modes) {
+    const double dt = st->dt;
+    const int kx = f->kx[m], ky = f->ky[m], kz = f->kz[m];
+    const double wx = g.wave_x * kx, wy = g.wave_y * ky, wz = g.wave_z * kz;
+    const double k2 = wx * wx + wy * wy + wz * wz;
+    double2 a[3] = {f->a[m][0], f->a[m][1], f->a[m][2]};
+    const double dr = (wx * a[0].x + wy * a[1].x + wz * a[2].x) / k2;
+    const double di = (wx * a[0].y + wy * a[1].y + wz * a[2].y) / k2;
+    const double kv[3] = {wx, wy, wz};
+    const long long nm = (long long)g.mx * g.my * g.mz;
+    const int jy = ky >= 0 ? ky : ky + g.my, jz = kz >= 0 ? kz : kz + g.mz;
+    const long long at = ((long long)kx * g.my + jy) * g.mz + jz;
+    const long long mirror = kx == 0 ? ((long long)(ky > 0 ? g.my - ky : -ky) * g.mz + (kz > 0 ? g.mz - kz : -kz)) : -1;
+    for (int c = 0; c < 3; ++c) {
+      const double fr = (a[c].x - kv[c] * dr) * dt, fi = (a[c].y - kv[c] * di) * dt;
+      C* p = u + c * nm + at;
+      *p = mk<C>(p->x + (T)fr, p->y + (T)fi);
+      if (mirror >= 0) {
+        C* q = u + c * nm + mirror;
+        *q = mk<C>(q->x + (T)fr, q->y - (T)fi);
+      }
+    }
+    const double rho = exp(-dt / f->t_l);
+    const double amp = f->sigma * sqrt(1.0 - rho * rho);
+    for (int c = 0; c < 3; ++c) {
+      const double2 xi = ou_xi(f->seed, step, m, c);
+      f->a[m][c] = make_double2(rho * a[c].x + amp * xi.x, rho * a[c].y + amp * xi.y);
+    }
+  }
+  __syncthreads();
+  if (m == 0) f->step = step;
+}
+
+int ou_modes(const Grid& g, double k_f, OuForcing& f) {
+  f.n_modes = 0;
+  const int kk = (int)floor(k_f);
+  for (int kx = 0; kx <= kk; ++kx)
+    for (int ky = -kk; ky <= kk; ++ky)
+      for (int kz = -kk; kz <= kk; ++kz) {
+        const double k2 = (double)kx * kx + (double)ky * ky + (double)kz * kz;
+        if (k2 == 0.0 || k2 > k_f * k_f) continue;
+        if (kx == 0 && !(ky > 0 || (ky == 0 && kz > 0))) continue;
+        if (kx > g.kx || abs(ky) > g.ky || abs(kz) > g.kz) continue;
+        if (f.n_modes >= kOuModesMax) return -1;
+        f.kx[f.n_modes] = kx;
+        f.ky[f.n_modes] = ky;
+        f.kz[f.n_modes] = kz;
+        ++f.n_modes;
+      }
+  return f.n_modes;
+}
+
+void ou_init(OuForcing* dev, cudaStream_t s) { k_ou_init<<<1, kOuModesMax, 0, s>>>(dev); }
+
+template <typename T>
+void ou_apply(cx_t<T>* u, const Grid& g, OuForcing* dev, const DevState* st, cudaStream_t s) {
+  k_ou_apply<T><<<1, kOuModesMax, 0, s>>>(u, g, dev, st);
+}
+template void ou_apply<float>(float2*, const Grid&, OuForcing*, const DevState*, cudaStream_t);
+template void ou_apply<double>(double2*, const Grid&, OuForcing*, const DevState*, cudaStream_t);
+
 template void convert_in<float>(const double2*, float2*, long long, cudaStream_t);
 template void convert_out<float>(const float2*, double2*, long long, cudaStream_t);
 template void convert_in<double>(const double2*, double2*, long long, cudaStream_t);

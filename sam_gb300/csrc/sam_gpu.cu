@@ -161,6 +161,7 @@ struct Ctx {
   Scratch sc[4];
   // tile choices
   int ty_zi = 16, tx_yi = 16, yt_x = 8, grp_x = 9, tz_yf = 16, ty_zf = 4;
+  OuForcing* ou = nullptr;  // device OU forcing state, null when off
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t graph_stream = nullptr;
   int graph_stale = 1;
@@ -420,7 +421,7 @@ static void free_ctx(Ctx* c) {
   free_plan(c->px); free_plan(c->py); free_plan(c->pz);
   cudaFree(c->U); cudaFree(c->R); cudaFree(c->P);
   cudaFree(c->S1); cudaFree(c->S2); cudaFree(c->S3);
-  cudaFree(c->partials); cudaFree(c->state);
+  cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou);
   for (auto& s : c->sc) cudaFree(s.p);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -894,6 +895,10 @@ int sam_gpu_step(int nsteps) {
     CK(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
     int rc = 0;
     for (int nrk = 1; nrk <= c.cfg.nrk_max && !rc; ++nrk) rc = stage_any(c, nrk);
+    if (!rc && c.ou) {
+      if (c.cfg.precision == 32) ou_apply<float>((float2*)c.U, c.g, c.ou, c.state, c.stream);
+      else ou_apply<double>((double2*)c.U, c.g, c.ou, c.state, c.stream);
+    }
     cudaError_t e = cudaStreamEndCapture(c.stream, &graph);
     if (rc) return rc;
     if (e != cudaSuccess) return fail(SAM_GPU_ECUDA, "graph capture: %s", cudaGetErrorString(e));
@@ -905,6 +910,31 @@ int sam_gpu_step(int nsteps) {
   for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(c.gexec, c.stream));
   c.nrk = c.cfg.nrk_max;
   return check_launch();
+}
+
+int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, double t_l, int* n_modes) {
+  NEED_CTX();
+  if (n_modes) *n_modes = 0;
+  if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+  if (k_f <= 0.0 || sigma == 0.0) {
+    cudaFree(c.ou);
+    c.ou = nullptr;
+    return 0;
+  }
+  if (!(t_l > 0.0) || !(sigma > 0.0) || !(k_f < 1e3))
+    return fail(SAM_GPU_EINVAL, "set_forcing: need sigma > 0, T_L > 0 and a finite k_f");
+  OuForcing h{};
+  const int n = ou_modes(c.g, k_f, h);
+  if (n < 0) return fail(SAM_GPU_EINVAL, "set_forcing: more than %d modes with |k| <= %g", kOuModesMax, k_f);
+  if (n == 0) return fail(SAM_GPU_EINVAL, "set_forcing: no stored mode with 0 < |k| <= %g", k_f);
+  h.seed = seed;
+  h.sigma = sigma;
+  h.t_l = t_l;
+  if (!c.ou) CK(cudaMalloc(&c.ou, sizeof(OuForcing)));
+  CK(cudaMemcpyAsync(c.ou, &h, sizeof(OuForcing), cudaMemcpyHostToDevice, c.stream));
+  ou_init(c.ou, c.stream);
+  if (n_modes) *n_modes = n;
+  return sync_stream(c);
 }
 
 int sam_gpu_measure_fp64_peak(double* tflops) {

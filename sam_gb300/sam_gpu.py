@@ -30,6 +30,7 @@ EXPORTS = [
     "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
     "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
     "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_planes",
+    "sam_gpu_set_forcing",
 ]
 
 
@@ -107,6 +108,7 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_get_mean.argtypes = [P, C.c_int, C.c_int, P, P, P]
     lib.sam_gpu_autotune.argtypes = [C.c_int]
     lib.sam_gpu_tiles.argtypes = [P]
+    lib.sam_gpu_set_forcing.argtypes = [C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int)]
     lib.sam_gpu_planes.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
     lib.sam_gpu_force.argtypes = [P, C.c_int]
     lib.sam_gpu_write_field.argtypes = [C.c_char_p]
@@ -322,6 +324,13 @@ class SamGpu:
         self._check(load_library().sam_gpu_spectra(_p(o)), "spectra")
         return dict(ek=o[:lm], tk=o[lm:2 * lm], dk=o[2 * lm:3 * lm], vt=o[3 * lm:4 * lm],
                     sample=o[4 * lm:5 * lm], energy_w=o[5 * lm], div_rms=o[5 * lm + 1], div_max=o[5 * lm + 2])
+
+    def set_forcing(self, seed, k_f=2.5, sigma=0.1, t_l=1.0):
+        """Ornstein-Uhlenbeck forcing of 0 < |k| <= k_f applied after every
+        step(); returns the number of forced modes (k_f <= 0 switches it off)."""
+        n = C.c_int(0)
+        self._check(load_library().sam_gpu_set_forcing(seed, k_f, sigma, t_l, C.byref(n)), "set_forcing")
+        return n.value
 
     def planes(self, k_xy=(), j_xz=(), i_yz=()):
         """Planes output of the resident state (sam.f:145-166, write_planes.f),

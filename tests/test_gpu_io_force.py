@@ -76,3 +76,46 @@ def test_restart_failure_paths(gpu_lib, tmp_path):
     open(h, "w").write(text)
     with pytest.raises(SamGpuError, match="nx differs"):
         g.read_header(h)
+
+
+@pytest.mark.parametrize("strat", [0, 1])
+def test_ou_forcing_matches_oracle(gpu_lib, strat):
+    """Stochastic low-wavenumber forcing inside sam_gpu_step against the
+    oracle's so_steps with the same seed, over several steps with CFL dt."""
+    cfg = dict(nx=24, ny=16, nz=32, i_strat=strat, buoy_fac_z=1.0 * strat, lapse=1.0 * strat, vis=1e-3,
+               i_cfl=1, cfl0=0.5)
+    g, o = SamGpu(**cfg), O.Oracle(**cfg)
+    u = o.init_random(4)
+    r = o.wave(o.d.lr)
+    g.upload(u)
+    assert g.set_forcing(11, k_f=2.5, sigma=0.5, t_l=0.3) == o.set_forcing(11, k_f=2.5, sigma=0.5, t_l=0.3)
+    o.steps(u, r, 6)
+    g.step(6)
+    ug = g.download()
+    for n in range(o.d.lu):
+        assert np.abs(ug[..., n] - u[..., n]).max() <= 1e-12 * np.abs(u[..., n]).max(), n
+
+
+def test_ou_forcing_off_and_restart(gpu_lib):
+    cfg = dict(nx=16, ny=16, nz=16, vis=1e-3)
+    g = SamGpu(**cfg)
+    g.init_taylor_green()
+    u0 = g.download()
+    g.set_forcing(1, k_f=2.5, sigma=0.5, t_l=1.0)
+    g.set_forcing(1, k_f=0.0)
+    g.step(2)
+    g2 = SamGpu(**cfg)
+    g2.init_taylor_green()
+    g2.step(2)
+    assert np.array_equal(g.download(), g2.download())
+    # a new set_forcing restarts the amplitude sequence from step 0
+    g.upload(u0)
+    g.set_forcing(5, k_f=2.0, sigma=0.2, t_l=1.0)
+    g.step(2)
+    a = g.download()
+    g.upload(u0)
+    g.set_forcing(5, k_f=2.0, sigma=0.2, t_l=1.0)
+    g.step(2)
+    assert np.array_equal(g.download(), a)
+    with pytest.raises(SamGpuError, match="EINVAL"):
+        g.set_forcing(5, k_f=2.0, sigma=0.2, t_l=0.0)

@@ -226,3 +226,67 @@ def test_planes_match_numpy(strat):
             np.testing.assert_allclose(r["yz"][:, :, s, m], ref, rtol=0, atol=tol)
     for n in range(lu):
         np.testing.assert_allclose(r["mean"][:, n], fields[n].mean(axis=(0, 1)), rtol=0, atol=tol)
+
+
+def _kvec(o, shape):
+    """Integer wave numbers (kz, ky, kx) of the wave-space layout (stored
+    order of fft_init.f:52-78: non-negative first, then negative)."""
+    d = o.d
+    kz = np.array([k if k <= d.kz_max else k - d.nz_min for k in range(d.nz_min)])
+    ky = np.array([k if k <= d.ky_max else k - d.ny_min for k in range(d.ny_min)])
+    kx = np.arange(d.nx_min)
+    return np.meshgrid(kz, ky, kx, indexing="ij")
+
+
+def test_ou_forcing_from_rest():
+    """Ornstein-Uhlenbeck forcing applied to a fluid at rest: after one step
+    only the modes 0 < |k| <= k_f hold energy, the forced field is
+    solenoidal, and the kx = 0 plane keeps the conjugate symmetry of a real
+    field; the same seed gives the same field, another seed another."""
+    cfg = dict(nx=24, ny=24, nz=24, vis=0.0, dt0=0.01)
+    o = O.Oracle(**cfg)
+    assert o.set_forcing(7, k_f=2.5, sigma=0.3, t_l=0.5) == 40
+    u = o.wave(o.d.lu)
+    r = o.wave(o.d.lr)
+    o.steps(u, r, 1)
+    d = o.d
+    kz, ky, kx = _kvec(o, None)
+    k2 = kz ** 2 + ky ** 2 + kx ** 2
+    um = u[: d.nz_min]
+    mag = np.abs(um).sum(axis=-1)
+    assert mag[(k2 > 6.25) | (k2 == 0)].max() == 0.0
+    assert (mag[(k2 <= 6.25) & (k2 > 0)] > 0).all()
+    div = kx * um[..., 0] + ky * um[..., 1] + kz * um[..., 2]
+    assert np.abs(div).max() < 1e-15 * np.abs(um).max() * 4
+    for j in range(d.ny_min):
+        for k in range(d.nz_min):
+            jm, km = (-j) % d.ny_min, (-k) % d.nz_min
+            assert np.allclose(um[k, j, 0], np.conj(um[km, jm, 0]), rtol=0, atol=1e-17)
+    o2 = O.Oracle(**cfg)
+    o2.set_forcing(7, k_f=2.5, sigma=0.3, t_l=0.5)
+    u2, r2 = o2.wave(d.lu), o2.wave(d.lr)
+    o2.steps(u2, r2, 1)
+    assert np.array_equal(u2, u)
+    o3 = O.Oracle(**cfg)
+    o3.set_forcing(8, k_f=2.5, sigma=0.3, t_l=0.5)
+    u3, r3 = o3.wave(d.lu), o3.wave(d.lr)
+    o3.steps(u3, r3, 1)
+    assert not np.array_equal(u3, u)
+
+
+def test_ou_forcing_stationary_variance():
+    """With dt / T_L small the injected velocity after n steps from rest is
+    dt * sum of correlated amplitudes; over many modes the per-component
+    mean square of u / (n dt) approaches sigma^2 times the solenoidal share
+    (2/3) for n dt << T_L.  A loose statistical check of the RNG scaling."""
+    o = O.Oracle(nx=32, ny=32, nz=32, vis=0.0, dt0=1e-4)
+    n = o.set_forcing(3, k_f=2.5, sigma=1.0, t_l=100.0)
+    u, r = o.wave(o.d.lu), o.wave(o.d.lr)
+    o.steps(u, r, 1)
+    kz, ky, kx = _kvec(o, None)
+    k2 = kz ** 2 + ky ** 2 + kx ** 2
+    sel = (k2 > 0) & (k2 <= 6.25) & ((kx > 0) | (ky > 0) | ((ky == 0) & (kz > 0)))
+    amp = u[: o.d.nz_min][sel] / 1e-4
+    ms = (np.abs(amp) ** 2).sum(axis=-1).mean()
+    assert sel.sum() == n
+    assert 0.5 * 2.0 < ms < 1.5 * 2.0
