@@ -214,6 +214,24 @@ int sam_gpu_planes(const int* k_xy, int n_xy, const int* j_xz, int n_xz, const i
  * receives the number of forced modes (at most 128). */
 int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, double t_l, int* n_modes);
 
+/* Subgrid closure coupled into the resident step (no reference counterpart:
+ * sm.f and dm.f are never linked, and rhs.f applies no eddy viscosity).
+ * With a model on, every stage also takes the strain S_ab = (i/2)(k_b u_a +
+ * k_a u_b) and (stratified) dT/dx_a = i k_a T to physical space and forms
+ *   T_ab = u_a u_b - 2 nu_t S_ab,  T_aT = u_a T - kappa_t dT/dx_a
+ * in place of rhs.f:49-57's products, nu_t = C delta^2 |S|,
+ * |S| = sqrt(2 S_ab S_ab), kappa_t = nu_t / pr_t, delta^2 = (dx dy dz)^(2/3).
+ *   model 0: off (the reference's products);
+ *   model 1: Smagorinsky, C delta^2 = c_smag delta^2 (sm.f:32);
+ *   model 2: dynamic Smagorinsky: C delta^2 is dm.f's volume-averaged
+ *            coefficient (dm.f:176) of the physical velocity, evaluated at
+ *            stage 1 of every step (as vel_max is, rhs.f:26-28) and clipped
+ *            at zero; it starts at 0 until the first stage 1.
+ * Allocates the extra pencil and dm.f work buffers on first use. */
+int sam_gpu_set_les(int model, double c_smag, double pr_t);
+/* C delta^2 last used (0 with the closure off) */
+int sam_gpu_les_coef(double* c_delta_sq);
+
 /* ---- restart files of the resident state ---- */
 /* write_field.f:1 / read_field.f:1  vel.NNNNNN: Lu*Nx_min records of
  * Nz_min x Ny_min complex128; read_field rejects a file of the wrong size */

@@ -98,6 +98,9 @@ def lib():
         _lib.so_fft_line.argtypes = [C.c_int, C.c_int, P]
         _lib.so_force.argtypes = [P, P, P, C.c_int]
         _lib.so_set_forcing.argtypes = [P, C.c_ulonglong, C.c_double, C.c_double, C.c_double]
+        _lib.so_set_les.argtypes = [P, C.c_int, C.c_double, C.c_double]
+        _lib.so_les_coef.argtypes = [P]
+        _lib.so_les_coef.restype = C.c_double
         _lib.so_planes.argtypes = [P, P, P, P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
         _lib.so_write_field.argtypes = [P, C.c_char_p, P]
         _lib.so_read_field.argtypes = [P, C.c_char_p, P]
@@ -276,6 +279,16 @@ class Oracle:
         if n < 0:
             raise ValueError("too many forced modes")
         return n
+
+    def set_les(self, model, c_smag=0.01, pr_t=1.0):
+        """Subgrid closure coupled into stage(): 0 off, 1 Smagorinsky,
+        2 dynamic (dm.f coefficient at nrk = 1); kappa_t = nu_t / pr_t."""
+        if lib().so_set_les(self.h, model, c_smag, pr_t):
+            raise ValueError("bad LES arguments")
+
+    def les_coef(self):
+        """C delta^2 last used by the coupled closure."""
+        return lib().so_les_coef(self.h)
 
     def planes(self, u, p, k_xy=(), j_xz=(), i_yz=()):
         """Planes output of sam.f:145-166 / write_planes.f (1-based plane

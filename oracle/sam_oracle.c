@@ -49,6 +49,16 @@ struct so_ctx {
   double ou_sigma, ou_tl;
   int ou_k[128][3];
   so_cplx ou_a[128][3];
+  /* subgrid closure coupled into the stage (so_set_les) */
+  int les_model;      /* 0 off, 1 Smagorinsky, 2 dynamic (dm.f coefficient) */
+  int les_stage;      /* set by so_stage while the gradient fields are valid */
+  double les_cds;     /* C delta^2 in use */
+  double les_c_smag, les_prt_inv;
+  so_cplx *les_w;     /* derived wave fields (Nze, Ny_min, Nx_min, Lr) */
+  so_cplx *les_zb;    /* their z_trans_b blocks */
+  double *les_g;      /* physical gradient fields (Nx, Ny, Nz, Lr) */
+  double *les_uh;     /* haloed velocity (Lx, Ly, Lz, 3) for so_dm */
+  double *les_vt;     /* haloed vt of so_dm */
 };
 
 static const double SO_PI = 3.14159265358979323846;
@@ -147,6 +157,7 @@ void so_destroy(so_ctx *c) {
   so_cplan_free(&c->py); so_cplan_free(&c->pz);
   free(c->k_x); free(c->k_y); free(c->k_z);
   free(c->zb); free(c->uu); free(c->usav);
+  free(c->les_w); free(c->les_zb); free(c->les_g); free(c->les_uh); free(c->les_vt);
   free(c);
 }
 
@@ -362,6 +373,11 @@ int so_vel_max(so_ctx *c, const double *u) {
   return 0;
 }
 
+static void so_les_fields(so_ctx *c, const so_cplx *u);
+static double delta_sq_of(const so_ctx *c);
+static void periodicity3(const so_ctx *c, double *f);
+static void so_les_stress(so_ctx *c, const double *uu, int nrk);
+
 /* rhs.f:11-142.  On entry uu(Nx,Ny,Nz,Lr) holds the physical fields in its
  * first Lu slots.  On exit r(:,:,:,1..Lu) holds the projected right-hand side
  * and r(:,:,:,Lu+1) the pressure. */
@@ -370,6 +386,9 @@ int so_rhs(so_ctx *c, double *uu, double *rd, const double *usd, int nrk) {
   const so_cplx *usav = (const so_cplx *)usd;
   if (nrk == 1) so_vel_max(c, uu);
   const size_t np = (size_t)c->nx * c->ny * c->nz;
+  const int les = c->les_stage;
+  if (les) so_les_stress(c, uu, nrk);
+  const double *g = c->les_g;
   /* rhs.f:32-61: the nine (six) products in upper-triangle column order */
   set_threads(c);
 #pragma omp parallel for schedule(static)
@@ -387,6 +406,8 @@ int so_rhs(so_ctx *c, double *uu, double *rd, const double *usd, int nrk) {
     uu[p + 2 * np] = b * b;
     uu[p + 1 * np] = a * b;
     uu[p] = a * a;
+    if (les)
+      for (int m = 0; m < c->lr; ++m) uu[p + m * np] += g[p + m * np];
   }
   so_xy_trans_f(c, uu, rd, c->lr);
   so_z2x_decomp(c, rd, rd, c->lr);
@@ -436,6 +457,14 @@ int so_stage(so_ctx *c, double *ud, double *rd, int nrk) {
   so_cplx *r = (so_cplx *)rd;
   const int lu = c->lu;
   so_z_trans_b(c, ud, (double *)c->zb, lu);
+  if (c->les_model) {
+    /* gradient fields of the current u to physical space */
+    so_les_fields(c, u);
+    so_z_trans_b(c, (const double *)c->les_w, (double *)c->les_zb, c->lr);
+    so_x2z_decomp(c, (const double *)c->les_zb, c->les_g, c->lr);
+    so_xy_trans_b(c, c->les_g, c->les_g, c->lr);
+    c->les_stage = 1;
+  }
   if (c->cfg.i_strat) {
     /* sam.f:175-195 */
     size_t st = (size_t)c->nz_min * c->ny_min * c->nx_min;
@@ -462,6 +491,7 @@ int so_stage(so_ctx *c, double *ud, double *rd, int nrk) {
   so_xy_trans_b(c, c->uu, c->uu, lu);
   /* sam.f:244 */
   so_rhs(c, c->uu, rd, (const double *)c->usav, nrk);
+  c->les_stage = 0;
   /* sam.f:293-314 */
   const double dt_fac1 = c->gamma[nrk - 1] * c->dt;
   const double dt_fac = dt_fac1 + dt_fac2;
@@ -1382,3 +1412,90 @@ static void so_ou_apply(so_ctx *c, double *ud) {
   }
   c->ou_step = step;
 }
+
+/* ------------------------------------------------ subgrid closure coupling
+ * Not in the reference: sm.f and dm.f are never linked and nothing adds an
+ * eddy viscosity to rhs.f.  The coupling restated here:
+ *   T_ab = u_a u_b - 2 nu_t S_ab   (the six velocity products of rhs.f:49-54)
+ *   T_aT = u_a T - kappa_t dT/dx_a (the three buoyancy products)
+ *   nu_t = C delta^2 |S|, |S| = sqrt(2 sum ifact S_n^2), kappa_t = nu_t / Pr_t
+ * with S_ab = (i/2)(k_b u_a + k_a u_b) and dT/dx_a = i k_a T formed in wave
+ * space from the stage's u (before the pre-update, like z_trans_b) and taken
+ * to physical space with the same backward transforms as u.  Field m of the
+ * gradient set is the one product m needs (same upper-triangle order).
+ * C delta^2 is c_smag delta^2 (model 1, sm.f:32) or, for model 2, the
+ * volume-averaged coefficient of dm.f evaluated at nrk = 1 of every step on
+ * the physical velocity (like vel_max, rhs.f:26-28) and clipped at zero. */
+static void so_les_fields(so_ctx *c, const so_cplx *u) {
+  static const int pa[6] = {0, 0, 1, 0, 1, 2}, pb[6] = {0, 1, 1, 2, 2, 2};
+  so_cplx *w = c->les_w;
+  set_threads(c);
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int i = 0; i < c->nx_min; ++i)
+    for (int j = 0; j < c->ny_min; ++j)
+      for (int k = 0; k < c->nz_min; ++k) {
+        const double kv[3] = {c->wave_x * c->k_x[i], c->wave_y * c->k_y[j], c->wave_z * c->k_z[k]};
+        for (int m = 0; m < 6; ++m) {
+          const int a = pa[m], b = pb[m];
+          so_cplx v;
+          if (a == b) v = I * kv[a] * u[W_IDX(c, k, j, i, a)];
+          else v = 0.5 * I * (kv[b] * u[W_IDX(c, k, j, i, a)] + kv[a] * u[W_IDX(c, k, j, i, b)]);
+          w[W_IDX(c, k, j, i, m)] = v;
+        }
+        if (c->cfg.i_strat)
+          for (int a = 0; a < 3; ++a) w[W_IDX(c, k, j, i, 6 + a)] = I * kv[a] * u[W_IDX(c, k, j, i, 3)];
+      }
+}
+
+static void so_les_stress(so_ctx *c, const double *uu, int nrk) {
+  const int nx = c->nx, ny = c->ny, nz = c->nz;
+  const size_t np = (size_t)nx * ny * nz;
+  if (c->les_model == 2 && nrk == 1) {
+    /* dm.f on the physical velocity with periodic halos */
+    const size_t vol = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+    for (int n = 0; n < 3; ++n) {
+      double *h = c->les_uh + vol * n;
+      for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+          for (int i = 0; i < nx; ++i) h[H3(c, i + 1, j + 1, k + 1)] = uu[P_IDX(c, i, j, k, n)];
+      periodicity3(c, h);
+    }
+    const double cds = so_dm(c, c->les_uh, c->les_vt);
+    c->les_cds = cds > 0.0 ? cds : 0.0; /* NaN (no strain) and backscatter give 0 */
+  }
+  const double cds = c->les_cds, prt_inv = c->les_prt_inv;
+  double *g = c->les_g;
+  set_threads(c);
+#pragma omp parallel for schedule(static)
+  for (size_t p = 0; p < np; ++p) {
+    double sum = 0.0;
+    for (int m = 0; m < 6; ++m) {
+      const double s = g[p + m * np];
+      sum += (m == 1 || m == 3 || m == 4 ? 2.0 : 1.0) * s * s;
+    }
+    const double nu = cds * sqrt(2.0 * sum);
+    const double nu2 = 2.0 * nu, kap = nu * prt_inv;
+    for (int m = 0; m < 6; ++m) g[p + m * np] = -nu2 * g[p + m * np];
+    for (int m = 6; m < c->lr; ++m) g[p + m * np] = -kap * g[p + m * np];
+  }
+}
+
+int so_set_les(so_ctx *c, int model, double c_smag, double pr_t) {
+  if (model < 0 || model > 2 || !(pr_t > 0.0)) return -1;
+  c->les_model = model;
+  c->les_c_smag = c_smag;
+  c->les_prt_inv = 1.0 / pr_t;
+  c->les_cds = model == 1 ? c_smag * delta_sq_of(c) : 0.0;
+  if (!model || c->les_w) return 0;
+  const size_t nw = (size_t)c->nze * c->ny_min * c->nx_min * c->lr;
+  const size_t np = (size_t)c->nx * c->ny * c->nz;
+  const size_t vol = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
+  c->les_w = (so_cplx *)calloc(nw, sizeof(so_cplx));
+  c->les_zb = (so_cplx *)calloc((size_t)c->ny_min * c->nx_min * c->nze * c->lr, sizeof(so_cplx));
+  c->les_g = (double *)calloc(np * c->lr, sizeof(double));
+  c->les_uh = (double *)calloc(vol * 3, sizeof(double));
+  c->les_vt = (double *)calloc(vol, sizeof(double));
+  return 0;
+}
+
+double so_les_coef(const so_ctx *c) { return c->les_cds; }

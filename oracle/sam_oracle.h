@@ -110,6 +110,11 @@ int so_force(so_ctx *c, double *u, const double *ek_0, int k_force);
 /* Ornstein-Uhlenbeck forcing of 0 < |k| <= k_f applied by so_steps after
  * every step; returns the number of forced modes, -1 above 128 */
 int so_set_forcing(so_ctx *c, unsigned long long seed, double k_f, double sigma, double t_l);
+/* subgrid closure coupled into so_stage (not in the reference): model 0 off,
+ * 1 Smagorinsky nu_t = c_smag delta^2 |S|, 2 dynamic (dm.f coefficient at
+ * nrk = 1); kappa_t = nu_t / pr_t; -1 on bad arguments */
+int so_set_les(so_ctx *c, int model, double c_smag, double pr_t);
+double so_les_coef(const so_ctx *c);
 int so_write_field(so_ctx *c, const char *fname, const double *u);
 /* 0 ok, -1 open, -2 wrong size (read_field.f:74-80), -3 short read */
 int so_read_field(so_ctx *c, const char *fname, double *u);

@@ -319,6 +319,55 @@ void les_dm(const double* u, double* ub, double* q, double* part, double* cds, d
   k_periodic3<<<grid_of((long long)(nx + 2) * (ny + 2) * (nz + 2)), kThreads, 0, s>>>(vt, H);
 }
 
+// ---- coupled dynamic closure: the physical velocity P(n, z, y, x) of the
+// x pass (working precision) into dm.f's haloed FP64 layout u(Lx,Ly,Lz,3),
+// halo planes filled with the periodic images (periodicity.f:215-239)
+template <typename T>
+__global__ void k_pack_halo(const T* __restrict__ phys, double* __restrict__ uh, Halo H) {
+  const long long vol = H.vol(), tot = 3 * vol;
+  const int lx = H.nx + 2, ly = H.ny + 2;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < tot; e += (long long)gridDim.x * blockDim.x) {
+    const int n = (int)(e / vol);
+    const long long r = e - n * vol;
+    const int i = (int)(r % lx), j = (int)((r / lx) % ly), k = (int)(r / ((long long)lx * ly));
+    uh[e] = (double)phys[(long long)n * H.ninterior() + H.in(i - 1, j - 1, k - 1)];
+  }
+}
+
+// C delta^2 in use: dm.f's value, or 0 where it is negative (backscatter
+// would make the eddy viscosity negative) or undefined (no strain: 0/0)
+__global__ void k_les_clip(const double* __restrict__ raw, double* __restrict__ cds) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    const double v = raw[0];
+    cds[0] = v > 0.0 ? v : 0.0;
+  }
+}
+
+size_t les_dynamic_work(int nx, int ny, int nz) {
+  const size_t n = (size_t)nx * ny * nz, vol = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  return 4 * vol + 22 * n + 2 * (size_t)les_dm_blocks(nx, ny, nz) + 8;
+}
+
+template <typename T>
+void les_dynamic(const T* phys, double* work, double* cds, int nx, int ny, int nz, double dxi, double dyi,
+                 double dzi, cudaStream_t s) {
+  const Halo H = halo(nx, ny, nz);
+  const size_t n = (size_t)nx * ny * nz, vol = (size_t)(nx + 2) * (ny + 2) * (nz + 2);
+  double* uh = work;
+  double* vt = uh + 3 * vol;
+  double* ub = vt + vol;
+  double* q = ub + 3 * n;
+  double* part = q + 19 * n;
+  double* raw = part + 2 * les_dm_blocks(nx, ny, nz);
+  k_pack_halo<T><<<grid_of(3 * (long long)vol), kThreads, 0, s>>>(phys, uh, H);
+  les_dm(uh, ub, q, part, raw, vt, nx, ny, nz, 4.0, dxi, dyi, dzi, s);
+  k_les_clip<<<1, 32, 0, s>>>(raw, cds);
+}
+template void les_dynamic<double>(const double*, double*, double*, int, int, int, double, double, double,
+                                  cudaStream_t);
+template void les_dynamic<float>(const float*, double*, double*, int, int, int, double, double, double,
+                                 cudaStream_t);
+
 void les_get_mean(double2* col, int mz, int kz, int nz, int i_remove, const FftPlan* dplan, const double2* tw,
                   const FftPlan& hplan, double* u_mean, double* jump, cudaStream_t s) {
   const int ld = line_stride(nz);

@@ -80,19 +80,67 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
   const int nl = min(a.ty, my - j0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
   const C* src = a.in + (long long)n * a.in_n + (long long)i * a.in_kx + (long long)j0 * a.in_ky;
-  batched<C>(
-      nl * nz,
-      [&](int e) {
-        const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
-        C v = mk<C>((T)0, (T)0);
-        if (p <= km) v = src[(long long)t * a.in_ky + p];
-        else if (p >= nz - km) v = src[(long long)t * a.in_ky + p - (nz - mz)];
-        return v;
-      },
-      [&](int e, C v) {
-        const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
-        s_ln[t * ld + sidx(p)] = v;
-      });
+  auto put = [&](int e, C v) {
+    const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
+    s_ln[t * ld + sidx(p)] = v;
+  };
+  if (!a.derive || n < a.g.lu) {
+    batched<C>(
+        nl * nz,
+        [&](int e) {
+          const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
+          C v = mk<C>((T)0, (T)0);
+          if (p <= km) v = src[(long long)t * a.in_ky + p];
+          else if (p >= nz - km) v = src[(long long)t * a.in_ky + p - (nz - mz)];
+          return v;
+        },
+        put);
+  } else {
+    // gradient field m of the subgrid stress: S_ab = (i/2)(k_b u_a + k_a u_b)
+    // (i k_a u_a when a = b) for the six velocity products in rhs.f's order,
+    // i k_a T for the three buoyancy products
+    const int m = n - a.g.lu;
+    int fa, fb;
+    if (m < 6) {
+      fb = m < 1 ? 0 : (m < 3 ? 1 : 2);
+      fa = m - (fb * (fb + 1)) / 2;
+    } else {
+      fa = m - 6;
+      fb = 3;
+    }
+    const long long off = (long long)i * a.in_kx + (long long)j0 * a.in_ky;
+    const C* srca = a.in + (long long)(m < 6 ? fa : 3) * a.in_n + off;
+    const C* srcb = a.in + (long long)(m < 6 ? fb : 3) * a.in_n + off;
+    const double kxv = a.g.wave_x * (double)i;
+    batched<C>(
+        nl * nz,
+        [&](int e) {
+          const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
+          C v = mk<C>((T)0, (T)0);
+          int q = -1;
+          if (p <= km) q = p;
+          else if (p >= nz - km) q = p - (nz - mz);
+          if (q >= 0) {
+            const double kv[3] = {kxv, a.g.wave_y * (double)kwave(j0 + t, a.g.ky, my),
+                                  a.g.wave_z * (double)kwave(q, km, mz)};
+            const C ua = srca[(long long)t * a.in_ky + q];
+            if (m >= 6) {
+              const T k = (T)kv[fa];
+              v = mk<C>(-k * ua.y, k * ua.x);
+            } else if (fa == fb) {
+              const T k = (T)kv[fa];
+              v = mk<C>(-k * ua.y, k * ua.x);
+            } else {
+              const C ub = srcb[(long long)t * a.in_ky + q];
+              const T ka = (T)kv[fa], kb = (T)kv[fb];
+              const T zr = kb * ua.x + ka * ub.x, zi = kb * ua.y + ka * ub.y;
+              v = mk<C>((T)-0.5 * zi, (T)0.5 * zr);
+            }
+          }
+          return v;
+        },
+        put);
+  }
   __syncthreads();
   fft_lines<+1>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
@@ -179,13 +227,34 @@ __device__ __forceinline__ void store_pair(double2* o, double2 a, double2 b) {
 template <typename C> struct ProductLoad {
   const C* a;
   const C* b;
+  const C* g;  // subgrid term added to the product (may be null)
   __device__ __forceinline__ C operator()(int idx) const {
     const C va = a[sidx(idx)];
     if (!b) return va;
     const C vb = b[sidx(idx)];
-    return mk<C>(va.x * vb.x, va.y * vb.y);
+    if (!g) return mk<C>(va.x * vb.x, va.y * vb.y);
+    const C vg = g[sidx(idx)];
+    return mk<C>(va.x * vb.x + vg.x, va.y * vb.y + vg.y);
   }
 };
+
+// Subgrid stress on one physical point: s[0..5] the strain in product order
+// (S11 S12 S22 S13 S23 S33), s[6..8] dT/dx_a; on return s holds the terms
+// the products receive, -2 nu_t S and -kappa_t dT/dx with
+// nu_t = cds |S|, |S| = sqrt(2 sum ifact S^2), kappa_t = nu_t prt_inv.
+template <typename T>
+__device__ __forceinline__ void sgs_point(T* s, int nf, T cds, T prt_inv) {
+  T sum = (T)0;
+#pragma unroll
+  for (int m = 0; m < 6; ++m) sum += (m == 1 || m == 3 || m == 4 ? (T)2 : (T)1) * s[m] * s[m];
+  const T nu = cds * sqrt((T)2 * sum);
+  const T nu2 = (T)2 * nu, kap = nu * prt_inv;
+#pragma unroll
+  for (int m = 0; m < 6; ++m) s[m] = -nu2 * s[m];
+#pragma unroll
+  for (int m = 6; m < 9; ++m)
+    if (m < nf) s[m] = -kap * s[m];
+}
 
 // ------------------------------------------------------------------ x pass
 // Tile: plane z, rows y0 .. y0+Y-1 (Y even).  Two real x-lines (rows y0+2c
@@ -327,6 +396,30 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
     }
   }
 
+  // ---- subgrid stress: the gradient lines become -2 nu_t S and -kappa_t dT
+  if (a.les) {
+    const int lu = a.g.lu, lr = a.g.lr;
+    const T cds = (T)a.les_cds[0], prt = (T)a.les_prt_inv;
+    for (int e = threadIdx.x; e < yp * nx; e += blockDim.x) {
+      const int c = (int)fdiv(e, a.fd_nx), x = e - c * nx;
+      C v[9];
+      T sx[9], sy[9];
+#pragma unroll
+      for (int m = 0; m < 9; ++m)
+        if (m < lr) {
+          v[m] = s_in[((lu + m) * yp + c) * ld + sidx(x)];
+          sx[m] = v[m].x;
+          sy[m] = v[m].y;
+        }
+      sgs_point<T>(sx, lr, cds, prt);
+      sgs_point<T>(sy, lr, cds, prt);
+#pragma unroll
+      for (int m = 0; m < 9; ++m)
+        if (m < lr) s_in[((lu + m) * yp + c) * ld + sidx(x)] = mk<C>(sx[m], sy[m]);
+    }
+    __syncthreads();
+  }
+
   // ---- outputs
   if (a.out_mode == 3) return;  // statistics only (vel_max.f)
   if (a.out_mode == 0) {
@@ -354,11 +447,12 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
     // them, straight into the product lines
     C* lines = a.out_mode == 1 ? s_in + m0 * yp * ld : s_pr;
     fft_lines_from<-1>(lines, ld, gm * yp, s_tw, pl, [&](int L) {
-      if (a.out_mode == 1) return ProductLoad<C>{lines + L * ld, nullptr};
+      if (a.out_mode == 1) return ProductLoad<C>{lines + L * ld, nullptr, nullptr};
       const int gi = L / yp, c = L - gi * yp;
       int fa, fb;
       product_pair(m0 + gi, fa, fb);
-      return ProductLoad<C>{s_in + (fa * yp + c) * ld, s_in + (fb * yp + c) * ld};
+      const C* gl = a.les ? s_in + ((a.g.lu + m0 + gi) * yp + c) * ld : nullptr;
+      return ProductLoad<C>{s_in + (fa * yp + c) * ld, s_in + (fb * yp + c) * ld, gl};
     });
     __syncthreads();
     // split the two real transforms, keep kx <= kx_max, scale, store

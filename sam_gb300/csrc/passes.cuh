@@ -12,6 +12,10 @@ struct ZInvArgs {
   cx_t<T>* out;        // A(n, z, kx, ky)
   const cx_t<T>* tw;   // twiddles of the Nz plan
   int nvar, ty, ld;
+  // derive = 1: fields n >= Lu of the launch are the subgrid gradient fields
+  // m = n - Lu formed from the velocity (and T) rows while loading: S_ab for
+  // the six velocity products, dT/dx_a for the three buoyancy products
+  int derive;
   long long in_ky, in_kx, in_n;
   long long out_kx, out_z, out_n;
   FastDiv fd_n, fd_t;  // filled by the launcher: Nz, ty
@@ -39,6 +43,12 @@ struct XPassArgs {
   double* partials;    // vel_max partials (nblocks, lu, 4) or null
   const cx_t<T>* tw;
   int in_mode, out_mode, nin, yt, group, ld;
+  // subgrid stress (les = 1): input fields Lu .. Lu+Lr-1 are the gradient
+  // fields of the products; nu_t = C delta^2 |S| with C delta^2 read from
+  // les_cds, kappa_t = nu_t * les_prt_inv
+  int les;
+  const double* les_cds;
+  double les_prt_inv;
   long long in_y, in_z, in_n;
   long long out_kx, out_z, out_n;
   long long out_py, out_pz, out_pn;

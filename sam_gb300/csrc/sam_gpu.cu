@@ -162,12 +162,25 @@ struct Ctx {
   // tile choices
   int ty_zi = 16, tx_yi = 16, yt_x = 8, grp_x = 9, tz_yf = 16, ty_zf = 4;
   OuForcing* ou = nullptr;  // device OU forcing state, null when off
+  // subgrid closure coupled into the stage (sam_gpu_set_les)
+  int les_model = 0;
+  double les_prt_inv = 1.0, les_dxi = 0, les_dyi = 0, les_dzi = 0;
+  double* les_cds = nullptr;   // device C delta^2 in use
+  void* les_phys = nullptr;    // physical velocity for dm.f (3 fields, working precision)
+  double* les_work = nullptr;  // dm.f work arrays
+  size_t s1_elems = 0, s2_elems = 0;
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t graph_stream = nullptr;
   int graph_stale = 1;
 };
 
 static Ctx* g_ctx = nullptr;
+
+static void grid_spacing(const Ctx& c, double& dxi, double& dyi, double& dzi, double& delta_sq) {
+  const double dx = c.cfg.xl / c.g.nx, dy = c.cfg.yl / c.g.ny, dz = c.cfg.zl / c.g.nz;
+  dxi = 1.0 / dx; dyi = 1.0 / dy; dzi = 1.0 / dz;
+  delta_sq = pow(dx * dy * dz, 2.0 / 3.0);  // init.f:28
+}
 
 static int ensure(Scratch& s, size_t bytes) {
   if (s.n >= bytes) return 0;
@@ -201,8 +214,9 @@ static int pick_tile(const Plan& P, int want, int lines_per_unit, size_t es, siz
 // --------------------------------------------------------------- the passes
 template <typename T>
 static int run_z_inv(Ctx& c, const void* in, void* out, int nvar, long long in_ky, long long in_kx, long long in_n,
-                     long long out_kx, long long out_z, long long out_n) {
+                     long long out_kx, long long out_z, long long out_n, int derive = 0) {
   ZInvArgs<T> a{};
+  a.derive = derive;
   a.g = c.g;
   a.in = (const cx_t<T>*)in;
   a.out = (cx_t<T>*)out;
@@ -262,8 +276,13 @@ template <typename T>
 static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in, const void* in_phys,
                       long long in_y, long long in_z, long long in_n, void* out, void* out_phys, long long out_kx,
                       long long out_z, long long out_n, long long out_py, long long out_pz, long long out_pn,
-                      bool stats) {
+                      bool stats, bool les = false) {
   XPassArgs<T> a{};
+  if (les) {
+    a.les = 1;
+    a.les_cds = c.les_cds;
+    a.les_prt_inv = c.les_prt_inv;
+  }
   a.g = c.g;
   a.in = (const cx_t<T>*)in;
   a.in_phys = (const T*)in_phys;
@@ -354,23 +373,38 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
   const long long nzmm = (long long)g.mx * g.my * g.mz;
   int rc = 0;
   auto run = [&](int p) { return only < 0 || only == p; };
+  // with a subgrid closure the backward transforms also carry the Lr
+  // gradient fields the products need
+  const bool les = c.les_model != 0;
+  const int nin = g.lu + (les ? g.lr : 0);
   if (ev) cudaEventRecord(ev[0], c.stream);
   // z inverse: U(n, kx, ky, kz) -> A(n, z, kx, ky)
   if (run(0))
-    rc = run_z_inv<T>(c, c.U, c.S1, g.lu, g.mz, (long long)g.my * g.mz, nzmm, g.my, (long long)g.mx * g.my,
-                      (long long)g.nz * g.mx * g.my);
+    rc = run_z_inv<T>(c, c.U, c.S1, nin, g.mz, (long long)g.my * g.mz, nzmm, g.my, (long long)g.mx * g.my,
+                      (long long)g.nz * g.mx * g.my, les ? 1 : 0);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[1], c.stream);
   // y inverse: A -> B(n, z, y, kx)
   if (run(1))
-    rc = run_y_inv<T>(c, c.S1, c.S2, g.lu, 0, g.my, (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, g.mx,
+    rc = run_y_inv<T>(c, c.S1, c.S2, nin, 0, g.my, (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, g.mx,
                       (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[2], c.stream);
+  // dynamic closure at nrk = 1 (once per step, like vel_max): the physical
+  // velocity, then dm.f's coefficient on it
+  if (run(2) && c.les_model == 2 && nrk == 1) {
+    rc = run_x_pass<T>(c, 0, 0, 3, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
+                       nullptr, c.les_phys, 0, 0, 0, g.nx, (long long)g.nx * g.ny, (long long)g.nx * g.ny * g.nz,
+                       false);
+    if (rc) return rc;
+    les_dynamic<T>((const T*)c.les_phys, c.les_work, c.les_cds, g.nx, g.ny, g.nz, c.les_dxi, c.les_dyi, c.les_dzi,
+                   c.stream);
+  }
   // x pass: B -> C(m, z, kx, y) with vel_max at nrk = 1
   if (run(2))
-    rc = run_x_pass<T>(c, 0, 2, g.lu, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
-                       c.S3, nullptr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, 0, 0, 0, nrk == 1);
+    rc = run_x_pass<T>(c, 0, 2, nin, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
+                       c.S3, nullptr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, 0, 0, 0, nrk == 1,
+                       les);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[3], c.stream);
   // y forward: C -> D(m, kx, ky, z)
@@ -422,6 +456,7 @@ static void free_ctx(Ctx* c) {
   cudaFree(c->U); cudaFree(c->R); cudaFree(c->P);
   cudaFree(c->S1); cudaFree(c->S2); cudaFree(c->S3);
   cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou);
+  cudaFree(c->les_cds); cudaFree(c->les_phys); cudaFree(c->les_work);
   for (auto& s : c->sc) cudaFree(s.p);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -590,6 +625,8 @@ int sam_gpu_init(const sam_gpu_config* cfg) {
   const size_t nzmm = (size_t)g.mx * g.my * g.mz;
   const size_t s1 = (size_t)g.lr * g.mx * g.my * g.nz;
   const size_t s2 = (size_t)g.lu * g.nz * g.ny * g.mx;
+  c->s1_elems = s1;
+  c->s2_elems = s2;
   const size_t s3 = (size_t)g.lr * g.nz * g.mx * g.ny;
   bool ok = cudaMalloc(&c->U, es * g.lu * nzmm) == cudaSuccess && cudaMalloc(&c->R, es * g.lu * nzmm) == cudaSuccess &&
             cudaMalloc(&c->P, es * nzmm) == cudaSuccess && cudaMalloc(&c->S1, es * s1) == cudaSuccess &&
@@ -937,6 +974,57 @@ int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, doubl
   return sync_stream(c);
 }
 
+int sam_gpu_set_les(int model, double c_smag, double pr_t) {
+  NEED_CTX();
+  if (model < 0 || model > 2) return fail(SAM_GPU_EINVAL, "set_les: model %d (0 off, 1 Smagorinsky, 2 dynamic)", model);
+  if (!(pr_t > 0.0)) return fail(SAM_GPU_EINVAL, "set_les: turbulent Prandtl number must be > 0");
+  if (model == 1 && !(c_smag >= 0.0)) return fail(SAM_GPU_EINVAL, "set_les: c_smag must be >= 0");
+  if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+  CK(cudaStreamSynchronize(c.stream));
+  const Grid& g = c.g;
+  const size_t es = csize(c);
+  if (model) {
+    // pencil buffers for the Lr gradient fields beside the Lu fields
+    const size_t s1 = (size_t)(g.lu + g.lr) * g.mx * g.my * g.nz;
+    const size_t s2 = (size_t)(g.lu + g.lr) * g.nz * g.ny * g.mx;
+    if (c.s1_elems < s1) {
+      cudaFree(c.S1); c.S1 = nullptr; c.s1_elems = 0;
+      CK(cudaMalloc(&c.S1, es * s1));
+      c.s1_elems = s1;
+    }
+    if (c.s2_elems < s2) {
+      cudaFree(c.S2); c.S2 = nullptr; c.s2_elems = 0;
+      CK(cudaMalloc(&c.S2, es * s2));
+      c.s2_elems = s2;
+    }
+    if (!c.les_cds) CK(cudaMalloc(&c.les_cds, sizeof(double)));
+    if (model == 2 && !c.les_work) {
+      CK(cudaMalloc(&c.les_phys, (es / 2) * 3 * (size_t)g.nx * g.ny * g.nz));
+      CK(cudaMalloc(&c.les_work, sizeof(double) * les_dynamic_work(g.nx, g.ny, g.nz)));
+    }
+  }
+  double dsq;
+  grid_spacing(c, c.les_dxi, c.les_dyi, c.les_dzi, dsq);
+  c.les_model = model;
+  c.les_prt_inv = 1.0 / pr_t;
+  if (model) {
+    // sm.f:32 (model 1); the dynamic coefficient starts at 0 and is set at
+    // stage 1 of every step (model 2)
+    const double cds = model == 1 ? c_smag * dsq : 0.0;
+    CK(cudaMemcpy(c.les_cds, &cds, sizeof(double), cudaMemcpyHostToDevice));
+  }
+  return 0;
+}
+
+int sam_gpu_les_coef(double* c_delta_sq) {
+  NEED_CTX();
+  if (!c_delta_sq) return fail(SAM_GPU_EINVAL, "les_coef: null output");
+  *c_delta_sq = 0.0;
+  if (!c.les_model) return 0;
+  CK(cudaMemcpyAsync(c_delta_sq, c.les_cds, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
 int sam_gpu_measure_fp64_peak(double* tflops) {
   NEED_CTX();
   if (!tflops) return fail(SAM_GPU_EINVAL, "measure_fp64_peak: null output");
@@ -1277,11 +1365,6 @@ int sam_gpu_filter(const double* f_bar, double* f_hat, int n_var) {
   return sync_stream(c);
 }
 
-static void grid_spacing(const Ctx& c, double& dxi, double& dyi, double& dzi, double& delta_sq) {
-  const double dx = c.cfg.xl / c.g.nx, dy = c.cfg.yl / c.g.ny, dz = c.cfg.zl / c.g.nz;
-  dxi = 1.0 / dx; dyi = 1.0 / dy; dzi = 1.0 / dz;
-  delta_sq = pow(dx * dy * dz, 2.0 / 3.0);  // init.f:28
-}
 
 int sam_gpu_sm(const double* u, double*, double*, double* vt) {
   NEED_CTX();

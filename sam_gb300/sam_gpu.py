@@ -30,7 +30,7 @@ EXPORTS = [
     "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
     "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
     "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_planes",
-    "sam_gpu_set_forcing",
+    "sam_gpu_set_forcing", "sam_gpu_set_les", "sam_gpu_les_coef",
 ]
 
 
@@ -109,6 +109,8 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_autotune.argtypes = [C.c_int]
     lib.sam_gpu_tiles.argtypes = [P]
     lib.sam_gpu_set_forcing.argtypes = [C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int)]
+    lib.sam_gpu_set_les.argtypes = [C.c_int, C.c_double, C.c_double]
+    lib.sam_gpu_les_coef.argtypes = [C.POINTER(C.c_double)]
     lib.sam_gpu_planes.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
     lib.sam_gpu_force.argtypes = [P, C.c_int]
     lib.sam_gpu_write_field.argtypes = [C.c_char_p]
@@ -331,6 +333,18 @@ class SamGpu:
         n = C.c_int(0)
         self._check(load_library().sam_gpu_set_forcing(seed, k_f, sigma, t_l, C.byref(n)), "set_forcing")
         return n.value
+
+    def set_les(self, model, c_smag=0.01, pr_t=1.0):
+        """Subgrid closure coupled into every stage: 0 off, 1 Smagorinsky
+        (C delta^2 = c_smag delta^2), 2 dynamic (dm.f's coefficient at stage
+        1 of each step); kappa_t = nu_t / pr_t."""
+        self._check(load_library().sam_gpu_set_les(model, c_smag, pr_t), "set_les")
+
+    def les_coef(self):
+        """C delta^2 the closure last used."""
+        v = C.c_double(0.0)
+        self._check(load_library().sam_gpu_les_coef(C.byref(v)), "les_coef")
+        return v.value
 
     def planes(self, k_xy=(), j_xz=(), i_yz=()):
         """Planes output of the resident state (sam.f:145-166, write_planes.f),

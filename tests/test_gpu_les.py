@@ -84,3 +84,75 @@ def test_get_mean(gpu_lib, i_remove):
     # the scale of the profile, not of itself
     assert abs(j_g - j_o) <= 1e-13 * np.abs(um_o).max()
     assert relerr(fg[: o.d.nz_min, 0, 0], fo[: o.d.nz_min, 0, 0]) < 1e-13
+
+
+LES_CASES = [(1, 0), (1, 1), (2, 0), (2, 1)]
+
+
+@pytest.mark.parametrize("model,strat", LES_CASES)
+def test_coupled_closure_matches_oracle(gpu_lib, model, strat):
+    """Smagorinsky (model 1) and dynamic Smagorinsky (model 2) coupled into
+    the RK3 step: the GPU run against the oracle's restatement, several CFL
+    steps, per field to 1e-12; the coefficient in use agrees too."""
+    cfg = dict(nx=24, ny=16, nz=32, i_strat=strat, buoy_fac_z=1.0 * strat, lapse=1.0 * strat, vis=1e-4,
+               i_cfl=1, cfl0=0.5)
+    g, o = SamGpu(**cfg), O.Oracle(**cfg)
+    u = o.init_random(7, 0, 1.0, 0, 0.1)
+    r = o.wave(o.d.lr)
+    g.upload(u)
+    g.set_les(model, c_smag=0.03, pr_t=0.7)
+    o.set_les(model, c_smag=0.03, pr_t=0.7)
+    o.steps(u, r, 4)
+    g.step(4)
+    ug = g.download()
+    for n in range(o.d.lu):
+        assert relerr(ug[..., n], u[..., n]) <= 1e-12, n
+    assert abs(g.les_coef() - o.les_coef()) <= 1e-12 * abs(o.les_coef())
+    assert o.les_coef() > 0
+
+
+def test_coupled_closure_stages_and_fp32(gpu_lib):
+    """Single stages (sam_gpu_stage) with the dynamic closure, then the FP32
+    bulk form of the same run within its tolerance."""
+    cfg = dict(nx=32, ny=32, nz=32, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=1e-4, dt0=0.01)
+    g, o = SamGpu(**cfg), O.Oracle(**cfg)
+    u = o.init_random(2, 0, 1.0, 0, 0.1)
+    u0 = u.copy(order="F")
+    r = o.wave(o.d.lr)
+    g.upload(u)
+    g.set_les(2, pr_t=1.0)
+    o.set_les(2, pr_t=1.0)
+    for nrk in (1, 2, 3):
+        o.stage(u, r, nrk)
+        g.stage(nrk)
+        ug, rg = g.download(with_r=True)
+        m = o.d.nz_min  # rows above Nz_min of r are unspecified (z_trans_f.f)
+        for n in range(o.d.lu):
+            assert relerr(ug[:m, ..., n], u[:m, ..., n]) <= 1e-12, (nrk, n)
+            assert relerr(rg[:m, ..., n], r[:m, ..., n]) <= 1e-12, (nrk, n)
+    g32 = SamGpu(precision=32, **cfg)
+    g32.upload(u0)
+    g32.set_les(2, pr_t=1.0)
+    g32.step(1)
+    u32 = g32.download()
+    for n in range(o.d.lu):
+        assert relerr(u32[..., n], u[..., n]) <= 2e-5, n
+
+
+def test_closure_off_restores_reference_products(gpu_lib):
+    cfg = dict(nx=16, ny=16, nz=16, vis=1e-3)
+    g = SamGpu(**cfg)
+    g.init_taylor_green()
+    u0 = g.download()
+    g.set_les(1, c_smag=0.05)
+    g.step(1)
+    assert g.les_coef() > 0
+    g.set_les(0)
+    g.upload(u0)
+    g.step(2)
+    g2 = SamGpu(**cfg)
+    g2.upload(u0)
+    g2.step(2)
+    assert np.array_equal(g.download(), g2.download())
+    with pytest.raises(Exception, match="EINVAL"):
+        g.set_les(3)
