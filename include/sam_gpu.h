@@ -232,6 +232,34 @@ int sam_gpu_set_les(int model, double c_smag, double pr_t);
 /* C delta^2 last used (0 with the closure off) */
 int sam_gpu_les_coef(double* c_delta_sq);
 
+/* ---- learned subgrid closure (no reference counterpart) ----
+ * A 12 -> 64 -> 64 -> 2 MLP (ReLU hidden layers) with BF16 weights and FP32
+ * accumulation on the tensor cores (tcgen05.mma, accumulators in TMEM).
+ * Its outputs are the coefficients (C_nu, C_kappa) = 0.02 softplus(o) of
+ * nu_t = C_nu delta^2 |S| and kappa_t = C_kappa delta^2 |S|.  Parameters are
+ * one FP32 vector of SAM_GPU_MLP_PARAMS: W1 (64 x 12, row-major [out][in]),
+ * b1 (64), W2 (64 x 64), b2 (64), W3 (2 x 64), b3 (2); the network belongs to
+ * the context (sam_gpu_init) and starts at zero. */
+#define SAM_GPU_MLP_PARAMS 5122
+#define SAM_GPU_MLP_FEATURES 12
+int sam_gpu_mlp_set(const float* params, int n);
+int sam_gpu_mlp_get(float* params, int n);
+/* features [n][12] (host, FP32; rounded to BF16) -> coef [n][2] */
+int sam_gpu_mlp_forward(const float* features, long long n, float* coef);
+/* gradient of L = (1/(2n)) sum (C - target)^2 over the n points and both
+ * outputs, target [n][2]; grad receives SAM_GPU_MLP_PARAMS floats, loss
+ * (may be NULL) L.  The backward pass runs on the CUDA cores in FP32 with
+ * the BF16 weights and activations of the forward pass. */
+int sam_gpu_mlp_grad(const float* features, const float* target, long long n, float* grad, float* loss);
+/* `steps` Adam steps (lr, beta 0.9/0.999, eps 1e-8) on minibatches of
+ * `batch` points taken in order from the data as given (the caller
+ * shuffles); loss_hist (may be NULL) receives each minibatch's loss. */
+int sam_gpu_mlp_train(const float* features, const float* target, long long n, int steps, int batch, float lr,
+                      float* loss_hist);
+/* Known-answer test of the tensor-core path: d(128 x 64) = a(128 x 16)
+ * b(64 x 16)^T with a, b rounded to BF16 and FP32 accumulation. */
+int sam_gpu_mma_selftest(const float* a, const float* b, float* d);
+
 /* ---- restart files of the resident state ---- */
 /* write_field.f:1 / read_field.f:1  vel.NNNNNN: Lu*Nx_min records of
  * Nz_min x Ny_min complex128; read_field rejects a file of the wrong size */

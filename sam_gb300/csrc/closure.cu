@@ -1,0 +1,529 @@
+// Learned subgrid closure: the 12 -> 64 -> 64 -> 2 MLP on sm_103a.
+//
+// Inference: one CTA of 128 threads (one warpgroup) per tile of 128 points.
+// The inputs and the weights sit in shared memory in the canonical K-major
+// no-swizzle layout of the tensor cores (8 x 16-byte core matrices: element
+// (r, k) at (r/8)*SBO + (k/8)*LBO + (r%8)*16 + (k%8)*2 with LBO = 128 B and
+// SBO = (K/8)*128 B).  One thread issues tcgen05.mma (kind::f16, BF16 x BF16
+// -> FP32 in TMEM, M = 128), tcgen05.commit arrives on an mbarrier, all four
+// warps wait on it and read their 32 TMEM lanes back with tcgen05.ld; the
+// bias and ReLU epilogue writes the next layer's BF16 operand into shared
+// memory.  Three MMA groups per tile (K = 16, then 4 x K = 16 twice).  Every
+// wait is bounded: on timeout the kernel sets *err, frees its TMEM and
+// returns.
+//
+// Training: the backward pass of the loss mean (C - y)^2 and Adam run on the
+// CUDA cores in FP32 (the network is small; the weight gradients are
+// per-CTA partial sums reduced in a fixed order, so runs are reproducible).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "closure.cuh"
+
+namespace samgpu {
+
+// ------------------------------------------------------------ PTX helpers
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// byte offset of element (r, k) of a K-major tile with K columns
+__device__ __forceinline__ uint32_t kmaj(int r, int k, int K) {
+  return (uint32_t)((r >> 3) * (K >> 3) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
+// offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+// instruction descriptor of kind::f16: D F32, A and B BF16, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// bounded wait on phase `parity`; 0 when it completed, 1 on timeout
+__device__ __forceinline__ int mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (uint32_t it = 0; it < (1u << 24); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return 0;
+  }
+  return 1;
+}
+// 16 consecutive FP32 columns of this warp's 32 TMEM lanes (one per thread)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr)
+      : "memory");
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
+  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// eight values of row r, columns k0..k0+7, into a K-major tile as one 16 B store
+__device__ __forceinline__ void st_row8(uint8_t* tile, int r, int k0, int K, const float* v) {
+  uint4 q;
+  q.x = pack_bf16(v[0], v[1]);
+  q.y = pack_bf16(v[2], v[3]);
+  q.z = pack_bf16(v[4], v[5]);
+  q.w = pack_bf16(v[6], v[7]);
+  *reinterpret_cast<uint4*>(tile + kmaj(r, k0, K)) = q;
+}
+
+// copy a row-major [R][K] BF16 matrix into a K-major tile
+__device__ __forceinline__ void stage_matrix(uint8_t* tile, const __nv_bfloat16* __restrict__ src, int R, int K) {
+  for (int e = threadIdx.x; e < R * (K / 8); e += blockDim.x) {
+    const int r = e / (K / 8), k0 = (e - r * (K / 8)) * 8;
+    *reinterpret_cast<uint4*>(tile + kmaj(r, k0, K)) = *reinterpret_cast<const uint4*>(src + r * K + k0);
+  }
+}
+
+__device__ __forceinline__ float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
+
+// ------------------------------------------------------------- MMA selftest
+// D(128 x 64) = A(128 x 16) B(64 x 16)^T: the smallest use of the path the
+// forward kernel takes, checked against a host product in the tests.
+__global__ void __launch_bounds__(128) k_mma_selftest(const __nv_bfloat16* __restrict__ a,
+                                                      const __nv_bfloat16* __restrict__ b, float* __restrict__ d,
+                                                      int* err) {
+  __shared__ __align__(1024) uint8_t sa[128 * 16 * 2];
+  __shared__ __align__(1024) uint8_t sb[64 * 16 * 2];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tbase;
+  if (threadIdx.x < 32) tmem_alloc(&tbase, 64);
+  if (threadIdx.x == 0) mbar_init(&bar, 1);
+  stage_matrix(sa, a, 128, 16);
+  stage_matrix(sb, b, 64, 16);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = tbase;
+  if (threadIdx.x == 0) {
+    mma_bf16(tm, sdesc(smem_u32(sa), 128, 256), sdesc(smem_u32(sb), 128, 256), idesc_bf16(128, 64), 0);
+    mma_commit(&bar);
+  }
+  int bad = mbar_wait(&bar, 0);
+  tc_fence_after();
+  bad = __syncthreads_or(bad);
+  if (!bad) {
+    const int w = threadIdx.x >> 5;
+    for (int c = 0; c < 64; c += 16) {
+      float v[16];
+      tmem_ld16(tm + ((uint32_t)(32 * w) << 16) + (uint32_t)c, v);
+      for (int i = 0; i < 16; ++i) d[threadIdx.x * 64 + c + i] = v[i];
+    }
+  } else if (threadIdx.x == 0) {
+    atomicExch(err, 1);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    tc_fence_after();
+    tmem_dealloc(tm, 64);
+  }
+}
+
+void mlp_mma_selftest(const __nv_bfloat16* a, const __nv_bfloat16* b, float* d, int* err, cudaStream_t s) {
+  k_mma_selftest<<<1, 128, 0, s>>>(a, b, d, err);
+}
+
+// ------------------------------------------------------------ forward pass
+// Persistent CTAs of 128 threads; thread t owns row t of every tile (its
+// TMEM lane).  Optionally stores the activations for the backward pass.
+__global__ void __launch_bounds__(128) k_mlp_fwd(const __nv_bfloat16* __restrict__ x16, long long n,
+                                                 const MlpDev* __restrict__ P, float2* __restrict__ coef,
+                                                 __nv_bfloat16* __restrict__ h1g, __nv_bfloat16* __restrict__ h2g,
+                                                 float* __restrict__ og, int* err) {
+  __shared__ __align__(1024) uint8_t sw1[kMlpH * kMlpK1 * 2];
+  __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];
+  __shared__ __align__(1024) uint8_t sw3[kMlpN3 * kMlpH * 2];
+  __shared__ __align__(1024) uint8_t sa1[kMlpTile * kMlpK1 * 2];
+  __shared__ __align__(1024) uint8_t sa2[kMlpTile * kMlpH * 2];
+  __shared__ float sb1[kMlpH], sb2[kMlpH], sb3[kMlpN3];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t tbase;
+  const int tid = threadIdx.x;
+  if (tid < 32) tmem_alloc(&tbase, 64);
+  if (tid == 0) mbar_init(&bar, 1);
+  stage_matrix(sw1, P->w1, kMlpH, kMlpK1);
+  stage_matrix(sw2, P->w2, kMlpH, kMlpH);
+  stage_matrix(sw3, P->w3, kMlpN3, kMlpH);
+  if (tid < kMlpH) {
+    sb1[tid] = P->b1[tid];
+    sb2[tid] = P->b2[tid];
+  }
+  if (tid < kMlpN3) sb3[tid] = P->b3[tid];
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = tbase;
+  const uint32_t tl = tm + ((uint32_t)(32 * (tid >> 5)) << 16);  // this warp's lanes
+  const uint32_t a1 = smem_u32(sa1), a2 = smem_u32(sa2);
+  const uint32_t w1 = smem_u32(sw1), w2 = smem_u32(sw2), w3 = smem_u32(sw3);
+  const uint32_t id64 = idesc_bf16(kMlpTile, kMlpH), id16 = idesc_bf16(kMlpTile, kMlpN3);
+  uint32_t phase = 0;
+  int bad = 0;
+  const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long long row = t * kMlpTile + tid;
+    const bool live = row < n;
+    uint4 q0 = make_uint4(0, 0, 0, 0), q1 = q0;
+    if (live) {
+      const uint4* src = reinterpret_cast<const uint4*>(x16 + row * kMlpK1);
+      q0 = src[0];
+      q1 = src[1];
+    }
+    *reinterpret_cast<uint4*>(sa1 + kmaj(tid, 0, kMlpK1)) = q0;
+    *reinterpret_cast<uint4*>(sa1 + kmaj(tid, 8, kMlpK1)) = q1;
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // layer 1: D = X W1^T (K = 16)
+    if (tid == 0) {
+      mma_bf16(tm, sdesc(a1, 128, 256), sdesc(w1, 128, 256), id64, 0);
+      mma_commit(&bar);
+    }
+    bad = mbar_wait(&bar, phase);
+    phase ^= 1;
+    tc_fence_after();
+    if (__syncthreads_or(bad)) break;
+    float h[kMlpH];
+#pragma unroll
+    for (int c = 0; c < kMlpH; c += 16) tmem_ld16(tl + (uint32_t)c, h + c);
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) h[k] = fmaxf(h[k] + sb1[k], 0.f);
+#pragma unroll
+    for (int k0 = 0; k0 < kMlpH; k0 += 8) st_row8(sa2, tid, k0, kMlpH, h + k0);
+    if (h1g && live) {
+#pragma unroll
+      for (int k0 = 0; k0 < kMlpH; k0 += 8)
+        *reinterpret_cast<uint4*>(h1g + row * kMlpH + k0) =
+            make_uint4(pack_bf16(h[k0], h[k0 + 1]), pack_bf16(h[k0 + 2], h[k0 + 3]), pack_bf16(h[k0 + 4], h[k0 + 5]),
+                       pack_bf16(h[k0 + 6], h[k0 + 7]));
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // layer 2: D = H1 W2^T (K = 64 as four K = 16 steps)
+    if (tid == 0) {
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, 1024), sdesc(w2 + 256 * kk, 128, 1024), id64, kk > 0);
+      mma_commit(&bar);
+    }
+    bad = mbar_wait(&bar, phase);
+    phase ^= 1;
+    tc_fence_after();
+    if (__syncthreads_or(bad)) break;
+#pragma unroll
+    for (int c = 0; c < kMlpH; c += 16) tmem_ld16(tl + (uint32_t)c, h + c);
+#pragma unroll
+    for (int k = 0; k < kMlpH; ++k) h[k] = fmaxf(h[k] + sb2[k], 0.f);
+#pragma unroll
+    for (int k0 = 0; k0 < kMlpH; k0 += 8) st_row8(sa2, tid, k0, kMlpH, h + k0);
+    if (h2g && live) {
+#pragma unroll
+      for (int k0 = 0; k0 < kMlpH; k0 += 8)
+        *reinterpret_cast<uint4*>(h2g + row * kMlpH + k0) =
+            make_uint4(pack_bf16(h[k0], h[k0 + 1]), pack_bf16(h[k0 + 2], h[k0 + 3]), pack_bf16(h[k0 + 4], h[k0 + 5]),
+                       pack_bf16(h[k0 + 6], h[k0 + 7]));
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // layer 3: D = H2 W3^T (N = 16, two rows used)
+    if (tid == 0) {
+#pragma unroll
+      for (int kk = 0; kk < 4; ++kk)
+        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, 1024), sdesc(w3 + 256 * kk, 128, 1024), id16, kk > 0);
+      mma_commit(&bar);
+    }
+    bad = mbar_wait(&bar, phase);
+    phase ^= 1;
+    tc_fence_after();
+    if (__syncthreads_or(bad)) break;
+    float o[16];
+    tmem_ld16(tl, o);
+    if (live) {
+      const float o0 = o[0] + sb3[0], o1 = o[1] + sb3[1];
+      coef[row] = make_float2(kMlpScale * softplus(o0), kMlpScale * softplus(o1));
+      if (og) {
+        og[2 * row] = o0;
+        og[2 * row + 1] = o1;
+      }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+  }
+  if (bad && tid == 0) atomicExch(err, 1);
+  tc_fence_before();
+  __syncthreads();
+  if (tid < 32) {
+    tc_fence_after();
+    tmem_dealloc(tm, 64);
+  }
+}
+
+int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2* coef, const MlpBatch* batch,
+                int* err, cudaStream_t s) {
+  const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
+  long long grid = 152 * 6;
+  if (grid > ntiles) grid = ntiles;
+  if (grid < 1) return 0;
+  k_mlp_fwd<<<(int)grid, kMlpTile, 0, s>>>(x16, n, dev, coef, batch ? batch->h1 : nullptr,
+                                           batch ? batch->h2 : nullptr, batch ? batch->o : nullptr, err);
+  return (int)grid;
+}
+
+// -------------------------------------------------------------- parameters
+__global__ void k_mlp_pack(const float* __restrict__ p, MlpDev* __restrict__ d) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < kMlpH * kMlpK1) {
+    const int r = i / kMlpK1, k = i - r * kMlpK1;
+    d->w1[i] = __float2bfloat16_rn(k < kMlpIn ? p[kMlpOffW1 + r * kMlpIn + k] : 0.f);
+  }
+  if (i < kMlpH * kMlpH) d->w2[i] = __float2bfloat16_rn(p[kMlpOffW2 + i]);
+  if (i < kMlpN3 * kMlpH) {
+    const int r = i / kMlpH;
+    d->w3[i] = __float2bfloat16_rn(r < kMlpOut ? p[kMlpOffW3 + i] : 0.f);
+  }
+  if (i < kMlpH) {
+    d->b1[i] = p[kMlpOffB1 + i];
+    d->b2[i] = p[kMlpOffB2 + i];
+  }
+  if (i < kMlpN3) d->b3[i] = i < kMlpOut ? p[kMlpOffB3 + i] : 0.f;
+}
+
+void mlp_pack(const float* params, MlpDev* dev, cudaStream_t s) {
+  k_mlp_pack<<<(kMlpH * kMlpH + 255) / 256, 256, 0, s>>>(params, dev);
+}
+
+__global__ void k_features_bf16(const float* __restrict__ f, __nv_bfloat16* __restrict__ x, long long n) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n * kMlpK1;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long r = e / kMlpK1;
+    const int k = (int)(e - r * kMlpK1);
+    x[e] = __float2bfloat16_rn(k < kMlpIn ? f[r * kMlpIn + k] : 0.f);
+  }
+}
+
+void mlp_features_bf16(const float* f, __nv_bfloat16* x16, long long n, cudaStream_t s) {
+  long long g = (n * kMlpK1 + 255) / 256;
+  if (g > 152 * 32) g = 152 * 32;
+  if (g < 1) g = 1;
+  k_features_bf16<<<(int)g, 256, 0, s>>>(f, x16, n);
+}
+
+// ----------------------------------------------------------- backward pass
+// One CTA per tile of 128 points, thread t owns point t: it forms the
+// output, hidden-2 and hidden-1 deltas of L = (1/(2n)) sum (C - y)^2 in FP32
+// with the BF16 weights the forward pass used, stages them in shared memory,
+// and the CTA writes its partial weight gradients (and loss sum) to
+// part[blockIdx.x][kMlpParams + 1].
+constexpr int kBwdLd = kMlpH + 1;  // padded row of the shared delta tiles
+constexpr size_t kBwdSmem = sizeof(float) * ((size_t)kMlpTile * kBwdLd * 4 + (size_t)kMlpTile * (kMlpIn + 2) +
+                                             (size_t)kMlpH * kBwdLd + (size_t)kMlpOut * kMlpH);
+
+__global__ void __launch_bounds__(128) k_mlp_bwd(const __nv_bfloat16* __restrict__ x16, const float2* __restrict__ y,
+                                                 long long n, const MlpDev* __restrict__ P,
+                                                 const __nv_bfloat16* __restrict__ h1g,
+                                                 const __nv_bfloat16* __restrict__ h2g, const float* __restrict__ og,
+                                                 float* __restrict__ part) {
+  extern __shared__ __align__(16) float sm[];
+  float* d2 = sm;                         // [128][65] hidden-2 deltas
+  float* d1 = d2 + kMlpTile * kBwdLd;     // [128][65] hidden-1 deltas
+  float* h1 = d1 + kMlpTile * kBwdLd;     // [128][65]
+  float* h2 = h1 + kMlpTile * kBwdLd;     // [128][65]
+  float* xo = h2 + kMlpTile * kBwdLd;     // [128][14]: 12 inputs, 2 output deltas
+  float* w2 = xo + kMlpTile * (kMlpIn + 2);  // [64][65] W2[n][k]
+  float* w3 = w2 + kMlpH * kBwdLd;        // [2][64]
+  __shared__ float s_loss[4];
+  const int tid = threadIdx.x;
+  for (int e = tid; e < kMlpH * kMlpH; e += blockDim.x) w2[(e / kMlpH) * kBwdLd + e % kMlpH] = __bfloat162float(P->w2[e]);
+  for (int e = tid; e < kMlpOut * kMlpH; e += blockDim.x) w3[e] = __bfloat162float(P->w3[e]);
+  __syncthreads();
+  const long long row = (long long)blockIdx.x * kMlpTile + tid;
+  const bool live = row < n;
+  const float inv_n = 1.0f / (float)n;
+  float loss = 0.f;
+  float dout[kMlpOut] = {0.f, 0.f};
+  float a1[kMlpH], a2[kMlpH];
+#pragma unroll
+  for (int k = 0; k < kMlpH; ++k) {
+    a1[k] = live ? __bfloat162float(h1g[row * kMlpH + k]) : 0.f;
+    a2[k] = live ? __bfloat162float(h2g[row * kMlpH + k]) : 0.f;
+  }
+  if (live) {
+    const float2 yy = y[row];
+    const float tgt[2] = {yy.x, yy.y};
+#pragma unroll
+    for (int j = 0; j < kMlpOut; ++j) {
+      const float o = og[2 * row + j];
+      const float sig = 1.f / (1.f + expf(-o));
+      const float c = kMlpScale * softplus(o);
+      const float r = c - tgt[j];
+      loss += r * r;
+      dout[j] = r * inv_n * kMlpScale * sig;
+    }
+  }
+  // hidden 2
+#pragma unroll
+  for (int k = 0; k < kMlpH; ++k) {
+    const float g = dout[0] * w3[k] + dout[1] * w3[kMlpH + k];
+    d2[tid * kBwdLd + k] = a2[k] > 0.f ? g : 0.f;
+    h1[tid * kBwdLd + k] = a1[k];
+    h2[tid * kBwdLd + k] = a2[k];
+  }
+  // hidden 1: (d2 W2)_k = sum_n d2_n W2[n][k]
+  for (int k = 0; k < kMlpH; ++k) {
+    float g = 0.f;
+#pragma unroll 8
+    for (int m = 0; m < kMlpH; ++m) g += d2[tid * kBwdLd + m] * w2[m * kBwdLd + k];
+    d1[tid * kBwdLd + k] = a1[k] > 0.f ? g : 0.f;
+  }
+#pragma unroll
+  for (int i = 0; i < kMlpIn; ++i) xo[tid * (kMlpIn + 2) + i] = live ? __bfloat162float(x16[row * kMlpK1 + i]) : 0.f;
+  xo[tid * (kMlpIn + 2) + kMlpIn] = dout[0];
+  xo[tid * (kMlpIn + 2) + kMlpIn + 1] = dout[1];
+  // loss sum of the tile (fixed order)
+  for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+  if ((tid & 31) == 0) s_loss[tid >> 5] = loss;
+  __syncthreads();
+  float* out = part + (long long)blockIdx.x * (kMlpParams + 1);
+  // weight gradients as sums over the tile's points
+  for (int e = tid; e < kMlpH * kMlpIn; e += blockDim.x) {
+    const int r = e / kMlpIn, i = e - r * kMlpIn;
+    float g = 0.f;
+    for (int p = 0; p < kMlpTile; ++p) g += d1[p * kBwdLd + r] * xo[p * (kMlpIn + 2) + i];
+    out[kMlpOffW1 + e] = g;
+  }
+  for (int e = tid; e < kMlpH * kMlpH; e += blockDim.x) {
+    const int r = e / kMlpH, k = e - r * kMlpH;
+    float g = 0.f;
+    for (int p = 0; p < kMlpTile; ++p) g += d2[p * kBwdLd + r] * h1[p * kBwdLd + k];
+    out[kMlpOffW2 + e] = g;
+  }
+  for (int e = tid; e < kMlpOut * kMlpH; e += blockDim.x) {
+    const int j = e / kMlpH, k = e - j * kMlpH;
+    float g = 0.f;
+    for (int p = 0; p < kMlpTile; ++p) g += xo[p * (kMlpIn + 2) + kMlpIn + j] * h2[p * kBwdLd + k];
+    out[kMlpOffW3 + e] = g;
+  }
+  if (tid < kMlpH) {
+    float g1 = 0.f, g2 = 0.f;
+    for (int p = 0; p < kMlpTile; ++p) {
+      g1 += d1[p * kBwdLd + tid];
+      g2 += d2[p * kBwdLd + tid];
+    }
+    out[kMlpOffB1 + tid] = g1;
+    out[kMlpOffB2 + tid] = g2;
+  }
+  if (tid < kMlpOut) {
+    float g = 0.f;
+    for (int p = 0; p < kMlpTile; ++p) g += xo[p * (kMlpIn + 2) + kMlpIn + tid];
+    out[kMlpOffB3 + tid] = g;
+  }
+  if (tid == 0) out[kMlpParams] = (s_loss[0] + s_loss[1]) + (s_loss[2] + s_loss[3]);
+}
+
+// grad[p] = sum over CTAs of part[b][p] in CTA order; loss[0] likewise
+__global__ void k_mlp_reduce(const float* __restrict__ part, int nblk, float* __restrict__ grad,
+                             float* __restrict__ loss) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > kMlpParams) return;
+  float g = 0.f;
+  for (int b = 0; b < nblk; ++b) g += part[(long long)b * (kMlpParams + 1) + p];
+  if (p < kMlpParams) grad[p] = g;
+  else loss[0] = g;
+}
+
+long long mlp_partials(long long n) { return ((n + kMlpTile - 1) / kMlpTile) * (kMlpParams + 1); }
+
+void mlp_backward(const __nv_bfloat16* x16, const float2* y, long long n, const MlpDev* dev, const MlpBatch& batch,
+                  float* part, float* grad, float* loss, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+    attr = true;
+  }
+  const int nblk = (int)((n + kMlpTile - 1) / kMlpTile);
+  k_mlp_bwd<<<nblk, kMlpTile, kBwdSmem, s>>>(x16, y, n, dev, batch.h1, batch.h2, batch.o, part);
+  k_mlp_reduce<<<(kMlpParams + 1 + 255) / 256, 256, 0, s>>>(part, nblk, grad, loss);
+}
+
+// Adam (Kingma & Ba 2015): beta1 0.9, beta2 0.999, eps 1e-8, bias-corrected
+__global__ void k_mlp_adam(float* __restrict__ p, float* __restrict__ m, float* __restrict__ v,
+                           const float* __restrict__ g, float lr_t, float b1, float b2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kMlpParams) return;
+  const float gi = g[i];
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr_t * mi / (sqrtf(vi) + 1e-8f);
+}
+
+void mlp_adam(float* params, float* m, float* v, const float* grad, int step, float lr, MlpDev* dev,
+              cudaStream_t s) {
+  const double b1 = 0.9, b2 = 0.999;
+  const double lr_t = lr * sqrt(1.0 - pow(b2, step)) / (1.0 - pow(b1, step));
+  k_mlp_adam<<<(kMlpParams + 255) / 256, 256, 0, s>>>(params, m, v, grad, (float)lr_t, (float)b1, (float)b2);
+  mlp_pack(params, dev, s);
+}
+
+}  // namespace samgpu

@@ -14,6 +14,7 @@
 #include <vector>
 
 #include "../../include/sam_gpu.h"
+#include "closure.cuh"
 #include "common.cuh"
 #include "diag.cuh"
 #include "fields.cuh"
@@ -169,6 +170,11 @@ struct Ctx {
   void* les_phys = nullptr;    // physical velocity for dm.f (3 fields, working precision)
   double* les_work = nullptr;  // dm.f work arrays
   size_t s1_elems = 0, s2_elems = 0;
+  // learned closure: FP32 parameters with Adam moments, the BF16 device form
+  float *mlp_p = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_g = nullptr, *mlp_loss = nullptr;
+  MlpDev* mlp_dev = nullptr;
+  int* mlp_err = nullptr;
+  int mlp_step = 0;
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t graph_stream = nullptr;
   int graph_stale = 1;
@@ -457,6 +463,8 @@ static void free_ctx(Ctx* c) {
   cudaFree(c->S1); cudaFree(c->S2); cudaFree(c->S3);
   cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou);
   cudaFree(c->les_cds); cudaFree(c->les_phys); cudaFree(c->les_work);
+  cudaFree(c->mlp_p); cudaFree(c->mlp_m); cudaFree(c->mlp_v); cudaFree(c->mlp_g); cudaFree(c->mlp_loss);
+  cudaFree(c->mlp_dev); cudaFree(c->mlp_err);
   for (auto& s : c->sc) cudaFree(s.p);
   if (c->own) cudaStreamDestroy(c->own);
   delete c;
@@ -1023,6 +1031,177 @@ int sam_gpu_les_coef(double* c_delta_sq) {
   if (!c.les_model) return 0;
   CK(cudaMemcpyAsync(c_delta_sq, c.les_cds, sizeof(double), cudaMemcpyDeviceToHost, c.stream));
   return sync_stream(c);
+}
+
+// ---------------------------------------------------------- learned closure
+static int mlp_ensure(Ctx& c) {
+  if (c.mlp_p) return 0;
+  CK(cudaMalloc(&c.mlp_p, sizeof(float) * kMlpParams));
+  CK(cudaMalloc(&c.mlp_m, sizeof(float) * kMlpParams));
+  CK(cudaMalloc(&c.mlp_v, sizeof(float) * kMlpParams));
+  CK(cudaMalloc(&c.mlp_g, sizeof(float) * kMlpParams));
+  CK(cudaMalloc(&c.mlp_loss, sizeof(float) * 4));
+  CK(cudaMalloc(&c.mlp_dev, sizeof(MlpDev)));
+  CK(cudaMalloc(&c.mlp_err, sizeof(int)));
+  CK(cudaMemset(c.mlp_p, 0, sizeof(float) * kMlpParams));
+  CK(cudaMemset(c.mlp_m, 0, sizeof(float) * kMlpParams));
+  CK(cudaMemset(c.mlp_v, 0, sizeof(float) * kMlpParams));
+  CK(cudaMemset(c.mlp_err, 0, sizeof(int)));
+  mlp_pack(c.mlp_p, c.mlp_dev, c.stream);
+  return 0;
+}
+
+static int mlp_check_err(Ctx& c) {
+  int e = 0;
+  CK(cudaMemcpyAsync(&e, c.mlp_err, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  if (e) {
+    cudaMemsetAsync(c.mlp_err, 0, sizeof(int), c.stream);
+    return fail(SAM_GPU_ECUDA, "closure network: tensor-core wait timed out");
+  }
+  return check_launch();
+}
+
+int sam_gpu_mlp_set(const float* params, int n) {
+  NEED_CTX();
+  if (!params || n != kMlpParams) return fail(SAM_GPU_EINVAL, "mlp_set: need %d parameters", kMlpParams);
+  int rc = mlp_ensure(c);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(c.mlp_p, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice, c.stream));
+  CK(cudaMemsetAsync(c.mlp_m, 0, sizeof(float) * kMlpParams, c.stream));
+  CK(cudaMemsetAsync(c.mlp_v, 0, sizeof(float) * kMlpParams, c.stream));
+  c.mlp_step = 0;
+  mlp_pack(c.mlp_p, c.mlp_dev, c.stream);
+  return sync_stream(c);
+}
+
+int sam_gpu_mlp_get(float* params, int n) {
+  NEED_CTX();
+  if (!params || n != kMlpParams) return fail(SAM_GPU_EINVAL, "mlp_get: need %d parameters", kMlpParams);
+  int rc = mlp_ensure(c);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(params, c.mlp_p, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+// features [n][12] (host, FP32) into sc[0] as BF16 [n][16]; sc[1] gets
+// room for `extra` more bytes after the coefficients
+static int mlp_stage_inputs(Ctx& c, const float* feat, long long n, __nv_bfloat16** x16) {
+  int rc;
+  const size_t fb = sizeof(float) * kMlpIn * (size_t)n;
+  if ((rc = ensure(c.sc[2], fb)) || (rc = ensure(c.sc[0], sizeof(__nv_bfloat16) * kMlpK1 * (size_t)n))) return rc;
+  CK(cudaMemcpyAsync(c.sc[2].p, feat, fb, cudaMemcpyHostToDevice, c.stream));
+  mlp_features_bf16((const float*)c.sc[2].p, (__nv_bfloat16*)c.sc[0].p, n, c.stream);
+  *x16 = (__nv_bfloat16*)c.sc[0].p;
+  return 0;
+}
+
+int sam_gpu_mlp_forward(const float* feat, long long n, float* coef) {
+  NEED_CTX();
+  if (!feat || !coef || n < 0) return fail(SAM_GPU_EINVAL, "mlp_forward: bad arguments");
+  if (n == 0) return 0;
+  int rc = mlp_ensure(c);
+  if (rc) return rc;
+  __nv_bfloat16* x16;
+  if ((rc = mlp_stage_inputs(c, feat, n, &x16)) || (rc = ensure(c.sc[1], sizeof(float2) * (size_t)n))) return rc;
+  mlp_forward(x16, n, c.mlp_dev, (float2*)c.sc[1].p, nullptr, c.mlp_err, c.stream);
+  CK(cudaMemcpyAsync(coef, c.sc[1].p, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToHost, c.stream));
+  return mlp_check_err(c);
+}
+
+// device buffers of one minibatch of up to nb points: targets, activations,
+// outputs and gradient partials, carved from sc[3]
+struct MlpWork {
+  float2* y;
+  float2* coef;
+  MlpBatch b;
+  float* part;
+};
+static int mlp_work(Ctx& c, long long nb, MlpWork& w) {
+  const size_t need = sizeof(float2) * nb * 2 + sizeof(__nv_bfloat16) * kMlpH * nb * 2 + sizeof(float) * 2 * nb +
+                      sizeof(float) * (size_t)mlp_partials(nb) + 256 * 6;
+  int rc = ensure(c.sc[3], need);
+  if (rc) return rc;
+  uint8_t* p = (uint8_t*)c.sc[3].p;
+  auto take = [&](size_t bytes) {
+    uint8_t* q = p;
+    p += (bytes + 255) & ~(size_t)255;
+    return q;
+  };
+  w.y = (float2*)take(sizeof(float2) * nb);
+  w.coef = (float2*)take(sizeof(float2) * nb);
+  w.b.h1 = (__nv_bfloat16*)take(sizeof(__nv_bfloat16) * kMlpH * nb);
+  w.b.h2 = (__nv_bfloat16*)take(sizeof(__nv_bfloat16) * kMlpH * nb);
+  w.b.o = (float*)take(sizeof(float) * 2 * nb);
+  w.part = (float*)take(sizeof(float) * (size_t)mlp_partials(nb));
+  return 0;
+}
+
+int sam_gpu_mlp_grad(const float* feat, const float* target, long long n, float* grad, float* loss) {
+  NEED_CTX();
+  if (!feat || !target || !grad || n <= 0) return fail(SAM_GPU_EINVAL, "mlp_grad: bad arguments");
+  int rc = mlp_ensure(c);
+  if (rc) return rc;
+  __nv_bfloat16* x16;
+  MlpWork w;
+  if ((rc = mlp_stage_inputs(c, feat, n, &x16)) || (rc = mlp_work(c, n, w))) return rc;
+  CK(cudaMemcpyAsync(w.y, target, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, c.stream));
+  mlp_forward(x16, n, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream);
+  mlp_backward(x16, w.y, n, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss, c.stream);
+  CK(cudaMemcpyAsync(grad, c.mlp_g, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, c.stream));
+  float ls = 0.f;
+  CK(cudaMemcpyAsync(&ls, c.mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+  rc = mlp_check_err(c);
+  if (loss) *loss = ls / (2.0f * (float)n);
+  return rc;
+}
+
+int sam_gpu_mlp_train(const float* feat, const float* target, long long n, int steps, int batch, float lr,
+                      float* loss_hist) {
+  NEED_CTX();
+  if (!feat || !target || n <= 0 || steps < 0 || batch <= 0 || !(lr > 0.f))
+    return fail(SAM_GPU_EINVAL, "mlp_train: bad arguments");
+  int rc = mlp_ensure(c);
+  if (rc) return rc;
+  const long long nb = batch < n ? batch : n;
+  __nv_bfloat16* x16;
+  MlpWork w;
+  if ((rc = mlp_stage_inputs(c, feat, n, &x16)) || (rc = mlp_work(c, nb, w))) return rc;
+  // all targets on the device; minibatch s is the contiguous chunk s (mod the
+  // number of full chunks) of the data as given (the caller shuffles)
+  if ((rc = ensure(c.sc[2], sizeof(float2) * (size_t)n))) return rc;
+  float2* y_all = (float2*)c.sc[2].p;
+  CK(cudaMemcpyAsync(y_all, target, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, c.stream));
+  const long long nchunks = n / nb;
+  std::vector<float> hist((size_t)steps);
+  for (int s = 0; s < steps; ++s) {
+    const long long off = (s % nchunks) * nb;
+    mlp_forward(x16 + off * kMlpK1, nb, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream);
+    mlp_backward(x16 + off * kMlpK1, y_all + off, nb, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss + 0, c.stream);
+    mlp_adam(c.mlp_p, c.mlp_m, c.mlp_v, c.mlp_g, ++c.mlp_step, lr, c.mlp_dev, c.stream);
+    if (loss_hist) CK(cudaMemcpyAsync(&hist[s], c.mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, c.stream));
+  }
+  rc = mlp_check_err(c);
+  if (loss_hist)
+    for (int s = 0; s < steps; ++s) loss_hist[s] = hist[s] / (2.0f * (float)nb);
+  return rc;
+}
+
+int sam_gpu_mma_selftest(const float* a, const float* b, float* d) {
+  NEED_CTX();
+  if (!a || !b || !d) return fail(SAM_GPU_EINVAL, "mma_selftest: null array");
+  int rc = mlp_ensure(c);
+  if (rc) return rc;
+  if ((rc = ensure(c.sc[0], 2 * (128 * 16 + 64 * 16) + 256)) || (rc = ensure(c.sc[1], 4 * 128 * 64))) return rc;
+  std::vector<__nv_bfloat16> h(128 * 16 + 64 * 16);
+  for (int i = 0; i < 128 * 16; ++i) h[i] = __float2bfloat16_rn(a[i]);
+  for (int i = 0; i < 64 * 16; ++i) h[128 * 16 + i] = __float2bfloat16_rn(b[i]);
+  CK(cudaMemcpyAsync(c.sc[0].p, h.data(), 2 * h.size(), cudaMemcpyHostToDevice, c.stream));
+  CK(cudaStreamSynchronize(c.stream));
+  const __nv_bfloat16* da = (const __nv_bfloat16*)c.sc[0].p;
+  mlp_mma_selftest(da, da + 128 * 16, (float*)c.sc[1].p, c.mlp_err, c.stream);
+  CK(cudaMemcpyAsync(d, c.sc[1].p, 4 * 128 * 64, cudaMemcpyDeviceToHost, c.stream));
+  return mlp_check_err(c);
 }
 
 int sam_gpu_measure_fp64_peak(double* tflops) {

@@ -31,7 +31,12 @@ EXPORTS = [
     "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
     "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_planes",
     "sam_gpu_set_forcing", "sam_gpu_set_les", "sam_gpu_les_coef",
+    "sam_gpu_mlp_set", "sam_gpu_mlp_get", "sam_gpu_mlp_forward", "sam_gpu_mlp_grad", "sam_gpu_mlp_train",
+    "sam_gpu_mma_selftest",
 ]
+
+MLP_PARAMS = 5122
+MLP_FEATURES = 12
 
 
 class SamGpuError(RuntimeError):
@@ -110,6 +115,12 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_tiles.argtypes = [P]
     lib.sam_gpu_set_forcing.argtypes = [C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int)]
     lib.sam_gpu_set_les.argtypes = [C.c_int, C.c_double, C.c_double]
+    lib.sam_gpu_mlp_set.argtypes = [P, C.c_int]
+    lib.sam_gpu_mlp_get.argtypes = [P, C.c_int]
+    lib.sam_gpu_mlp_forward.argtypes = [P, C.c_longlong, P]
+    lib.sam_gpu_mlp_grad.argtypes = [P, P, C.c_longlong, P, P]
+    lib.sam_gpu_mlp_train.argtypes = [P, P, C.c_longlong, C.c_int, C.c_int, C.c_float, P]
+    lib.sam_gpu_mma_selftest.argtypes = [P, P, P]
     lib.sam_gpu_les_coef.argtypes = [C.POINTER(C.c_double)]
     lib.sam_gpu_planes.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
     lib.sam_gpu_force.argtypes = [P, C.c_int]
@@ -345,6 +356,57 @@ class SamGpu:
         v = C.c_double(0.0)
         self._check(load_library().sam_gpu_les_coef(C.byref(v)), "les_coef")
         return v.value
+
+    # ---- learned closure
+    @staticmethod
+    def _f32(a, shape=None):
+        a = np.ascontiguousarray(a, dtype=np.float32)
+        if shape is not None:
+            a = a.reshape(shape)
+        return a
+
+    def mlp_set(self, params):
+        p = self._f32(params, (MLP_PARAMS,))
+        self._check(load_library().sam_gpu_mlp_set(p.ctypes.data_as(C.c_void_p), MLP_PARAMS), "mlp_set")
+
+    def mlp_get(self):
+        p = np.zeros(MLP_PARAMS, dtype=np.float32)
+        self._check(load_library().sam_gpu_mlp_get(p.ctypes.data_as(C.c_void_p), MLP_PARAMS), "mlp_get")
+        return p
+
+    def mlp_forward(self, features):
+        f = self._f32(features).reshape(-1, MLP_FEATURES)
+        out = np.zeros((len(f), 2), dtype=np.float32)
+        self._check(load_library().sam_gpu_mlp_forward(f.ctypes.data_as(C.c_void_p), len(f),
+                                                       out.ctypes.data_as(C.c_void_p)), "mlp_forward")
+        return out
+
+    def mlp_grad(self, features, target):
+        f = self._f32(features).reshape(-1, MLP_FEATURES)
+        t = self._f32(target).reshape(-1, 2)
+        g = np.zeros(MLP_PARAMS, dtype=np.float32)
+        loss = C.c_float(0.0)
+        self._check(load_library().sam_gpu_mlp_grad(f.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p),
+                                                    len(f), g.ctypes.data_as(C.c_void_p), C.byref(loss)),
+                    "mlp_grad")
+        return g, loss.value
+
+    def mlp_train(self, features, target, steps, batch=8192, lr=1e-3):
+        f = self._f32(features).reshape(-1, MLP_FEATURES)
+        t = self._f32(target).reshape(-1, 2)
+        hist = np.zeros(max(steps, 1), dtype=np.float32)
+        self._check(load_library().sam_gpu_mlp_train(f.ctypes.data_as(C.c_void_p), t.ctypes.data_as(C.c_void_p),
+                                                     len(f), steps, batch, lr, hist.ctypes.data_as(C.c_void_p)),
+                    "mlp_train")
+        return hist[:steps]
+
+    def mma_selftest(self, a, b):
+        a = self._f32(a, (128, 16))
+        b = self._f32(b, (64, 16))
+        d = np.zeros((128, 64), dtype=np.float32)
+        self._check(load_library().sam_gpu_mma_selftest(a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p),
+                                                       d.ctypes.data_as(C.c_void_p)), "mma_selftest")
+        return d
 
     def planes(self, k_xy=(), j_xz=(), i_yz=()):
         """Planes output of the resident state (sam.f:145-166, write_planes.f),

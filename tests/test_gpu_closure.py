@@ -1,0 +1,87 @@
+"""The learned closure's network on the GPU: the tcgen05 tensor-core path
+against a host product, the forward and backward passes against the numpy
+restatement (oracle/closure.py), and training with Adam."""
+import numpy as np
+import pytest
+
+import closure as CL
+from sam_gb300 import SamGpu
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    g = SamGpu(nx=16, ny=16, nz=16)
+    yield g
+    g.close()
+
+
+def test_mma_known_answer(gpu_lib, ctx):
+    """One M=128, N=64, K=16 tcgen05.mma: BF16 inputs, FP32 accumulation."""
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal((128, 16)).astype(np.float32)
+    b = rng.standard_normal((64, 16)).astype(np.float32)
+    d = ctx.mma_selftest(a, b)
+    ref = CL.bf16(a).astype(np.float64) @ CL.bf16(b).astype(np.float64).T
+    assert np.abs(d - ref).max() <= 1e-5 * np.abs(ref).max()
+    # structured operands pin the layout: row r of a is e_(r mod 16), so row
+    # r of d is column (r mod 16) of b^T
+    a = np.zeros((128, 16), np.float32)
+    a[np.arange(128), np.arange(128) % 16] = 1.0
+    b = (np.arange(64 * 16, dtype=np.float32).reshape(64, 16) % 251)
+    d = ctx.mma_selftest(a, b)
+    assert np.array_equal(d, CL.bf16(b).T[np.arange(128) % 16])
+
+
+def test_forward_matches_oracle(gpu_lib, ctx):
+    rng = np.random.default_rng(1)
+    p = CL.init_params(2)
+    p[CL.OFF_W3:CL.OFF_B3] *= 10
+    p[CL.OFF_B1:CL.OFF_W2] = 0.1 * rng.standard_normal(CL.N_H)
+    x = rng.standard_normal((1000, CL.N_IN)).astype(np.float32)  # not a multiple of the 128-point tile
+    ctx.mlp_set(p)
+    assert np.array_equal(ctx.mlp_get(), p)
+    got = ctx.mlp_forward(x)
+    ref = CL.forward(p, x)[0]
+    err = np.abs(got - ref)
+    # FP32 accumulation order differs from the oracle's float64 sums; a BF16
+    # activation may round the other way at a tie, so bound the worst case
+    # loosely and the typical case tightly
+    assert err.max() <= 2e-3 * np.abs(ref).max()
+    assert np.median(err / np.abs(ref)) < 1e-5
+
+
+def test_gradient_matches_oracle(gpu_lib, ctx):
+    rng = np.random.default_rng(2)
+    p = CL.init_params(3)
+    p[CL.OFF_W3:CL.OFF_B3] *= 10
+    ctx.mlp_set(p)
+    x = rng.standard_normal((2048 + 77, CL.N_IN)).astype(np.float32)
+    y = (0.02 * np.abs(rng.standard_normal((len(x), 2)))).astype(np.float32)
+    g, loss = ctx.mlp_grad(x, y)
+    gr, lr = CL.grad(p, x, y)
+    assert abs(loss - lr) <= 1e-4 * lr
+    assert np.linalg.norm(g - gr) <= 2e-3 * np.linalg.norm(gr)
+    for lo, hi in ((CL.OFF_W1, CL.OFF_B1), (CL.OFF_W2, CL.OFF_B2), (CL.OFF_W3, CL.OFF_B3), (CL.OFF_B3, CL.N_PARAMS)):
+        assert np.linalg.norm(g[lo:hi] - gr[lo:hi]) <= 5e-3 * np.linalg.norm(gr[lo:hi]), (lo, hi)
+
+
+def test_adam_training_fits_a_smooth_target(gpu_lib, ctx):
+    """A coefficient that depends on two of the inputs: 300 Adam steps of
+    batch 1024 cut the loss by more than 10x and generalise to new points."""
+    rng = np.random.default_rng(4)
+
+    def target(x):
+        return np.stack([0.01 + 0.01 * np.tanh(x[:, 0]), 0.015 + 0.005 * np.sin(x[:, 1])], axis=1).astype(np.float32)
+
+    x = rng.standard_normal((1 << 16, CL.N_IN)).astype(np.float32)
+    ctx.mlp_set(CL.init_params(5))
+    hist = ctx.mlp_train(x, target(x), steps=300, batch=1024, lr=3e-3)
+    assert hist[-10:].mean() < 0.1 * hist[:5].mean()
+    xt = rng.standard_normal((4096, CL.N_IN)).astype(np.float32)
+    err = ctx.mlp_forward(xt) - target(xt)
+    assert np.sqrt((err ** 2).mean()) < 0.2 * np.sqrt(((target(xt) - target(xt).mean(0)) ** 2).mean())
+    # the trained parameters reproduce the GPU forward pass in the oracle
+    p = ctx.mlp_get()
+    assert np.abs(CL.forward(p, xt)[0] - ctx.mlp_forward(xt)).max() <= 2e-3 * 0.03
