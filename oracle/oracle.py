@@ -101,6 +101,8 @@ def lib():
         _lib.so_set_les.argtypes = [P, C.c_int, C.c_double, C.c_double]
         _lib.so_les_coef.argtypes = [P]
         _lib.so_les_coef.restype = C.c_double
+        _lib.so_mlp_set.argtypes = [P, P]
+        _lib.so_closure_invariants.argtypes = [P, P, P, C.c_double, C.c_double, C.c_double, C.c_double, P]
         _lib.so_planes.argtypes = [P, P, P, P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
         _lib.so_write_field.argtypes = [P, C.c_char_p, P]
         _lib.so_read_field.argtypes = [P, C.c_char_p, P]
@@ -116,6 +118,18 @@ def fft_line(data: np.ndarray, kind: str) -> np.ndarray:
     if rc:
         raise ValueError(f"unsupported length {len(a)}")
     return a
+
+
+def closure_invariants(S, g, w, bz=0.0, n2=0.0, dsq=1.0, nu=1.0):
+    """The learned closure's 12 inputs of one point (oracle formulas)."""
+    S = np.ascontiguousarray(S, dtype=np.float64)
+    g = np.ascontiguousarray(g, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    f = np.zeros(12, dtype=np.float32)
+    v = C.c_void_p
+    lib().so_closure_invariants(S.ctypes.data_as(v), g.ctypes.data_as(v), w.ctypes.data_as(v), bz, n2, dsq, nu,
+                                f.ctypes.data_as(v))
+    return f
 
 
 def _p(a: np.ndarray):
@@ -285,6 +299,12 @@ class Oracle:
         2 dynamic (dm.f coefficient at nrk = 1); kappa_t = nu_t / pr_t."""
         if lib().so_set_les(self.h, model, c_smag, pr_t):
             raise ValueError("bad LES arguments")
+
+    def mlp_set(self, params):
+        """Parameters of the learned closure (model 3 of set_les)."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        assert p.size == 5122
+        lib().so_mlp_set(self.h, p.ctypes.data_as(C.c_void_p))
 
     def les_coef(self):
         """C delta^2 last used by the coupled closure."""

@@ -59,6 +59,7 @@ struct so_ctx {
   double *les_g;      /* physical gradient fields (Nx, Ny, Nz, Lr) */
   double *les_uh;     /* haloed velocity (Lx, Ly, Lz, 3) for so_dm */
   double *les_vt;     /* haloed vt of so_dm */
+  float les_mlp[5122]; /* learned closure parameters (so_mlp_set) */
 };
 
 static const double SO_PI = 3.14159265358979323846;
@@ -459,10 +460,11 @@ int so_stage(so_ctx *c, double *ud, double *rd, int nrk) {
   so_z_trans_b(c, ud, (double *)c->zb, lu);
   if (c->les_model) {
     /* gradient fields of the current u to physical space */
+    const int ng = c->lr + (c->les_model == 3 ? 3 : 0);
     so_les_fields(c, u);
-    so_z_trans_b(c, (const double *)c->les_w, (double *)c->les_zb, c->lr);
-    so_x2z_decomp(c, (const double *)c->les_zb, c->les_g, c->lr);
-    so_xy_trans_b(c, c->les_g, c->les_g, c->lr);
+    so_z_trans_b(c, (const double *)c->les_w, (double *)c->les_zb, ng);
+    so_x2z_decomp(c, (const double *)c->les_zb, c->les_g, ng);
+    so_xy_trans_b(c, c->les_g, c->les_g, ng);
     c->les_stage = 1;
   }
   if (c->cfg.i_strat) {
@@ -1444,7 +1446,86 @@ static void so_les_fields(so_ctx *c, const so_cplx *u) {
         }
         if (c->cfg.i_strat)
           for (int a = 0; a < 3; ++a) w[W_IDX(c, k, j, i, 6 + a)] = I * kv[a] * u[W_IDX(c, k, j, i, 3)];
+        if (c->les_model == 3)
+          for (int a = 0; a < 3; ++a) {
+            /* vorticity w_a = i (k_b u_c - k_c u_b), (a, b, c) cyclic */
+            const int b = (a + 1) % 3, cc = (a + 2) % 3;
+            w[W_IDX(c, k, j, i, c->lr + a)] =
+                I * (kv[b] * u[W_IDX(c, k, j, i, cc)] - kv[cc] * u[W_IDX(c, k, j, i, b)]);
+          }
       }
+}
+
+/* round to the nearest BF16 (ties to even) */
+static float so_bf16(float x) {
+  uint32_t u;
+  memcpy(&u, &x, 4);
+  u = (u + 0x7FFFu + ((u >> 16) & 1u)) & 0xFFFF0000u;
+  memcpy(&x, &u, 4);
+  return x;
+}
+
+/* The learned closure's 12 invariants of one point (strain S in product
+ * order, temperature gradient g, vorticity w); the same formulas as the
+ * CUDA feature pass (closure_invariants). */
+static void so_invariants(const double *S, const double *g, const double *w, double bz, double n2, double dsq,
+                          double nu, float *f) {
+  const double eps = 1e-30;
+  const double M[3][3] = {{S[0], S[1], S[3]}, {S[1], S[2], S[4]}, {S[3], S[4], S[5]}};
+  double s2 = 0, tr3 = 0, wSw = 0, gSg = 0;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      s2 += M[i][j] * M[i][j];
+      double sq = 0;
+      for (int k = 0; k < 3; ++k) sq += M[i][k] * M[k][j];
+      tr3 += sq * M[j][i];
+      wSw += w[i] * M[i][j] * w[j];
+      gSg += g[i] * M[i][j] * g[j];
+    }
+  s2 = 2 * s2;
+  const double sn = sqrt(s2);
+  const double w2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2], wn = sqrt(w2);
+  const double g2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2], gn = sqrt(g2);
+  const double inv_s2 = 1.0 / (s2 + eps);
+  f[0] = (float)log1p(w2 * inv_s2);
+  f[1] = (float)(tr3 / (s2 * sn + eps));
+  f[2] = (float)(wSw / (sn * w2 + eps));
+  f[3] = (float)log1p(fabs(n2) * inv_s2);
+  f[4] = (float)asinh(bz * g[2] * inv_s2);
+  f[5] = (float)log1p(fabs(bz) * sqrt(g[0] * g[0] + g[1] * g[1]) * inv_s2);
+  f[6] = (float)(M[2][2] / (sn + eps));
+  f[7] = (float)(w[2] / (sn + wn + eps));
+  f[8] = (float)(gSg / (sn * g2 + eps));
+  f[9] = (float)((w[0] * g[0] + w[1] * g[1] + w[2] * g[2]) / (wn * gn + eps));
+  f[10] = (float)log1p(sn * dsq / nu);
+  f[11] = (float)(4 * (S[3] * S[3] + S[4] * S[4]) * inv_s2);
+}
+
+/* The network of the learned closure (12 -> 64 -> 64 -> 2, ReLU, BF16
+ * weights, inputs and hidden activations): (C_nu, C_kappa) =
+ * 0.02 softplus(o) in FP32 as the GPU returns them. */
+static void so_mlp_eval(const float *p, const float *f, float *cout) {
+  double x[12], h1[64], h2[64];
+  for (int i = 0; i < 12; ++i) x[i] = so_bf16(f[i]);
+  for (int n = 0; n < 64; ++n) {
+    double a = 0;
+    for (int i = 0; i < 12; ++i) a += (double)so_bf16(p[n * 12 + i]) * x[i];
+    a += p[768 + n];
+    h1[n] = so_bf16((float)(a > 0 ? a : 0));
+  }
+  for (int n = 0; n < 64; ++n) {
+    double a = 0;
+    for (int k = 0; k < 64; ++k) a += (double)so_bf16(p[832 + n * 64 + k]) * h1[k];
+    a += p[4928 + n];
+    h2[n] = so_bf16((float)(a > 0 ? a : 0));
+  }
+  for (int j = 0; j < 2; ++j) {
+    double a = 0;
+    for (int k = 0; k < 64; ++k) a += (double)so_bf16(p[4992 + j * 64 + k]) * h2[k];
+    const float o = (float)a + p[5120 + j];
+    const float sp = o > 20.f ? o : log1pf(expf(o));
+    cout[j] = 0.02f * sp;
+  }
 }
 
 static void so_les_stress(so_ctx *c, const double *uu, int nrk) {
@@ -1465,6 +1546,31 @@ static void so_les_stress(so_ctx *c, const double *uu, int nrk) {
   }
   const double cds = c->les_cds, prt_inv = c->les_prt_inv;
   double *g = c->les_g;
+  if (c->les_model == 3) {
+    const double dsq = delta_sq_of(c), bz = c->cfg.buoy_fac_z, n2 = c->cfg.buoy_fac_z * c->cfg.lapse;
+    const double nu_ref = c->cfg.vis > 1e-12 ? c->cfg.vis : 1e-12;
+    const int lr = c->lr;
+    set_threads(c);
+#pragma omp parallel for schedule(static)
+    for (size_t p = 0; p < np; ++p) {
+      double S[6], gt[3] = {0, 0, 0}, w[3];
+      for (int m = 0; m < 6; ++m) S[m] = g[p + m * np];
+      if (lr == 9)
+        for (int m = 0; m < 3; ++m) gt[m] = g[p + (6 + m) * np];
+      for (int m = 0; m < 3; ++m) w[m] = g[p + (lr + m) * np];
+      float f[12], cf[2];
+      so_invariants(S, gt, w, bz, n2, dsq, nu_ref, f);
+      so_mlp_eval(c->les_mlp, f, cf);
+      double sum = 0.0;
+      for (int m = 0; m < 6; ++m) sum += (m == 1 || m == 3 || m == 4 ? 2.0 : 1.0) * S[m] * S[m];
+      const double sm = sqrt(2.0 * sum);
+      const double nu = ((double)cf[0] * dsq) * sm, kap = ((double)cf[1] * dsq) * sm;
+      const double nu2 = 2.0 * nu;
+      for (int m = 0; m < 6; ++m) g[p + m * np] = -nu2 * g[p + m * np];
+      for (int m = 6; m < lr; ++m) g[p + m * np] = -kap * g[p + m * np];
+    }
+    return;
+  }
   set_threads(c);
 #pragma omp parallel for schedule(static)
   for (size_t p = 0; p < np; ++p) {
@@ -1481,21 +1587,37 @@ static void so_les_stress(so_ctx *c, const double *uu, int nrk) {
 }
 
 int so_set_les(so_ctx *c, int model, double c_smag, double pr_t) {
-  if (model < 0 || model > 2 || !(pr_t > 0.0)) return -1;
+  if (model < 0 || model > 3 || !(pr_t > 0.0)) return -1;
+  if (c->les_w && model == 3 && c->les_model != 3) {
+    /* the learned closure carries three more fields: reallocate */
+    free(c->les_w); free(c->les_zb); free(c->les_g); free(c->les_uh); free(c->les_vt);
+    c->les_w = NULL;
+  }
   c->les_model = model;
   c->les_c_smag = c_smag;
   c->les_prt_inv = 1.0 / pr_t;
   c->les_cds = model == 1 ? c_smag * delta_sq_of(c) : 0.0;
   if (!model || c->les_w) return 0;
-  const size_t nw = (size_t)c->nze * c->ny_min * c->nx_min * c->lr;
+  const int ng = c->lr + 3; /* room for the learned closure's vorticity */
+  const size_t nw = (size_t)c->nze * c->ny_min * c->nx_min * ng;
   const size_t np = (size_t)c->nx * c->ny * c->nz;
   const size_t vol = (size_t)(c->nx + 2) * (c->ny + 2) * (c->nz + 2);
   c->les_w = (so_cplx *)calloc(nw, sizeof(so_cplx));
-  c->les_zb = (so_cplx *)calloc((size_t)c->ny_min * c->nx_min * c->nze * c->lr, sizeof(so_cplx));
-  c->les_g = (double *)calloc(np * c->lr, sizeof(double));
+  c->les_zb = (so_cplx *)calloc((size_t)c->ny_min * c->nx_min * c->nze * ng, sizeof(so_cplx));
+  c->les_g = (double *)calloc(np * ng, sizeof(double));
   c->les_uh = (double *)calloc(vol * 3, sizeof(double));
   c->les_vt = (double *)calloc(vol, sizeof(double));
   return 0;
 }
 
 double so_les_coef(const so_ctx *c) { return c->les_cds; }
+
+int so_mlp_set(so_ctx *c, const float *params) {
+  memcpy(c->les_mlp, params, sizeof(c->les_mlp));
+  return 0;
+}
+
+void so_closure_invariants(const double *S, const double *g, const double *w, double bz, double n2, double dsq,
+                           double nu, float *f) {
+  so_invariants(S, g, w, bz, n2, dsq, nu, f);
+}

@@ -115,6 +115,12 @@ int so_set_forcing(so_ctx *c, unsigned long long seed, double k_f, double sigma,
  * nrk = 1); kappa_t = nu_t / pr_t; -1 on bad arguments */
 int so_set_les(so_ctx *c, int model, double c_smag, double pr_t);
 double so_les_coef(const so_ctx *c);
+/* model 3 of so_set_les: the learned closure; params are its 5122 FP32
+ * parameters (W1 64x12, b1, W2 64x64, b2, W3 2x64, b3) */
+int so_mlp_set(so_ctx *c, const float *params);
+/* the closure's 12 invariants of one point */
+void so_closure_invariants(const double *S, const double *g, const double *w, double bz, double n2, double dsq,
+                           double nu, float *f);
 int so_write_field(so_ctx *c, const char *fname, const double *u);
 /* 0 ok, -1 open, -2 wrong size (read_field.f:74-80), -3 short read */
 int so_read_field(so_ctx *c, const char *fname, double *u);

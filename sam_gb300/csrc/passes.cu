@@ -12,6 +12,7 @@
 //   y_fwd  : xy_trans_f.f:39-54      (m, z, kx, y)    -> (m, kx, ky, z)
 //   z_fwd  : z_trans_f.f:144-157 + rhs.f:108-142 + sam.f:210-221,293-314
 //            (m, kx, ky, z) -> projected rhs, RK3 update of u
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
 
@@ -99,9 +100,15 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
     // gradient field m of the subgrid stress: S_ab = (i/2)(k_b u_a + k_a u_b)
     // (i k_a u_a when a = b) for the six velocity products in rhs.f's order,
     // i k_a T for the three buoyancy products
+    // (fields m >= Lr: the vorticity w_a = i (k_b u_c - k_c u_b), (a, b, c)
+    // cyclic, which only the learned closure's invariants use)
     const int m = n - a.g.lu;
+    const bool vort = m >= a.g.lr;
     int fa, fb;
-    if (m < 6) {
+    if (vort) {
+      fa = (m - a.g.lr + 2) % 3;  // u_c, multiplied by k_b
+      fb = (m - a.g.lr + 1) % 3;  // u_b, multiplied by k_c
+    } else if (m < 6) {
       fb = m < 1 ? 0 : (m < 3 ? 1 : 2);
       fa = m - (fb * (fb + 1)) / 2;
     } else {
@@ -109,8 +116,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
       fb = 3;
     }
     const long long off = (long long)i * a.in_kx + (long long)j0 * a.in_ky;
-    const C* srca = a.in + (long long)(m < 6 ? fa : 3) * a.in_n + off;
-    const C* srcb = a.in + (long long)(m < 6 ? fb : 3) * a.in_n + off;
+    const C* srca = a.in + (long long)(vort || m < 6 ? fa : 3) * a.in_n + off;
+    const C* srcb = a.in + (long long)(vort || m < 6 ? fb : 3) * a.in_n + off;
     const double kxv = a.g.wave_x * (double)i;
     batched<C>(
         nl * nz,
@@ -124,7 +131,12 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
             const double kv[3] = {kxv, a.g.wave_y * (double)kwave(j0 + t, a.g.ky, my),
                                   a.g.wave_z * (double)kwave(q, km, mz)};
             const C ua = srca[(long long)t * a.in_ky + q];
-            if (m >= 6) {
+            if (vort) {
+              const C ub = srcb[(long long)t * a.in_ky + q];
+              const T kb = (T)kv[fb], kc = (T)kv[fa];  // w_a = i (k_b u_c - k_c u_b)
+              const T zr = kb * ua.x - kc * ub.x, zi = kb * ua.y - kc * ub.y;
+              v = mk<C>(-zi, zr);
+            } else if (m >= 6) {
               const T k = (T)kv[fa];
               v = mk<C>(-k * ua.y, k * ua.x);
             } else if (fa == fb) {
@@ -254,6 +266,83 @@ __device__ __forceinline__ void sgs_point(T* s, int nf, T cds, T prt_inv) {
 #pragma unroll
   for (int m = 6; m < 9; ++m)
     if (m < nf) s[m] = -kap * s[m];
+}
+
+// As sgs_point with per-point coefficients: nu_t = cnu |S|, kappa_t = ckap |S|.
+template <typename T>
+__device__ __forceinline__ void sgs_point_c(T* s, int nf, T cnu, T ckap) {
+  T sum = (T)0;
+#pragma unroll
+  for (int m = 0; m < 6; ++m) sum += (m == 1 || m == 3 || m == 4 ? (T)2 : (T)1) * s[m] * s[m];
+  const T sm = sqrt((T)2 * sum);
+  const T nu = cnu * sm, kap = ckap * sm;
+  const T nu2 = (T)2 * nu;
+#pragma unroll
+  for (int m = 0; m < 6; ++m) s[m] = -nu2 * s[m];
+#pragma unroll
+  for (int m = 6; m < 9; ++m)
+    if (m < nf) s[m] = -kap * s[m];
+}
+
+// The learned closure's 12 inputs at one point from the strain S (product
+// order S11 S12 S22 S13 S23 S33), the temperature gradient g and the
+// vorticity w; |S| = sqrt(2 S:S), eps = 1e-30:
+//   f0 log(1 + |w|^2/|S|^2)           f6  S33 / |S|
+//   f1 tr(S^3) / |S|^3                f7  w_z / (|S| + |w|)
+//   f2 w.S.w / (|S| |w|^2)            f8  g.S.g / (|S| |g|^2)
+//   f3 log(1 + |N^2| / |S|^2)         f9  w.g / (|w| |g|)
+//   f4 asinh(b g_z / |S|^2)           f10 log(1 + |S| delta^2 / nu)
+//   f5 log(1 + |b| |g_h| / |S|^2)     f11 4 (S13^2 + S23^2) / |S|^2
+// (b = buoy_fac_z, g_h the horizontal part of g).
+template <typename T>
+__device__ __forceinline__ void closure_invariants(const T* S, const T* g, const T* w, T bz, T n2, T dsq, T nu,
+                                                   float* f) {
+  const T eps = (T)1e-30;
+  const T M[3][3] = {{S[0], S[1], S[3]}, {S[1], S[2], S[4]}, {S[3], S[4], S[5]}};
+  T s2 = (T)0, tr3 = (T)0, wSw = (T)0, gSg = (T)0;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      s2 += M[i][j] * M[i][j];
+      T sq = (T)0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k) sq += M[i][k] * M[k][j];
+      tr3 += sq * M[j][i];
+      wSw += w[i] * M[i][j] * w[j];
+      gSg += g[i] * M[i][j] * g[j];
+    }
+  s2 = (T)2 * s2;
+  const T sn = sqrt(s2);
+  const T w2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2], wn = sqrt(w2);
+  const T g2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2], gn = sqrt(g2);
+  const T inv_s2 = (T)1 / (s2 + eps);
+  f[0] = (float)log1p(w2 * inv_s2);
+  f[1] = (float)(tr3 / (s2 * sn + eps));
+  f[2] = (float)(wSw / (sn * w2 + eps));
+  f[3] = (float)log1p(fabs(n2) * inv_s2);
+  f[4] = (float)asinh(bz * g[2] * inv_s2);
+  f[5] = (float)log1p(fabs(bz) * sqrt(g[0] * g[0] + g[1] * g[1]) * inv_s2);
+  f[6] = (float)(M[2][2] / (sn + eps));
+  f[7] = (float)(w[2] / (sn + wn + eps));
+  f[8] = (float)(gSg / (sn * g2 + eps));
+  f[9] = (float)((w[0] * g[0] + w[1] * g[1] + w[2] * g[2]) / (wn * gn + eps));
+  f[10] = (float)log1p(sn * dsq / nu);
+  f[11] = (float)((T)4 * (S[3] * S[3] + S[4] * S[4]) * inv_s2);
+}
+
+__device__ __forceinline__ void store_features(void* feat, long long pt, const float* f) {
+  uint32_t q[8];
+#pragma unroll
+  for (int i = 0; i < 6; ++i) {
+    const __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
+    q[i] = *reinterpret_cast<const uint32_t*>(&h);
+  }
+  q[6] = 0u;
+  q[7] = 0u;
+  uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(feat) + pt * 16);
+  dst[0] = make_uint4(q[0], q[1], q[2], q[3]);
+  dst[1] = make_uint4(q[4], q[5], q[6], q[7]);
 }
 
 // ------------------------------------------------------------------ x pass
@@ -396,10 +485,51 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
     }
   }
 
+  // ---- the closure's invariants (out_mode 4): inputs are S (6), dT/dx (3
+  // when Lr = 9) and w (3)
+  if (a.out_mode == 4) {
+    const int lr = a.g.lr;
+    const T bz = (T)a.f_bz, n2 = (T)a.f_n2, dsq = (T)a.f_dsq, nu = (T)a.f_nu;
+    for (int e = threadIdx.x; e < yp * nx; e += blockDim.x) {
+      const int c = (int)fdiv(e, a.fd_nx), x = e - c * nx;
+      T sx[6], sy[6], gx[3] = {(T)0, (T)0, (T)0}, gy[3] = {(T)0, (T)0, (T)0}, wx[3], wy[3];
+#pragma unroll
+      for (int m = 0; m < 6; ++m) {
+        const C v = s_in[(m * yp + c) * ld + sidx(x)];
+        sx[m] = v.x;
+        sy[m] = v.y;
+      }
+      if (lr == 9)
+#pragma unroll
+        for (int m = 0; m < 3; ++m) {
+          const C v = s_in[((6 + m) * yp + c) * ld + sidx(x)];
+          gx[m] = v.x;
+          gy[m] = v.y;
+        }
+#pragma unroll
+      for (int m = 0; m < 3; ++m) {
+        const C v = s_in[((lr + m) * yp + c) * ld + sidx(x)];
+        wx[m] = v.x;
+        wy[m] = v.y;
+      }
+      float f[12];
+      const int ya = y0 + 2 * c;
+      if (ya < ny) {
+        closure_invariants<T>(sx, gx, wx, bz, n2, dsq, nu, f);
+        store_features(a.feat, ((long long)z * ny + ya) * nx + x, f);
+      }
+      if (ya + 1 < ny) {
+        closure_invariants<T>(sy, gy, wy, bz, n2, dsq, nu, f);
+        store_features(a.feat, ((long long)z * ny + ya + 1) * nx + x, f);
+      }
+    }
+    return;
+  }
+
   // ---- subgrid stress: the gradient lines become -2 nu_t S and -kappa_t dT
   if (a.les) {
     const int lu = a.g.lu, lr = a.g.lr;
-    const T cds = (T)a.les_cds[0], prt = (T)a.les_prt_inv;
+    const T cds = a.les == 1 ? (T)a.les_cds[0] : (T)0, prt = (T)a.les_prt_inv;
     for (int e = threadIdx.x; e < yp * nx; e += blockDim.x) {
       const int c = (int)fdiv(e, a.fd_nx), x = e - c * nx;
       C v[9];
@@ -411,8 +541,18 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
           sx[m] = v[m].x;
           sy[m] = v[m].y;
         }
-      sgs_point<T>(sx, lr, cds, prt);
-      sgs_point<T>(sy, lr, cds, prt);
+      if (a.les == 2) {
+        // learned closure: per-point coefficients (rows past Ny are padding)
+        const int ya = min(y0 + 2 * c, ny - 1), yb = min(y0 + 2 * c + 1, ny - 1);
+        const float2 ca = a.les_coef[((long long)z * ny + ya) * nx + x];
+        const float2 cb = a.les_coef[((long long)z * ny + yb) * nx + x];
+        const double dsq = a.les_dsq;
+        sgs_point_c<T>(sx, lr, (T)((double)ca.x * dsq), (T)((double)ca.y * dsq));
+        sgs_point_c<T>(sy, lr, (T)((double)cb.x * dsq), (T)((double)cb.y * dsq));
+      } else {
+        sgs_point<T>(sx, lr, cds, prt);
+        sgs_point<T>(sy, lr, cds, prt);
+      }
 #pragma unroll
       for (int m = 0; m < 9; ++m)
         if (m < lr) s_in[((lu + m) * yp + c) * ld + sidx(x)] = mk<C>(sx[m], sy[m]);

@@ -46,9 +46,20 @@ struct XPassArgs {
   // subgrid stress (les = 1): input fields Lu .. Lu+Lr-1 are the gradient
   // fields of the products; nu_t = C delta^2 |S| with C delta^2 read from
   // les_cds, kappa_t = nu_t * les_prt_inv
+  // les = 2: per-point coefficients les_coef[(z Ny + y) Nx + x] =
+  // (C_nu, C_kappa) of the learned closure, nu_t = C_nu les_dsq |S|,
+  // kappa_t = C_kappa les_dsq |S|
   int les;
   const double* les_cds;
   double les_prt_inv;
+  const float2* les_coef;
+  double les_dsq;
+  // out_mode 4: the closure's 12 invariants of point (z Ny + y) Nx + x as
+  // BF16 [16] (zero padded) from the input fields S (6), dT/dx (3, when
+  // Lr = 9) and w (3); f_bz = buoy_fac_z, f_n2 = N^2, f_dsq = delta^2,
+  // f_nu = viscosity
+  void* feat;
+  double f_bz, f_n2, f_dsq, f_nu;
   long long in_y, in_z, in_n;
   long long out_kx, out_z, out_n;
   long long out_py, out_pz, out_pn;

@@ -169,6 +169,9 @@ struct Ctx {
   double* les_cds = nullptr;   // device C delta^2 in use
   void* les_phys = nullptr;    // physical velocity for dm.f (3 fields, working precision)
   double* les_work = nullptr;  // dm.f work arrays
+  void* les_feat = nullptr;    // learned closure: BF16 invariants [pt][16]
+  float2* les_coef = nullptr;  // and its coefficients [pt]
+  double les_dsq = 0;
   size_t s1_elems = 0, s2_elems = 0;
   // learned closure: FP32 parameters with Adam moments, the BF16 device form
   float *mlp_p = nullptr, *mlp_m = nullptr, *mlp_v = nullptr, *mlp_g = nullptr, *mlp_loss = nullptr;
@@ -282,12 +285,21 @@ template <typename T>
 static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in, const void* in_phys,
                       long long in_y, long long in_z, long long in_n, void* out, void* out_phys, long long out_kx,
                       long long out_z, long long out_n, long long out_py, long long out_pz, long long out_pn,
-                      bool stats, bool les = false) {
+                      bool stats, int les = 0) {
   XPassArgs<T> a{};
   if (les) {
-    a.les = 1;
+    a.les = les;
     a.les_cds = c.les_cds;
     a.les_prt_inv = c.les_prt_inv;
+    a.les_coef = c.les_coef;
+    a.les_dsq = c.les_dsq;
+  }
+  if (out_mode == 4) {
+    a.feat = c.les_feat;
+    a.f_bz = c.cfg.buoy_fac_z;
+    a.f_n2 = c.cfg.buoy_fac_z * c.cfg.lapse;
+    a.f_dsq = c.les_dsq;
+    a.f_nu = c.cfg.vis > 1e-12 ? c.cfg.vis : 1e-12;
   }
   a.g = c.g;
   a.in = (const cx_t<T>*)in;
@@ -383,16 +395,17 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
   // gradient fields the products need
   const bool les = c.les_model != 0;
   const int nin = g.lu + (les ? g.lr : 0);
+  const int ninv = nin + (c.les_model == 3 ? 3 : 0);  // + vorticity for the invariants
   if (ev) cudaEventRecord(ev[0], c.stream);
   // z inverse: U(n, kx, ky, kz) -> A(n, z, kx, ky)
   if (run(0))
-    rc = run_z_inv<T>(c, c.U, c.S1, nin, g.mz, (long long)g.my * g.mz, nzmm, g.my, (long long)g.mx * g.my,
+    rc = run_z_inv<T>(c, c.U, c.S1, ninv, g.mz, (long long)g.my * g.mz, nzmm, g.my, (long long)g.mx * g.my,
                       (long long)g.nz * g.mx * g.my, les ? 1 : 0);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[1], c.stream);
   // y inverse: A -> B(n, z, y, kx)
   if (run(1))
-    rc = run_y_inv<T>(c, c.S1, c.S2, nin, 0, g.my, (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, g.mx,
+    rc = run_y_inv<T>(c, c.S1, c.S2, ninv, 0, g.my, (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, g.mx,
                       (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx);
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[2], c.stream);
@@ -406,11 +419,20 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
     les_dynamic<T>((const T*)c.les_phys, c.les_work, c.les_cds, g.nx, g.ny, g.nz, c.les_dxi, c.les_dyi, c.les_dzi,
                    c.stream);
   }
+  // learned closure: the invariants of every point, then the network
+  if (run(2) && c.les_model == 3) {
+    const long long bn = (long long)g.nz * g.ny * g.mx;
+    rc = run_x_pass<T>(c, 0, 4, g.lr + 3, (const cx_t<T>*)c.S2 + g.lu * bn, nullptr, g.mx, (long long)g.ny * g.mx,
+                       bn, nullptr, nullptr, 0, 0, 0, 0, 0, 0, false);
+    if (rc) return rc;
+    mlp_forward((const __nv_bfloat16*)c.les_feat, (long long)g.nx * g.ny * g.nz, c.mlp_dev, c.les_coef, nullptr,
+                c.mlp_err, c.stream);
+  }
   // x pass: B -> C(m, z, kx, y) with vel_max at nrk = 1
   if (run(2))
     rc = run_x_pass<T>(c, 0, 2, nin, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
                        c.S3, nullptr, g.ny, (long long)g.mx * g.ny, (long long)g.nz * g.mx * g.ny, 0, 0, 0, nrk == 1,
-                       les);
+                       c.les_model == 3 ? 2 : (les ? 1 : 0));
   if (rc) return rc;
   if (ev) cudaEventRecord(ev[3], c.stream);
   // y forward: C -> D(m, kx, ky, z)
@@ -463,6 +485,7 @@ static void free_ctx(Ctx* c) {
   cudaFree(c->S1); cudaFree(c->S2); cudaFree(c->S3);
   cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou);
   cudaFree(c->les_cds); cudaFree(c->les_phys); cudaFree(c->les_work);
+  cudaFree(c->les_feat); cudaFree(c->les_coef);
   cudaFree(c->mlp_p); cudaFree(c->mlp_m); cudaFree(c->mlp_v); cudaFree(c->mlp_g); cudaFree(c->mlp_loss);
   cudaFree(c->mlp_dev); cudaFree(c->mlp_err);
   for (auto& s : c->sc) cudaFree(s.p);
@@ -982,9 +1005,12 @@ int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, doubl
   return sync_stream(c);
 }
 
+static int mlp_ensure(Ctx& c);
+
 int sam_gpu_set_les(int model, double c_smag, double pr_t) {
   NEED_CTX();
-  if (model < 0 || model > 2) return fail(SAM_GPU_EINVAL, "set_les: model %d (0 off, 1 Smagorinsky, 2 dynamic)", model);
+  if (model < 0 || model > 3)
+    return fail(SAM_GPU_EINVAL, "set_les: model %d (0 off, 1 Smagorinsky, 2 dynamic, 3 learned)", model);
   if (!(pr_t > 0.0)) return fail(SAM_GPU_EINVAL, "set_les: turbulent Prandtl number must be > 0");
   if (model == 1 && !(c_smag >= 0.0)) return fail(SAM_GPU_EINVAL, "set_les: c_smag must be >= 0");
   if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
@@ -993,8 +1019,9 @@ int sam_gpu_set_les(int model, double c_smag, double pr_t) {
   const size_t es = csize(c);
   if (model) {
     // pencil buffers for the Lr gradient fields beside the Lu fields
-    const size_t s1 = (size_t)(g.lu + g.lr) * g.mx * g.my * g.nz;
-    const size_t s2 = (size_t)(g.lu + g.lr) * g.nz * g.ny * g.mx;
+    const int nf = g.lu + g.lr + (model == 3 ? 3 : 0);
+    const size_t s1 = (size_t)nf * g.mx * g.my * g.nz;
+    const size_t s2 = (size_t)nf * g.nz * g.ny * g.mx;
     if (c.s1_elems < s1) {
       cudaFree(c.S1); c.S1 = nullptr; c.s1_elems = 0;
       CK(cudaMalloc(&c.S1, es * s1));
@@ -1010,9 +1037,17 @@ int sam_gpu_set_les(int model, double c_smag, double pr_t) {
       CK(cudaMalloc(&c.les_phys, (es / 2) * 3 * (size_t)g.nx * g.ny * g.nz));
       CK(cudaMalloc(&c.les_work, sizeof(double) * les_dynamic_work(g.nx, g.ny, g.nz)));
     }
+    if (model == 3 && !c.les_feat) {
+      const size_t np = (size_t)g.nx * g.ny * g.nz;
+      int rc = mlp_ensure(c);
+      if (rc) return rc;
+      CK(cudaMalloc(&c.les_feat, 32 * np));
+      CK(cudaMalloc(&c.les_coef, sizeof(float2) * np));
+    }
   }
   double dsq;
   grid_spacing(c, c.les_dxi, c.les_dyi, c.les_dzi, dsq);
+  c.les_dsq = dsq;
   c.les_model = model;
   c.les_prt_inv = 1.0 / pr_t;
   if (model) {

@@ -35,3 +35,41 @@ def test_gradient_against_finite_differences():
         lm = CL.grad(pm, x, y, rnd=False)[1]
         fd = (lp - lm) / (2 * h)
         assert abs(fd - g[i]) <= 1e-6 * max(abs(fd), 1e-8) + 1e-12, (i, fd, g[i])
+
+
+def test_invariants_of_simple_flows():
+    """Pure strain, pure rotation and stratification give the invariants
+    their definitions predict."""
+    import oracle as O
+    # axisymmetric strain diag(2, -1, -1): |S|^2 = 2 * 6 = 12, tr(S^3) = 6
+    S = np.array([2.0, 0, -1.0, 0, 0, -1.0])
+    f = O.closure_invariants(S, np.zeros(3), np.zeros(3), dsq=1.0, nu=1.0)
+    assert abs(f[0]) < 1e-7 and abs(f[1] - 6 / 12 ** 1.5) < 1e-6 and abs(f[6] + 1 / 12 ** 0.5) < 1e-6
+    assert abs(f[10] - np.log1p(12 ** 0.5)) < 1e-6 and f[11] == 0
+    # strain plus rotation about z: w = (0, 0, 2), |w|^2/|S|^2 = 4/12
+    f = O.closure_invariants(S, np.zeros(3), np.array([0, 0, 2.0]), dsq=1.0, nu=1.0)
+    assert abs(f[0] - np.log1p(4 / 12)) < 1e-6
+    assert abs(f[2] - (-1 * 4) / (12 ** 0.5 * 4)) < 1e-6 and abs(f[7] - 2 / (12 ** 0.5 + 2)) < 1e-6
+    # stable stratification dT/dz = 0.5 with b = 2, N^2 = 3
+    f = O.closure_invariants(S, np.array([0, 0, 0.5]), np.zeros(3), bz=2.0, n2=3.0, dsq=1.0, nu=1.0)
+    assert abs(f[3] - np.log1p(3 / 12)) < 1e-6 and abs(f[4] - np.arcsinh(1 / 12)) < 1e-6 and f[5] == 0
+    assert abs(f[8] - (-1 * 0.25) / (12 ** 0.5 * 0.25)) < 1e-6
+
+
+def test_zero_network_is_smagorinsky():
+    """With every parameter zero the network returns C = 0.02 ln 2 for both
+    coefficients, so the learned closure (model 3) must reproduce the
+    Smagorinsky closure (model 1) with that constant and Pr_t = 1 exactly."""
+    import oracle as O
+    c0 = float(np.float32(0.02) * np.float32(np.log1p(np.float32(1.0))))
+    cfg = dict(nx=16, ny=16, nz=24, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=1e-4, dt0=0.01)
+    us = []
+    for model in (1, 3):
+        o = O.Oracle(**cfg)
+        u = o.init_random(4, 0, 1.0, 0, 0.1)
+        o.mlp_set(np.zeros(CL.N_PARAMS, np.float32))
+        o.set_les(model, c_smag=c0, pr_t=1.0)
+        r = o.wave(o.d.lr)
+        o.steps(u, r, 2)
+        us.append(u)
+    assert np.array_equal(us[0], us[1])

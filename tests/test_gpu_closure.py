@@ -85,3 +85,59 @@ def test_adam_training_fits_a_smooth_target(gpu_lib, ctx):
     # the trained parameters reproduce the GPU forward pass in the oracle
     p = ctx.mlp_get()
     assert np.abs(CL.forward(p, xt)[0] - ctx.mlp_forward(xt)).max() <= 2e-3 * 0.03
+
+
+def _relerr(a, b):
+    return np.abs(a - b).max() / max(np.abs(b).max(), 1e-300)
+
+
+CFG3 = dict(nx=24, ny=16, nz=32, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=1e-4, i_cfl=1, cfl0=0.5)
+
+
+def test_zero_network_step_is_smagorinsky(gpu_lib):
+    """All-zero parameters give C = 0.02 ln 2 everywhere: the learned-closure
+    step must equal the Smagorinsky step with that constant bit for bit."""
+    import oracle as O
+    c0 = float(np.float32(0.02) * np.float32(np.log1p(np.float32(1.0))))
+    o = O.Oracle(**CFG3)
+    u0 = o.init_random(7, 0, 1.0, 0, 0.1)
+    out = []
+    for model in (1, 3):
+        g = SamGpu(**CFG3)
+        g.upload(u0)
+        g.mlp_set(np.zeros(CL.N_PARAMS, np.float32))
+        g.set_les(model, c_smag=c0, pr_t=1.0)
+        g.step(3)
+        out.append(g.download())
+        g.close()
+    assert np.array_equal(out[0], out[1])
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 5e-6), (32, 3e-5)])
+def test_learned_closure_step_matches_oracle(gpu_lib, precision, tol):
+    """A non-trivial network inside the step: invariants on the GPU, the
+    tcgen05 network, per-point nu_t and kappa_t, against the oracle (FP64
+    features and network with the same BF16 roundings).  The network's FP32
+    accumulation order differs from the oracle's, and an invariant that sits
+    at a BF16 rounding tie may round the other way (a 2^-8 change of one
+    input at one point), which bounds the FP64 case at a few 1e-6 instead of
+    round-off."""
+    import oracle as O
+    rng = np.random.default_rng(11)
+    p = CL.init_params(6)
+    p[CL.OFF_W3:CL.OFF_B3] *= 10
+    p[CL.OFF_B3:] = rng.standard_normal(2).astype(np.float32)
+    o = O.Oracle(**CFG3)
+    u = o.init_random(7, 0, 1.0, 0, 0.1)
+    g = SamGpu(precision=precision, **CFG3)
+    g.upload(u)
+    g.mlp_set(p)
+    g.set_les(3, pr_t=1.0)
+    o.mlp_set(p)
+    o.set_les(3, pr_t=1.0)
+    r = o.wave(o.d.lr)
+    o.steps(u, r, 3)
+    g.step(3)
+    ug = g.download()
+    for n in range(o.d.lu):
+        assert _relerr(ug[..., n], u[..., n]) <= tol, n

@@ -155,4 +155,4 @@ def test_closure_off_restores_reference_products(gpu_lib):
     g2.step(2)
     assert np.array_equal(g.download(), g2.download())
     with pytest.raises(Exception, match="EINVAL"):
-        g.set_les(3)
+        g.set_les(4)
