@@ -14,6 +14,14 @@ step).  Synthetic seeded input, generated on the device.
           uploads u from pinned host memory, runs the step, downloads u.
   fp32  : the FP32-bulk form (FP64 reductions) on the same workload, with its
           relative error against the FP64 run after the timed steps.
+  les   : LES of stratified forced turbulence at 256^3 (N = 1, OU forcing of
+          |k| <= 2.5): the FP64 drop-in with dm.f's dynamic Smagorinsky
+          coupled in against the FP32 bulk form with the learned closure
+          (tcgen05 network), steps/s of each, their ratio, and the spectrum
+          difference for k <= k_max/2 after the timed steps.
+  ensemble: 96 independent members of uneven sizes in one graph per step
+          (aggregate member-steps/s) against the members run one by one in
+          the plain FP64 drop-in.
 
 `--impl reference` times the reference algorithm on the host cores instead
 (the oracle, a C restatement of the Fortran path; the Fortran reference itself
@@ -40,7 +48,8 @@ sys.path.insert(0, ROOT)
 N = 256
 WORKLOAD = ("gravity-wave packet 256^3 stratified Boussinesq, N=2, nu=kappa=1e-4, k0=(8,0,16), "
             "width pi/4, amplitude 0.05, 1% noise, RK3 CFL 0.5")
-METRIC = "RK3 steps/s at 256^3 (FP64 drop-in; FP32 bulk reported beside it)"
+METRIC = ("RK3 steps/s at 256^3 (FP64 drop-in; FP32 bulk, FP64 + dm.f LES and FP32 + learned-closure LES "
+          "reported beside it)")
 
 
 def workload_cfg(n=None, precision=64):
@@ -179,6 +188,126 @@ def cpu_oracle_rate(n, steps, threads, warm_stages=1):
     return steps / dt, dt
 
 
+def closure_params():
+    """The trained closure network (sam_gb300/data/closure_mlp.npz, made by
+    python -m sam_gb300.closure_data on the GPU) or, without it, the
+    untrained initial network (the timing does not depend on the weights)."""
+    import numpy as np
+    from sam_gb300 import closure_data as CD
+    try:
+        z = np.load(CD.WEIGHTS)
+        return z["params"], "trained (" + os.path.relpath(CD.WEIGHTS, ROOT) + ")"
+    except (OSError, KeyError):
+        return CD.init_params(0), "untrained initial weights"
+
+
+def les_forms(stream, u_init, K, W):
+    """Steps/s of the FP64 drop-in with dm.f's dynamic closure and of the
+    FP32 bulk form with the learned closure on the same workload and start
+    state (CUDA events on the launching stream), and how far the FP32 +
+    learned spectrum is from the FP64 + dm.f spectrum after the timed steps
+    (shells k <= k_max/2)."""
+    import numpy as np
+    import torch
+    from sam_gb300 import SamGpu
+    params, src = closure_params()
+    out = {}
+    spectra = {}
+    for name, prec, model in (("fp64_dm", 64, 2), ("fp32_learned", 32, 3)):
+        g = SamGpu(**workload_cfg(precision=prec))
+        g.set_stream(stream.cuda_stream)
+        g.upload(u_init)
+        if model == 3:
+            g.mlp_set(params)
+        g.set_les(model)
+        g.step(W)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            g.step(K)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        spectra[name] = g.spectra()["ek"]
+        passes = [g.profile_stage(nrk, 2) for nrk in (1, 2, 3)]
+        out[name] = {"value": K / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / K,
+                     "c_delta_sq_final": g.les_coef() if model == 2 else None,
+                     "passes_ms": {k: sum(p[k] for p in passes) / 3 for k in passes[0]}}
+        g.close()
+    kmax = int((N - 0.1) / 3)
+    ks = np.arange(1, kmax // 2 + 1)
+    out["speedup_fp32_learned_over_fp64_dm"] = out["fp32_learned"]["value"] / out["fp64_dm"]["value"]
+    out["spectrum_max_rel_diff_k_le_kmax_half"] = float(
+        np.abs(spectra["fp32_learned"][ks] / spectra["fp64_dm"][ks] - 1).max())
+    out["after_steps"] = W + K
+    out["network"] = src
+    return out
+
+
+def ensemble_members(seed=5):
+    """96 stratified-turbulence members of uneven sizes: 32 at 32^3, 32 at
+    64^3, 24 at 96^3, 8 at 128^3; per member a seed, N uniform in [0.5, 4]
+    (buoy_fac_z = N^2, lapse = 1), and the viscosity of a Taylor-microscale
+    Reynolds number uniform in [50, 150] for the k^4 exp(-2 (k/4)^2) start
+    field at rms velocity 1 (u' = 1, lambda = (5 E / Z)^(1/2) = 1/2, so
+    nu = 0.5 / Re_lambda); FP32 bulk, CFL 0.5; the learned closure on the
+    members of 96^3 and more."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for n, count in ((32, 32), (64, 32), (96, 24), (128, 8)):
+        for _ in range(count):
+            nn = rng.uniform(0.5, 4.0)
+            re = rng.uniform(50.0, 150.0)
+            out.append((dict(nx=n, ny=n, nz=n, i_strat=1, i_cfl=1, cfl0=0.5, vis=0.5 / re, pr=1.0, dt0=1e-3,
+                             buoy_fac_z=nn * nn, lapse=1.0), int(rng.integers(1 << 30)), n >= 96))
+    return out
+
+
+def ensemble_form(K, W):
+    """Aggregate member-steps/s of the 96-member ensemble (one graph per step
+    over all members) against the same members run one after another in the
+    plain FP64 drop-in."""
+    import torch
+    from sam_gb300 import SamEnsemble, SamGpu
+    params, src = closure_params()
+    members = ensemble_members()
+    ens = SamEnsemble([dict(cfg, precision=32) for cfg, _, _ in members])
+    try:
+        for m, (cfg, seed, learned) in enumerate(members):
+            ens[m].init_random(seed, 6, 1.0, 6, 0.1)
+            if learned:
+                ens[m].mlp_set(params)
+                ens[m].set_les(3)
+        ens.step(W)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        ens.step(K)
+        t_ens = time.perf_counter() - t0
+    finally:
+        ens.close()
+    # the sequential FP64 plain baseline: each member alone, graph-replayed
+    Ks = max(2, K // 4)
+    t_seq = 0.0
+    for cfg, seed, _ in members:
+        g = SamGpu(**cfg)
+        g.init_random(seed, 6, 1.0, 6, 0.1)
+        g.step(1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        g.step(Ks)
+        torch.cuda.synchronize()
+        t_seq += (time.perf_counter() - t0) / Ks
+        g.close()
+    agg = len(members) * K / t_ens
+    seq = len(members) / t_seq
+    return {"members": len(members), "sizes": {"32^3": 32, "64^3": 32, "96^3": 24, "128^3": 8},
+            "value": agg, "unit": "member-steps/s", "precision": "FP32 bulk, learned closure on >= 96^3 (" + src + ")",
+            "sequential_fp64_plain": {"value": seq, "unit": "member-steps/s"}, "speedup": agg / seq,
+            "timing": "host clock around ensemble_step (it synchronises), after warm-up steps"}
+
+
 def run_reference(args):
     rank, _, ws = dist_env()
     if rank != 0:
@@ -207,6 +336,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-les", action="store_true")
+    ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="N of the N^3 box (profiling of smaller cases)")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
                     help="precision of the timed run (32 for profiling the FP32 bulk form)")
@@ -328,6 +459,15 @@ def main():
                 "rel_err_vs_fp64_per_field": err, "after_steps": W + K,
                 "hbm_gbs": b32 / (ms32 / K / 1e3) / 1e9, "passes_ms": passes32, "tiles": tiles32}
 
+    # ---- the LES forms of the same workload: FP64 drop-in with dm.f's
+    # dynamic Smagorinsky coupled in, and FP32 bulk with the learned closure
+    les = None
+    if not args.no_les:
+        les = les_forms(stream, u_init, K, W)
+    ens = None
+    if not args.no_ensemble:
+        ens = ensemble_form(max(4, K // 2), W)
+
     # ---- CPU baseline: the oracle on the host cores, bounded sample
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -364,7 +504,7 @@ def main():
                        "hbm_gbs_step": algorithmic_bytes_per_step() / (ms_step / 1e3) / 1e9,
                        "dt_final": st["dt"], "tiles": tiles},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * K,
-            "clocks": clk.summary(), "fp32_bulk": fp32}
+            "clocks": clk.summary(), "fp32_bulk": fp32, "les": les, "ensemble": ens}
     print(json.dumps(line), flush=True)
     return 0
 

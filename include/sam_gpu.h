@@ -261,9 +261,36 @@ int sam_gpu_mlp_grad(const float* features, const float* target, long long n, fl
  * shuffles); loss_hist (may be NULL) receives each minibatch's loss. */
 int sam_gpu_mlp_train(const float* features, const float* target, long long n, int steps, int batch, float lr,
                       float* loss_hist);
+/* Training data of the closure.  sam_gpu_box_filter: the resident field
+ * in physical space, box-filtered and downsampled by f (Nx, Ny, Nz divisible
+ * by f): out(Nx/f, Ny/f, Nz/f, Lu+Lr) holds the block means of u, v, w, [T],
+ * then of the products u_a u_b (rhs.f:49-54 order) and [u_a T].
+ * sam_gpu_closure_inputs: the invariants the learned closure sees for the
+ * resident field, feat[(z Ny + y) Nx + x][16] as BF16 bit patterns (12
+ * used), and grads(Nx, Ny, Nz, Lr+3) the physical S (6, product order),
+ * [dT/dx_a (3)] and vorticity (3) they are formed from; either may be NULL. */
+int sam_gpu_box_filter(int f, double* out);
+int sam_gpu_closure_inputs(unsigned short* feat, double* grads);
 /* Known-answer test of the tensor-core path: d(128 x 64) = a(128 x 16)
  * b(64 x 16)^T with a, b rounded to BF16 and FP32 accumulation. */
 int sam_gpu_mma_selftest(const float* a, const float* b, float* d);
+
+/* ---- ensembles of independent runs (no reference counterpart) ----
+ * sam_gpu_ensemble_create builds n contexts at once (any mix of grid sizes,
+ * precisions and settings; each its own device buffers and stream) and
+ * selects member 0.  While an ensemble exists, every other entry point acts
+ * on the selected member (sam_gpu_ensemble_select), so members are set up
+ * with the usual calls (init_*, upload, set_les, mlp_set, set_forcing,
+ * autotune) and read back with download / get_stats / spectra.
+ * sam_gpu_ensemble_step advances every member nsteps steps from one CUDA
+ * graph per step in which each member's passes form their own branch, so
+ * the small members' kernels run concurrently; it returns after the last
+ * step completes.  sam_gpu_init, sam_gpu_finalize and
+ * sam_gpu_ensemble_destroy end the ensemble. */
+int sam_gpu_ensemble_create(const sam_gpu_config* cfgs, int n);
+int sam_gpu_ensemble_select(int m);
+int sam_gpu_ensemble_step(int nsteps);
+int sam_gpu_ensemble_destroy(void);
 
 /* ---- restart files of the resident state ---- */
 /* write_field.f:1 / read_field.f:1  vel.NNNNNN: Lu*Nx_min records of

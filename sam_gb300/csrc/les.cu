@@ -368,6 +368,57 @@ template void les_dynamic<double>(const double*, double*, double*, int, int, int
 template void les_dynamic<float>(const float*, double*, double*, int, int, int, double, double, double,
                                  cudaStream_t);
 
+// ---- training data of the learned closure: box filter and downsample by f
+// of the physical fields P(n, z, y, x) (Lu fields): block means of u_a,
+// T, the velocity products u_a u_b (rhs.f's order) and u_a T, written as
+// out(X, Y, Z, m) with X = Nx/f fastest, m = 0..Lu+Lr-1.
+template <typename T>
+__global__ void k_box_filter(const T* __restrict__ ph, int lu, int nx, int ny, int nz, int f, double* __restrict__ out) {
+  const int cx = nx / f, cy = ny / f, cz = nz / f;
+  const long long nc = (long long)cx * cy * cz, np = (long long)nx * ny * nz;
+  const int lr = lu == 4 ? 9 : 6;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < nc; e += (long long)gridDim.x * blockDim.x) {
+    const int X = (int)(e % cx), Y = (int)((e / cx) % cy), Z = (int)(e / ((long long)cx * cy));
+    double acc[13];
+#pragma unroll
+    for (int m = 0; m < 13; ++m) acc[m] = 0.0;
+    for (int k = 0; k < f; ++k)
+      for (int j = 0; j < f; ++j)
+        for (int i = 0; i < f; ++i) {
+          const long long p = ((long long)(Z * f + k) * ny + (Y * f + j)) * nx + (X * f + i);
+          const double u = ph[p], v = ph[np + p], w = ph[2 * np + p];
+          const double t = lu == 4 ? (double)ph[3 * np + p] : 0.0;
+          acc[0] += u; acc[1] += v; acc[2] += w; acc[3] += t;
+          acc[4] += u * u; acc[5] += u * v; acc[6] += v * v; acc[7] += u * w; acc[8] += v * w; acc[9] += w * w;
+          acc[10] += u * t; acc[11] += v * t; acc[12] += w * t;
+        }
+    const double inv = 1.0 / ((double)f * f * f);
+    int m = 0;
+    for (int q = 0; q < lu; ++q) out[(long long)(m++) * nc + e] = acc[q] * inv;
+    for (int q = 0; q < lr; ++q) out[(long long)(m++) * nc + e] = acc[4 + q] * inv;
+  }
+}
+
+template <typename T>
+__global__ void k_to_double(const T* __restrict__ a, double* __restrict__ b, long long n) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x)
+    b[e] = (double)a[e];
+}
+
+template <typename T>
+void les_box_filter(const T* ph, int lu, int nx, int ny, int nz, int f, double* out, cudaStream_t s) {
+  const long long nc = (long long)(nx / f) * (ny / f) * (nz / f);
+  k_box_filter<T><<<grid_of(nc), kThreads, 0, s>>>(ph, lu, nx, ny, nz, f, out);
+}
+template <typename T>
+void les_to_double(const T* a, double* b, long long n, cudaStream_t s) {
+  k_to_double<T><<<grid_of(n), kThreads, 0, s>>>(a, b, n);
+}
+template void les_box_filter<double>(const double*, int, int, int, int, int, double*, cudaStream_t);
+template void les_box_filter<float>(const float*, int, int, int, int, int, double*, cudaStream_t);
+template void les_to_double<double>(const double*, double*, long long, cudaStream_t);
+template void les_to_double<float>(const float*, double*, long long, cudaStream_t);
+
 void les_get_mean(double2* col, int mz, int kz, int nz, int i_remove, const FftPlan* dplan, const double2* tw,
                   const FftPlan& hplan, double* u_mean, double* jump, cudaStream_t s) {
   const int ld = line_stride(nz);

@@ -18,6 +18,11 @@ size_t les_dynamic_work(int nx, int ny, int nz);
 template <typename T>
 void les_dynamic(const T* phys, double* work, double* cds, int nx, int ny, int nz, double dxi, double dyi,
                  double dzi, cudaStream_t s);
+// box filter and downsample by f (training data of the learned closure)
+template <typename T>
+void les_box_filter(const T* ph, int lu, int nx, int ny, int nz, int f, double* out, cudaStream_t s);
+template <typename T>
+void les_to_double(const T* a, double* b, long long n, cudaStream_t s);
 void les_get_mean(double2* col, int mz, int kz, int nz, int i_remove, const FftPlan* dplan, const double2* tw,
                   const FftPlan& hplan, double* u_mean, double* jump, cudaStream_t s);
 }  // namespace samgpu

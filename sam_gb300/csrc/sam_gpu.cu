@@ -185,6 +185,16 @@ struct Ctx {
 
 static Ctx* g_ctx = nullptr;
 
+// Ensemble of independent contexts (sam_gpu_ensemble_*): g_ctx points at the
+// selected member; the step graph runs every member on its own stream.
+struct Ensemble {
+  std::vector<Ctx*> members;
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  std::vector<cudaEvent_t> events;
+};
+static Ensemble* g_ens = nullptr;
+
 static void grid_spacing(const Ctx& c, double& dxi, double& dyi, double& dzi, double& delta_sq) {
   const double dx = c.cfg.xl / c.g.nx, dy = c.cfg.yl / c.g.ny, dz = c.cfg.zl / c.g.nz;
   dxi = 1.0 / dx; dyi = 1.0 / dy; dzi = 1.0 / dz;
@@ -588,9 +598,17 @@ extern "C" {
 
 const char* sam_gpu_error_string(void) { return g_err; }
 
+static int init_ctx(const sam_gpu_config* cfg);
+static void ensemble_free();
+
 int sam_gpu_init(const sam_gpu_config* cfg) {
-  if (!cfg) return fail(SAM_GPU_EINVAL, "null config");
+  if (g_ens) ensemble_free();
   if (g_ctx) { free_ctx(g_ctx); g_ctx = nullptr; }
+  return init_ctx(cfg);
+}
+
+static int init_ctx(const sam_gpu_config* cfg) {
+  if (!cfg) return fail(SAM_GPU_EINVAL, "null config");
   if (cfg->nx < 2 || cfg->nx % 2 || cfg->ny < 1 || cfg->nz < 1)
     return fail(SAM_GPU_EINVAL, "grid %d x %d x %d: Nx must be even and >= 2", cfg->nx, cfg->ny, cfg->nz);
   if (cfg->precision != 64 && cfg->precision != 32) return fail(SAM_GPU_EINVAL, "precision must be 64 or 32");
@@ -681,7 +699,105 @@ int sam_gpu_init(const sam_gpu_config* cfg) {
 }
 
 int sam_gpu_finalize(void) {
+  if (g_ens) {
+    ensemble_free();
+    return 0;
+  }
   if (g_ctx) { cudaStreamSynchronize(g_ctx->stream); free_ctx(g_ctx); g_ctx = nullptr; }
+  return 0;
+}
+
+// ------------------------------------------------------------------ ensemble
+static void ensemble_free() {
+  if (!g_ens) return;
+  for (Ctx* m : g_ens->members) {
+    cudaStreamSynchronize(m->stream);
+    free_ctx(m);
+  }
+  if (g_ens->gexec) cudaGraphExecDestroy(g_ens->gexec);
+  for (cudaEvent_t e : g_ens->events) cudaEventDestroy(e);
+  if (g_ens->stream) cudaStreamDestroy(g_ens->stream);
+  delete g_ens;
+  g_ens = nullptr;
+  g_ctx = nullptr;
+}
+
+int sam_gpu_ensemble_create(const sam_gpu_config* cfgs, int n) {
+  if (!cfgs || n < 1) return fail(SAM_GPU_EINVAL, "ensemble_create: need at least one configuration");
+  if (g_ens) ensemble_free();
+  if (g_ctx) { free_ctx(g_ctx); g_ctx = nullptr; }
+  g_ens = new Ensemble();
+  for (int m = 0; m < n; ++m) {
+    g_ctx = nullptr;
+    const int rc = init_ctx(&cfgs[m]);
+    if (rc) {
+      ensemble_free();
+      return rc;
+    }
+    g_ens->members.push_back(g_ctx);
+  }
+  g_ctx = g_ens->members[0];
+  CK(cudaStreamCreateWithFlags(&g_ens->stream, cudaStreamNonBlocking));
+  g_ens->events.resize((size_t)n + 1);
+  for (auto& e : g_ens->events) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  return 0;
+}
+
+int sam_gpu_ensemble_select(int m) {
+  if (!g_ens) return fail(SAM_GPU_ENOTINIT, "no ensemble (sam_gpu_ensemble_create)");
+  if (m < 0 || m >= (int)g_ens->members.size()) return fail(SAM_GPU_EINVAL, "ensemble member %d out of range", m);
+  g_ctx = g_ens->members[(size_t)m];
+  return 0;
+}
+
+static int enqueue_step(Ctx& c) {
+  int rc = 0;
+  for (int nrk = 1; nrk <= c.cfg.nrk_max && !rc; ++nrk) rc = stage_any(c, nrk);
+  if (!rc && c.ou) {
+    if (c.cfg.precision == 32) ou_apply<float>((float2*)c.U, c.g, c.ou, c.state, c.stream);
+    else ou_apply<double>((double2*)c.U, c.g, c.ou, c.state, c.stream);
+  }
+  return rc;
+}
+
+int sam_gpu_ensemble_step(int nsteps) {
+  if (!g_ens) return fail(SAM_GPU_ENOTINIT, "no ensemble (sam_gpu_ensemble_create)");
+  if (nsteps < 0) return fail(SAM_GPU_EINVAL, "negative step count");
+  Ensemble& E = *g_ens;
+  // a member's settings (closure, forcing) may have changed since the graph
+  // was captured: rebuild it whenever any member's own graph was dropped
+  bool stale = !E.gexec;
+  for (Ctx* m : E.members) stale = stale || m->graph_stale;
+  if (stale) {
+    if (E.gexec) { cudaGraphExecDestroy(E.gexec); E.gexec = nullptr; }
+    for (Ctx* m : E.members) CK(cudaStreamSynchronize(m->stream));
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
+    CK(cudaEventRecord(E.events.back(), E.stream));
+    int rc = 0;
+    for (size_t i = 0; i < E.members.size() && !rc; ++i) {
+      Ctx& m = *E.members[i];
+      cudaStreamWaitEvent(m.stream, E.events.back(), 0);
+      rc = enqueue_step(m);
+      cudaEventRecord(E.events[i], m.stream);
+      cudaStreamWaitEvent(E.stream, E.events[i], 0);
+    }
+    cudaError_t e = cudaStreamEndCapture(E.stream, &graph);
+    if (rc) return rc;
+    if (e != cudaSuccess) return fail(SAM_GPU_ECUDA, "ensemble graph capture: %s", cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&E.gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess) return fail(SAM_GPU_ECUDA, "ensemble graph instantiate: %s", cudaGetErrorString(e));
+    for (Ctx* m : E.members) m->graph_stale = 0;
+  }
+  for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(E.gexec, E.stream));
+  for (Ctx* m : E.members) m->nrk = m->cfg.nrk_max;
+  CK(cudaStreamSynchronize(E.stream));
+  return check_launch();
+}
+
+int sam_gpu_ensemble_destroy(void) {
+  ensemble_free();
   return 0;
 }
 
@@ -696,6 +812,7 @@ int sam_gpu_dims(int* o) {
 int sam_gpu_set_stream(void* s) {
   NEED_CTX();
   c.stream = s ? (cudaStream_t)s : c.own;
+  c.graph_stale = 1;
   return 0;
 }
 
@@ -984,6 +1101,7 @@ int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, doubl
   NEED_CTX();
   if (n_modes) *n_modes = 0;
   if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+  c.graph_stale = 1;
   if (k_f <= 0.0 || sigma == 0.0) {
     cudaFree(c.ou);
     c.ou = nullptr;
@@ -1014,6 +1132,7 @@ int sam_gpu_set_les(int model, double c_smag, double pr_t) {
   if (!(pr_t > 0.0)) return fail(SAM_GPU_EINVAL, "set_les: turbulent Prandtl number must be > 0");
   if (model == 1 && !(c_smag >= 0.0)) return fail(SAM_GPU_EINVAL, "set_les: c_smag must be >= 0");
   if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+  c.graph_stale = 1;
   CK(cudaStreamSynchronize(c.stream));
   const Grid& g = c.g;
   const size_t es = csize(c);
@@ -1222,6 +1341,94 @@ int sam_gpu_mlp_train(const float* feat, const float* target, long long n, int s
   return rc;
 }
 
+}  // extern "C"
+
+// The resident state's physical fields (Lu) into sc[0] (working precision).
+template <typename T>
+static int physical_fields(Ctx& c) {
+  const Grid& g = c.g;
+  const size_t nm = (size_t)g.mx * g.my * g.mz, vol = (size_t)g.nx * g.ny * g.nz;
+  const size_t es = sizeof(cx_t<T>);
+  int rc;
+  if ((rc = ensure(c.sc[0], vol * g.lu * sizeof(T))) || (rc = ensure(c.sc[1], es * g.lu * g.nz * g.mx * g.my)) ||
+      (rc = ensure(c.sc[2], es * g.lu * g.nz * g.ny * g.mx)))
+    return rc;
+  if ((rc = run_z_inv<T>(c, c.U, c.sc[1].p, g.lu, g.mz, (long long)g.my * g.mz, (long long)nm, g.my,
+                         (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my)))
+    return rc;
+  if ((rc = run_y_inv<T>(c, c.sc[1].p, c.sc[2].p, g.lu, 0, g.my, (long long)g.mx * g.my,
+                         (long long)g.nz * g.mx * g.my, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx)))
+    return rc;
+  return run_x_pass<T>(c, 0, 0, g.lu, c.sc[2].p, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
+                       nullptr, c.sc[0].p, 0, 0, 0, g.nx, (long long)g.nx * g.ny, (long long)vol, false);
+}
+
+template <typename T>
+static int box_filter_impl(Ctx& c, int f, double* out) {
+  const Grid& g = c.g;
+  int rc = physical_fields<T>(c);
+  if (rc) return rc;
+  const size_t nc = (size_t)(g.nx / f) * (g.ny / f) * (g.nz / f), nfo = (size_t)(g.lu + g.lr);
+  if ((rc = ensure(c.sc[3], nc * nfo * 8))) return rc;
+  les_box_filter<T>((const T*)c.sc[0].p, g.lu, g.nx, g.ny, g.nz, f, (double*)c.sc[3].p, c.stream);
+  CK(cudaMemcpyAsync(out, c.sc[3].p, nc * nfo * 8, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+extern "C" {
+
+int sam_gpu_box_filter(int f, double* out) {
+  NEED_CTX();
+  const Grid& g = c.g;
+  if (!out || f < 1 || g.nx % f || g.ny % f || g.nz % f)
+    return fail(SAM_GPU_EINVAL, "box_filter: the grid must divide into blocks of %d", f);
+  return c.cfg.precision == 32 ? box_filter_impl<float>(c, f, out) : box_filter_impl<double>(c, f, out);
+}
+
+}  // extern "C"
+
+template <typename T>
+static int closure_inputs_impl(Ctx& c, unsigned short* feat, double* grads) {
+  const Grid& g = c.g;
+  const int nf = g.lu + g.lr + 3, ng = g.lr + 3;
+  const size_t nm = (size_t)g.mx * g.my * g.mz, vol = (size_t)g.nx * g.ny * g.nz;
+  const size_t es = sizeof(cx_t<T>);
+  const long long bn = (long long)g.nz * g.ny * g.mx;
+  int rc;
+  if ((rc = ensure(c.sc[0], vol * ng * sizeof(T))) || (rc = ensure(c.sc[1], es * nf * g.nz * g.mx * g.my)) ||
+      (rc = ensure(c.sc[2], es * nf * g.nz * g.ny * g.mx)) || (rc = ensure(c.sc[3], vol * ng * 8)))
+    return rc;
+  if (!c.les_feat) CK(cudaMalloc(&c.les_feat, 32 * vol));
+  if ((rc = run_z_inv<T>(c, c.U, c.sc[1].p, nf, g.mz, (long long)g.my * g.mz, (long long)nm, g.my,
+                         (long long)g.mx * g.my, (long long)g.nz * g.mx * g.my, 1)))
+    return rc;
+  if ((rc = run_y_inv<T>(c, c.sc[1].p, c.sc[2].p, nf, 0, g.my, (long long)g.mx * g.my,
+                         (long long)g.nz * g.mx * g.my, g.mx, (long long)g.ny * g.mx, bn)))
+    return rc;
+  const cx_t<T>* gin = (const cx_t<T>*)c.sc[2].p + g.lu * bn;
+  if ((rc = run_x_pass<T>(c, 0, 0, ng, gin, nullptr, g.mx, (long long)g.ny * g.mx, bn, nullptr, c.sc[0].p, 0, 0, 0,
+                          g.nx, (long long)g.nx * g.ny, (long long)vol, false)))
+    return rc;
+  if ((rc = run_x_pass<T>(c, 0, 4, ng, gin, nullptr, g.mx, (long long)g.ny * g.mx, bn, nullptr, nullptr, 0, 0, 0, 0,
+                          0, 0, false)))
+    return rc;
+  les_to_double<T>((const T*)c.sc[0].p, (double*)c.sc[3].p, (long long)(vol * ng), c.stream);
+  if (grads) CK(cudaMemcpyAsync(grads, c.sc[3].p, vol * ng * 8, cudaMemcpyDeviceToHost, c.stream));
+  if (feat) CK(cudaMemcpyAsync(feat, c.les_feat, 32 * vol, cudaMemcpyDeviceToHost, c.stream));
+  return sync_stream(c);
+}
+
+extern "C" {
+
+int sam_gpu_closure_inputs(unsigned short* feat, double* grads) {
+  NEED_CTX();
+  double dsq, dxi, dyi, dzi;
+  grid_spacing(c, dxi, dyi, dzi, dsq);
+  c.les_dsq = dsq;
+  return c.cfg.precision == 32 ? closure_inputs_impl<float>(c, feat, grads)
+                               : closure_inputs_impl<double>(c, feat, grads);
+}
+
 int sam_gpu_mma_selftest(const float* a, const float* b, float* d) {
   NEED_CTX();
   if (!a || !b || !d) return fail(SAM_GPU_EINVAL, "mma_selftest: null array");
@@ -1301,7 +1508,8 @@ int sam_gpu_autotune(int reps) {
   CK(cudaStreamSynchronize(c.stream));
   cudaFree(su);
   cudaFree(sr);
-  if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }  // recapture with the new tiles
+  if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+  c.graph_stale = 1;  // recapture with the new tiles
   return check_launch();
 }
 

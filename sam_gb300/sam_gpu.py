@@ -32,7 +32,8 @@ EXPORTS = [
     "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_planes",
     "sam_gpu_set_forcing", "sam_gpu_set_les", "sam_gpu_les_coef",
     "sam_gpu_mlp_set", "sam_gpu_mlp_get", "sam_gpu_mlp_forward", "sam_gpu_mlp_grad", "sam_gpu_mlp_train",
-    "sam_gpu_mma_selftest",
+    "sam_gpu_mma_selftest", "sam_gpu_box_filter", "sam_gpu_closure_inputs",
+    "sam_gpu_ensemble_create", "sam_gpu_ensemble_select", "sam_gpu_ensemble_step", "sam_gpu_ensemble_destroy",
 ]
 
 MLP_PARAMS = 5122
@@ -121,6 +122,11 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_mlp_grad.argtypes = [P, P, C.c_longlong, P, P]
     lib.sam_gpu_mlp_train.argtypes = [P, P, C.c_longlong, C.c_int, C.c_int, C.c_float, P]
     lib.sam_gpu_mma_selftest.argtypes = [P, P, P]
+    lib.sam_gpu_box_filter.argtypes = [C.c_int, P]
+    lib.sam_gpu_ensemble_create.argtypes = [P, C.c_int]
+    lib.sam_gpu_ensemble_select.argtypes = [C.c_int]
+    lib.sam_gpu_ensemble_step.argtypes = [C.c_int]
+    lib.sam_gpu_closure_inputs.argtypes = [P, P]
     lib.sam_gpu_les_coef.argtypes = [C.POINTER(C.c_double)]
     lib.sam_gpu_planes.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
     lib.sam_gpu_force.argtypes = [P, C.c_int]
@@ -400,6 +406,24 @@ class SamGpu:
                     "mlp_train")
         return hist[:steps]
 
+    def box_filter(self, f):
+        """Block means over f^3 cells of u, [T], u_a u_b, [u_a T]: (X, Y, Z, Lu+Lr)."""
+        n = self.cfg
+        out = np.zeros((n.nx // f, n.ny // f, n.nz // f, self.lu + self.lr), order="F")
+        self._check(load_library().sam_gpu_box_filter(f, _p(out)), "box_filter")
+        return out
+
+    def closure_inputs(self):
+        """(features [Nx*Ny*Nz][12] float32 (BF16 values), grads (Nx,Ny,Nz,Lr+3))."""
+        n = self.cfg
+        npt = n.nx * n.ny * n.nz
+        raw = np.zeros((npt, 16), dtype=np.uint16)
+        grads = np.zeros((n.nx, n.ny, n.nz, self.lr + 3), order="F")
+        self._check(load_library().sam_gpu_closure_inputs(raw.ctypes.data_as(C.c_void_p), _p(grads)),
+                    "closure_inputs")
+        feat = (raw[:, :12].astype(np.uint32) << 16).view(np.float32)
+        return feat, grads
+
     def mma_selftest(self, a, b):
         a = self._f32(a, (128, 16))
         b = self._f32(b, (64, 16))
@@ -463,3 +487,77 @@ class SamGpu:
     def init_packet(self, seed, k0=(8, 0, 16), sigma=np.pi / 4, amplitude=0.05, noise=0.01):
         self._check(load_library().sam_gpu_init_packet(seed, k0[0], k0[1], k0[2], sigma, amplitude, noise),
                     "init_packet")
+
+
+class _Member(SamGpu):
+    """One member of a SamEnsemble: every SamGpu method, acting on the
+    member (selected before each call through __getattribute__)."""
+
+    def __init__(self, ens, index, cfg):
+        self._ens, self._index, self.cfg = ens, index, cfg
+        load_library().sam_gpu_ensemble_select(index)
+        d = np.zeros(11, dtype=np.int32)
+        self._check(load_library().sam_gpu_dims(d.ctypes.data_as(C.c_void_p)), "sam_gpu_dims")
+        (self.nx_min, self.ny_min, self.nz_min, self.nze, self.lu, self.lr, self.kx_max, self.ky_max,
+         self.kz_max, self.lm, self.nx2) = [int(x) for x in d]
+        self.nx, self.ny, self.nz = cfg.nx, cfg.ny, cfg.nz
+
+    def __getattribute__(self, name):
+        attr = object.__getattribute__(self, name)
+        if callable(attr) and not name.startswith("__") and name not in ("_check", "wave", "zblocks", "xyplanes",
+                                                                          "phys"):
+            self._check(load_library().sam_gpu_ensemble_select(object.__getattribute__(self, "_index")),
+                        "ensemble_select")
+        return attr
+
+    def close(self):
+        pass
+
+
+class SamEnsemble:
+    """Independent runs advanced together (sam_gpu_ensemble_*): one CUDA graph
+    per step over every member, each member its own branch and buffers."""
+
+    def __init__(self, cfgs):
+        lib = load_library()
+        if SamGpu._live is not None:
+            SamGpu._live.close()
+        defaults = dict(n_dealias=1, i_strat=0, i_cfl=0, nrk_max=3, rot_sav=0, i_les=0, precision=64,
+                        xl=2 * np.pi, yl=2 * np.pi, zl=2 * np.pi, vis=0.0, pr=1.0, dt0=0.01, cfl0=0.5,
+                        buoy_fac_x=0.0, buoy_fac_z=0.0, lapse=0.0, cos_theta=1.0, sin_theta=0.0, c_smag=0.01)
+        arr = (Config * len(cfgs))()
+        for i, cfg in enumerate(cfgs):
+            d = dict(defaults)
+            d.update(cfg)
+            for k, v in d.items():
+                setattr(arr[i], k, v)
+        self._arr = arr
+        rc = lib.sam_gpu_ensemble_create(C.cast(arr, C.c_void_p), len(cfgs))
+        if rc != SAM_GPU_OK:
+            raise SamGpuError(f"ensemble_create failed ({ERRORS.get(rc, rc)}): "
+                              + lib.sam_gpu_error_string().decode(errors="replace"))
+        SamGpu._live = self
+        self.members = [_Member(self, i, arr[i]) for i in range(len(cfgs))]
+
+    def __len__(self):
+        return len(self.members)
+
+    def __getitem__(self, i):
+        return self.members[i]
+
+    def step(self, nsteps=1):
+        rc = load_library().sam_gpu_ensemble_step(nsteps)
+        if rc != SAM_GPU_OK:
+            raise SamGpuError(f"ensemble_step failed ({ERRORS.get(rc, rc)}): "
+                              + load_library().sam_gpu_error_string().decode(errors="replace"))
+
+    def close(self):
+        if SamGpu._live is self:
+            load_library().sam_gpu_ensemble_destroy()
+            SamGpu._live = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
