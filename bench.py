@@ -201,22 +201,44 @@ def closure_params():
         return CD.init_params(0), "untrained initial weights"
 
 
-def les_forms(stream, u_init, K, W):
+LES_WORKLOAD = ("LES of stratified forced turbulence 256^3, N=1 (buoy_fac_z = lapse = 1), Pr=1, nu=1e-4, "
+                "random solenoidal start k^4 exp(-2(k/4)^2) at rms 1 (seed 3), T at 0.1, OU forcing of "
+                "|k| <= 2.5 (sigma 0.15, T_L 0.5, seed 4), RK3 CFL 0.5")
+
+
+def les_cfg(precision):
+    return dict(nx=N, ny=N, nz=N, i_strat=1, i_cfl=1, cfl0=0.5, vis=1e-4, pr=1.0, dt0=1e-3, buoy_fac_z=1.0,
+                lapse=1.0, precision=precision)
+
+
+def les_forms(stream, K, W):
     """Steps/s of the FP64 drop-in with dm.f's dynamic closure and of the
-    FP32 bulk form with the learned closure on the same workload and start
-    state (CUDA events on the launching stream), and how far the FP32 +
+    FP32 bulk form with the learned closure on the LES workload from the same
+    start (CUDA events on the launching stream), and how far the FP32 +
     learned spectrum is from the FP64 + dm.f spectrum after the timed steps
     (shells k <= k_max/2)."""
     import numpy as np
     import torch
     from sam_gb300 import SamGpu
     params, src = closure_params()
-    out = {}
+    out = {"workload": LES_WORKLOAD, "spinup": "FP32 + learned closure to t = 1 (untimed), then both runs from "
+                                               "that state"}
+    # a developed start: the random field has no energy near the cutoff
+    g = SamGpu(**les_cfg(32))
+    g.init_random(3, 6, 1.0, 6, 0.1)
+    g.set_forcing(4, 2.5, 0.15, 0.5)
+    g.mlp_set(params)
+    g.set_les(3)
+    while g.stats()["time"] < 1.0:
+        g.step(20)
+    u0 = g.download()
+    g.close()
     spectra = {}
     for name, prec, model in (("fp64_dm", 64, 2), ("fp32_learned", 32, 3)):
-        g = SamGpu(**workload_cfg(precision=prec))
+        g = SamGpu(**les_cfg(prec))
         g.set_stream(stream.cuda_stream)
-        g.upload(u_init)
+        g.upload(u0)
+        g.set_forcing(4, 2.5, 0.15, 0.5)
         if model == 3:
             g.mlp_set(params)
         g.set_les(model)
@@ -463,7 +485,7 @@ def main():
     # dynamic Smagorinsky coupled in, and FP32 bulk with the learned closure
     les = None
     if not args.no_les:
-        les = les_forms(stream, u_init, K, W)
+        les = les_forms(stream, max(K, 20), W)
     ens = None
     if not args.no_ensemble:
         ens = ensemble_form(max(4, K // 2), W)

@@ -21,112 +21,9 @@
 #include <stdint.h>
 
 #include "closure.cuh"
+#include "tc05.cuh"
 
 namespace samgpu {
-
-// ------------------------------------------------------------ PTX helpers
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-// byte offset of element (r, k) of a K-major tile with K columns
-__device__ __forceinline__ uint32_t kmaj(int r, int k, int K) {
-  return (uint32_t)((r >> 3) * (K >> 3) * 128 + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
-}
-
-// shared-memory matrix descriptor: start, leading (K) and stride (M/N) byte
-// offsets, descriptor version 1, no swizzle
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-  uint64_t d = (uint64_t)((saddr & 0x3FFFFu) >> 4);
-  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
-  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
-  d |= (uint64_t)1 << 46;
-  return d;
-}
-
-// instruction descriptor of kind::f16: D F32, A and B BF16, both K-major
-__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
-  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
-}
-
-__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
-  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(dst)), "r"(ncols)
-               : "memory");
-  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-}
-__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
-  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
-}
-__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
-      "l"(a), "l"(b), "r"(idesc), "r"(acc)
-      : "memory");
-}
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-               : "memory");
-}
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-// bounded wait on phase `parity`; 0 when it completed, 1 on timeout
-__device__ __forceinline__ int mbar_wait(uint64_t* bar, uint32_t parity) {
-  const uint32_t a = smem_u32(bar);
-  for (uint32_t it = 0; it < (1u << 24); ++it) {
-    uint32_t done;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(done)
-        : "r"(a), "r"(parity)
-        : "memory");
-    if (done) return 0;
-  }
-  return 1;
-}
-// 16 consecutive FP32 columns of this warp's 32 TMEM lanes (one per thread)
-__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
-  uint32_t r[16];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15}, [%16];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<const uint32_t*>(&h);
-}
-
-// eight values of row r, columns k0..k0+7, into a K-major tile as one 16 B store
-__device__ __forceinline__ void st_row8(uint8_t* tile, int r, int k0, int K, const float* v) {
-  uint4 q;
-  q.x = pack_bf16(v[0], v[1]);
-  q.y = pack_bf16(v[2], v[3]);
-  q.z = pack_bf16(v[4], v[5]);
-  q.w = pack_bf16(v[6], v[7]);
-  *reinterpret_cast<uint4*>(tile + kmaj(r, k0, K)) = q;
-}
-
-// copy a row-major [R][K] BF16 matrix into a K-major tile
-__device__ __forceinline__ void stage_matrix(uint8_t* tile, const __nv_bfloat16* __restrict__ src, int R, int K) {
-  for (int e = threadIdx.x; e < R * (K / 8); e += blockDim.x) {
-    const int r = e / (K / 8), k0 = (e - r * (K / 8)) * 8;
-    *reinterpret_cast<uint4*>(tile + kmaj(r, k0, K)) = *reinterpret_cast<const uint4*>(src + r * K + k0);
-  }
-}
-
-__device__ __forceinline__ float softplus(float x) { return x > 20.f ? x : log1pf(expf(x)); }
 
 // ------------------------------------------------------------- MMA selftest
 // D(128 x 64) = A(128 x 16) B(64 x 16)^T: the smallest use of the path the
@@ -177,17 +74,40 @@ void mlp_mma_selftest(const __nv_bfloat16* a, const __nv_bfloat16* b, float* d, 
 }
 
 // ------------------------------------------------------------ forward pass
+// One hidden layer's epilogue for this thread's row: TMEM -> +bias, ReLU ->
+// BF16 K-major operand tile (and, when hg is given, the activations).
+__device__ __forceinline__ void epilogue(uint32_t tl, const float* __restrict__ bias, uint8_t* tile, int r,
+                                         __nv_bfloat16* __restrict__ hg, long long row, bool live) {
+#pragma unroll
+  for (int c0 = 0; c0 < kMlpH; c0 += 16) {
+    float h[16];
+    tmem_ld16(tl + (uint32_t)c0, h);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) h[k] = fmaxf(h[k] + bias[c0 + k], 0.f);
+    st_row8(tile, r, c0, kMlpH, h);
+    st_row8(tile, r, c0 + 8, kMlpH, h + 8);
+    if (hg && live) {
+      uint4* dst = reinterpret_cast<uint4*>(hg + row * kMlpH + c0);
+      dst[0] = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
+      dst[1] = make_uint4(pack_bf16(h[8], h[9]), pack_bf16(h[10], h[11]), pack_bf16(h[12], h[13]),
+                          pack_bf16(h[14], h[15]));
+    }
+  }
+}
+
 // Persistent CTAs of 128 threads; thread t owns row t of every tile (its
 // TMEM lane).  Optionally stores the activations for the backward pass.
-__global__ void __launch_bounds__(128) k_mlp_fwd(const __nv_bfloat16* __restrict__ x16, long long n,
+__global__ void __launch_bounds__(128, 7) k_mlp_fwd(const __nv_bfloat16* __restrict__ x16, long long n,
                                                  const MlpDev* __restrict__ P, float2* __restrict__ coef,
                                                  __nv_bfloat16* __restrict__ h1g, __nv_bfloat16* __restrict__ h2g,
                                                  float* __restrict__ og, int* err) {
   __shared__ __align__(1024) uint8_t sw1[kMlpH * kMlpK1 * 2];
   __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];
   __shared__ __align__(1024) uint8_t sw3[kMlpN3 * kMlpH * 2];
-  __shared__ __align__(1024) uint8_t sa1[kMlpTile * kMlpK1 * 2];
+  // the input tile (128 x 16) lives in the first 4 KB of the hidden tile:
+  // layer 1's output overwrites it only after its MMA has completed
   __shared__ __align__(1024) uint8_t sa2[kMlpTile * kMlpH * 2];
+  uint8_t* sa1 = sa2;
   __shared__ float sb1[kMlpH], sb2[kMlpH], sb3[kMlpN3];
   __shared__ uint64_t bar;
   __shared__ uint32_t tbase;
@@ -214,17 +134,25 @@ __global__ void __launch_bounds__(128) k_mlp_fwd(const __nv_bfloat16* __restrict
   uint32_t phase = 0;
   int bad = 0;
   const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const long long row = t * kMlpTile + tid;
-    const bool live = row < n;
-    uint4 q0 = make_uint4(0, 0, 0, 0), q1 = q0;
-    if (live) {
-      const uint4* src = reinterpret_cast<const uint4*>(x16 + row * kMlpK1);
+  // the inputs of the next tile are loaded while this tile's MMA chain runs
+  auto fetch = [&](long long t, uint4& q0, uint4& q1) {
+    const long long r = t * kMlpTile + tid;
+    q0 = make_uint4(0, 0, 0, 0);
+    q1 = q0;
+    if (t < ntiles && r < n) {
+      const uint4* src = reinterpret_cast<const uint4*>(x16 + r * kMlpK1);
       q0 = src[0];
       q1 = src[1];
     }
+  };
+  uint4 q0, q1;
+  fetch(blockIdx.x, q0, q1);
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const long long row = t * kMlpTile + tid;
+    const bool live = row < n;
     *reinterpret_cast<uint4*>(sa1 + kmaj(tid, 0, kMlpK1)) = q0;
     *reinterpret_cast<uint4*>(sa1 + kmaj(tid, 8, kMlpK1)) = q1;
+    fetch(t + gridDim.x, q0, q1);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -238,20 +166,9 @@ __global__ void __launch_bounds__(128) k_mlp_fwd(const __nv_bfloat16* __restrict
     phase ^= 1;
     tc_fence_after();
     if (__syncthreads_or(bad)) break;
-    float h[kMlpH];
-#pragma unroll
-    for (int c = 0; c < kMlpH; c += 16) tmem_ld16(tl + (uint32_t)c, h + c);
-#pragma unroll
-    for (int k = 0; k < kMlpH; ++k) h[k] = fmaxf(h[k] + sb1[k], 0.f);
-#pragma unroll
-    for (int k0 = 0; k0 < kMlpH; k0 += 8) st_row8(sa2, tid, k0, kMlpH, h + k0);
-    if (h1g && live) {
-#pragma unroll
-      for (int k0 = 0; k0 < kMlpH; k0 += 8)
-        *reinterpret_cast<uint4*>(h1g + row * kMlpH + k0) =
-            make_uint4(pack_bf16(h[k0], h[k0 + 1]), pack_bf16(h[k0 + 2], h[k0 + 3]), pack_bf16(h[k0 + 4], h[k0 + 5]),
-                       pack_bf16(h[k0 + 6], h[k0 + 7]));
-    }
+    // epilogue in chunks of 16 columns: bias, ReLU, BF16 into the next
+    // operand tile (and the activations for the backward pass)
+    epilogue(tl, sb1, sa2, tid, h1g, row, live);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -267,19 +184,7 @@ __global__ void __launch_bounds__(128) k_mlp_fwd(const __nv_bfloat16* __restrict
     phase ^= 1;
     tc_fence_after();
     if (__syncthreads_or(bad)) break;
-#pragma unroll
-    for (int c = 0; c < kMlpH; c += 16) tmem_ld16(tl + (uint32_t)c, h + c);
-#pragma unroll
-    for (int k = 0; k < kMlpH; ++k) h[k] = fmaxf(h[k] + sb2[k], 0.f);
-#pragma unroll
-    for (int k0 = 0; k0 < kMlpH; k0 += 8) st_row8(sa2, tid, k0, kMlpH, h + k0);
-    if (h2g && live) {
-#pragma unroll
-      for (int k0 = 0; k0 < kMlpH; k0 += 8)
-        *reinterpret_cast<uint4*>(h2g + row * kMlpH + k0) =
-            make_uint4(pack_bf16(h[k0], h[k0 + 1]), pack_bf16(h[k0 + 2], h[k0 + 3]), pack_bf16(h[k0 + 4], h[k0 + 5]),
-                       pack_bf16(h[k0 + 6], h[k0 + 7]));
-    }
+    epilogue(tl, sb2, sa2, tid, h2g, row, live);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
@@ -321,7 +226,7 @@ __global__ void __launch_bounds__(128) k_mlp_fwd(const __nv_bfloat16* __restrict
 int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2* coef, const MlpBatch* batch,
                 int* err, cudaStream_t s) {
   const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
-  long long grid = 152 * 6;
+  long long grid = 152 * 7;  // 28.7 KB of shared memory and 64 TMEM columns per CTA
   if (grid > ntiles) grid = ntiles;
   if (grid < 1) return 0;
   k_mlp_fwd<<<(int)grid, kMlpTile, 0, s>>>(x16, n, dev, coef, batch ? batch->h1 : nullptr,
