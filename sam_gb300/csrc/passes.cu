@@ -233,6 +233,42 @@ __device__ __forceinline__ void store_pair(double2* o, double2 a, double2 b) {
   o[1] = b;
 }
 
+// First-stage loader of the backward x transform: the stored half spectrum
+// with the truncated band lo < idx < hi read as zero.
+template <typename C> struct BandLoad {
+  const C* line;
+  int lo, hi;
+  __device__ __forceinline__ C operator()(int idx) const {
+    if (idx > lo && idx < hi) return mk<C>((decltype(C::x))0, (decltype(C::x))0);
+    return line[sidx(idx)];
+  }
+};
+
+// Error-free FP32 accumulation (Knuth's TwoSum, Dekker/FMA TwoProduct): a
+// running sum kept as an unevaluated pair hi + lo carries about 48 bits,
+// enough for the FP64-accurate vel_max sums of the FP32 form without FP64
+// arithmetic (which runs at 1/64 of the FP32 rate on this GPU).
+struct DF {
+  float hi, lo;
+};
+__device__ __forceinline__ DF df_add(DF a, float b) {
+  const float s = a.hi + b;
+  const float bb = s - a.hi;
+  const float err = (a.hi - (s - bb)) + (b - bb);
+  const float lo = a.lo + err;
+  const float h = s + lo;
+  return DF{h, lo - (h - s)};
+}
+__device__ __forceinline__ DF df_add(DF a, DF b) {
+  DF r = df_add(a, b.hi);
+  return df_add(r, b.lo);
+}
+__device__ __forceinline__ DF df_add_sq(DF a, float v) {
+  const float p = v * v;
+  const float e = fmaf(v, v, -p);  // p + e = v^2 exactly
+  return df_add(df_add(a, p), e);
+}
+
 // First-stage loader of the forward x transform: element idx of line a, or,
 // when b is given, of line a times line b component by component (the two
 // real rows of a pair multiply separately), i.e. a product line of rhs.f.
@@ -384,11 +420,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
   // ---- build the input lines
   if (a.in_mode == 0) {
     // spectral rows of B(n, z, y, kx): Hermitian half spectra with kx <= kx_max
-    const int nband = nx - 2 * kmx - 1;
-    for (int e = threadIdx.x; e < nin * yp * nband; e += blockDim.x) {
-      const int L = (int)fdiv(e, a.fd_band), p = e - L * nband;
-      s_in[L * ld + sidx(kmx + 1 + p)] = mk<C>((T)0, (T)0);
-    }
+    // (the truncated band kx_max < p < Nx - kx_max is never stored: the
+    // transform's first stage reads it as zero)
     // element e -> line L = (f, c) and kx; loads the two rows of the pair
     struct Pair { C x, y; };
     batched<Pair>(
@@ -414,7 +447,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
           if (kx > 0) s_in[L * ld + sidx(nx - kx)] = mk<C>(X.x + Yv.y, Yv.x - X.y);
         });
     __syncthreads();
-    fft_lines<+1>(s_in, ld, nin * yp, s_tw, pl);
+    fft_lines_from<+1>(s_in, ld, nin * yp, s_tw, pl,
+                       [&](int L) { return BandLoad<C>{s_in + L * ld, kmx, nx - kmx}; });
   } else {
     // physical rows of P(n, z, y, x)
     struct Pair { T x, y; };
@@ -437,36 +471,59 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
   }
   __syncthreads();
 
-  // ---- vel_max partial sums (vel_max.f:158-168), FP64, deterministic order
+  // ---- vel_max partial sums (vel_max.f:158-168), FP64-accurate,
+  // deterministic order (FP64 arithmetic in the FP64 form; error-free FP32
+  // pairs in the FP32 form, turned into FP64 per warp)
   if (a.partials) {
     for (int f = 0; f < a.g.lu; ++f) {
       double s1 = 0.0, s2 = 0.0;
+      DF d1{0.f, 0.f}, d2{0.f, 0.f};
       T mxv = (T)0;
       int bad = 0;
       for (int e = threadIdx.x; e < yp * nx; e += blockDim.x) {
         const int c = (int)fdiv(e, a.fd_nx), x = e - c * nx;
         const C v = s_in[(f * yp + c) * ld + sidx(x)];
         if (y0 + 2 * c < ny) {
-          const double d = (double)v.x;
-          s1 += d; s2 += d * d;
+          if (sizeof(T) == 8) {
+            const double d = (double)v.x;
+            s1 += d; s2 += d * d;
+          } else {
+            d1 = df_add(d1, (float)v.x);
+            d2 = df_add_sq(d2, (float)v.x);
+          }
           mxv = fmax(mxv, fabs(v.x));
           bad |= !isfinite(v.x);
         }
         if (y0 + 2 * c + 1 < ny) {
-          const double d = (double)v.y;
-          s1 += d; s2 += d * d;
+          if (sizeof(T) == 8) {
+            const double d = (double)v.y;
+            s1 += d; s2 += d * d;
+          } else {
+            d1 = df_add(d1, (float)v.y);
+            d2 = df_add_sq(d2, (float)v.y);
+          }
           mxv = fmax(mxv, fabs(v.y));
           bad |= !isfinite(v.y);
         }
       }
+      if (sizeof(T) == 4) {
+        for (int o = 16; o > 0; o >>= 1) {
+          d1 = df_add(d1, DF{__shfl_xor_sync(0xffffffffu, d1.hi, o), __shfl_xor_sync(0xffffffffu, d1.lo, o)});
+          d2 = df_add(d2, DF{__shfl_xor_sync(0xffffffffu, d2.hi, o), __shfl_xor_sync(0xffffffffu, d2.lo, o)});
+        }
+        s1 = (double)d1.hi + (double)d1.lo;
+        s2 = (double)d2.hi + (double)d2.lo;
+      }
       // warp reduce then CTA reduce
-      double mxd = (double)mxv;
       for (int o = 16; o > 0; o >>= 1) {
-        s1 += __shfl_xor_sync(0xffffffffu, s1, o);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-        mxd = fmax(mxd, __shfl_xor_sync(0xffffffffu, mxd, o));
+        if (sizeof(T) == 8) {
+          s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+          s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        mxv = fmax(mxv, __shfl_xor_sync(0xffffffffu, mxv, o));
         bad |= __shfl_xor_sync(0xffffffffu, bad, o);
       }
+      const double mxd = (double)mxv;
       const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
       if ((threadIdx.x & 31) == 0) {
         s_red[w * 4 + 0] = s1; s_red[w * 4 + 1] = s2; s_red[w * 4 + 2] = mxd; s_red[w * 4 + 3] = (double)bad;
