@@ -355,15 +355,22 @@ __device__ __forceinline__ void fft256_lines(C* base, int ld, int nlines, const 
   }
 }
 
+// Code paths of the line transforms: kFftAny picks at run time (the plan's
+// length); kFft256 compiles only the 16 x 16 register path (n = 256) and
+// kFftGeneric only the Stockham stages, so a kernel built for one length
+// carries no registers for the other path.
+constexpr int kFftAny = 0, kFft256 = 1, kFftGeneric = 2;
+
 // Transform `nlines` lines of a CTA's shared-memory tile.  Line L starts at
 // base + L*ld.  Every thread of the CTA must call this with the same plan.
-template <int SIGN, typename C>
+template <int SIGN, int PATH = kFftAny, typename C>
 __device__ __forceinline__ void fft_lines(C* base, int ld, int nlines, const C* __restrict__ tw, const FftPlan& pl) {
   if (pl.n == 1) return;
-  if (pl.tw16_off >= 0) {
+  if (PATH == kFft256 || (PATH == kFftAny && pl.tw16_off >= 0)) {
     fft256_lines<SIGN>(base, ld, nlines, tw, pl, [&](int L) { return LineLoad<C>{base + L * ld}; });
     return;
   }
+  if (PATH == kFft256) return;
   const int TW = team_of<C>(pl);
   const int nteams = blockDim.x / TW;
   const int team = threadIdx.x / TW;
@@ -379,17 +386,18 @@ __device__ __forceinline__ void fft_lines(C* base, int ld, int nlines, const C* 
 // As fft_lines, with the first stage of line L reading through the loader
 // first(L) returns (a functor idx -> value).  A length-1 transform is the
 // identity: the inputs are only copied into place.
-template <int SIGN, typename C, typename First>
+template <int SIGN, int PATH = kFftAny, typename C, typename First>
 __device__ __forceinline__ void fft_lines_from(C* base, int ld, int nlines, const C* __restrict__ tw,
                                                const FftPlan& pl, First first) {
   if (pl.n == 1 || pl.nst == 0) {
     for (int L = threadIdx.x; L < nlines; L += blockDim.x) base[L * ld] = first(L)(0);
     return;
   }
-  if (pl.tw16_off >= 0) {
+  if (PATH == kFft256 || (PATH == kFftAny && pl.tw16_off >= 0)) {
     fft256_lines<SIGN>(base, ld, nlines, tw, pl, first);
     return;
   }
+  if (PATH == kFft256) return;
   const int TW = team_of<C>(pl);
   const int nteams = blockDim.x / TW;
   const int team = threadIdx.x / TW;

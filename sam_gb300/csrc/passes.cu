@@ -61,7 +61,7 @@ __device__ __forceinline__ void batched(int count, Get get, Put put) {
 // --------------------------------------------------------------- z inverse
 // Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
 // modes; output A(n, z, kx, ky) with ky fastest.
-template <typename T>
+template <typename T, int PATH>
 __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
         put);
   }
   __syncthreads();
-  fft_lines<+1>(s_ln, ld, nl, s_tw, pl);
+  fft_lines<+1, PATH>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)i * a.out_kx + j0;
   batched<C>(
@@ -173,7 +173,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
 // Tile: field n, plane z, kx columns i0 .. i0+TX-1.  Input rows (one per kx)
 // hold either Ny_min compact modes (zero band inserted here, as
 // x2z_decomp.f:111-124 does) or Ny values with the band already present.
-template <typename T>
+template <typename T, int PATH>
 __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv>::value) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -208,7 +208,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv>::value) k_y_
         s_ln[t * ld + sidx(p)] = v;
       });
   __syncthreads();
-  fft_lines<+1>(s_ln, ld, nl, s_tw, pl);
+  fft_lines<+1, PATH>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)z * a.out_z + i0;
   batched<C>(
@@ -396,7 +396,7 @@ __device__ __forceinline__ void product_pair(int m, int& a, int& b) {
   }
 }
 
-template <typename T>
+template <typename T, int PATH>
 __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -447,7 +447,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
           if (kx > 0) s_in[L * ld + sidx(nx - kx)] = mk<C>(X.x + Yv.y, Yv.x - X.y);
         });
     __syncthreads();
-    fft_lines_from<+1>(s_in, ld, nin * yp, s_tw, pl,
+    fft_lines_from<+1, PATH>(s_in, ld, nin * yp, s_tw, pl,
                        [&](int L) { return BandLoad<C>{s_in + L * ld, kmx, nx - kmx}; });
   } else {
     // physical rows of P(n, z, y, x)
@@ -643,7 +643,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
     // products of the physical lines, formed while the first FFT stage loads
     // them, straight into the product lines
     C* lines = a.out_mode == 1 ? s_in + m0 * yp * ld : s_pr;
-    fft_lines_from<-1>(lines, ld, gm * yp, s_tw, pl, [&](int L) {
+    fft_lines_from<-1, PATH>(lines, ld, gm * yp, s_tw, pl, [&](int L) {
       if (a.out_mode == 1) return ProductLoad<C>{lines + L * ld, nullptr, nullptr};
       const int gi = L / yp, c = L - gi * yp;
       int fa, fb;
@@ -682,7 +682,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
 // --------------------------------------------------------------- y forward
 // Tile: field m, kx column i, planes z0 .. z0+TZ-1.  Output D(m, kx, ky, z)
 // keeps |ky| <= ky_max (xy_trans_f.f:45-52).
-template <typename T>
+template <typename T, int PATH>
 __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd>::value) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -713,7 +713,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd>::value) k_y_
         s_ln[t * ld + sidx(p)] = v;
       });
   __syncthreads();
-  fft_lines<-1>(s_ln, ld, nl, s_tw, pl);
+  fft_lines<-1, PATH>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)m * a.out_n + (long long)i * a.out_kx + z0;
   batched<C>(
@@ -875,7 +875,7 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
 //   mode 0: write the truncated modes back in place (z_trans_f),
 //   mode 1: rhs epilogue (rhs.f:108-142) into r with u_sav from memory,
 //   mode 2: full stage epilogue: rhs, then sam.f:210-221 and 293-314.
-template <typename T>
+template <typename T, int PATH>
 __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -908,7 +908,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_
         if (t < nl) s_ln[(f * nl + t) * ld + sidx(p)] = v;
       });
   __syncthreads();
-  fft_lines<-1>(s_ln, ld, nf * nl, s_tw, pl);
+  fft_lines<-1, PATH>(s_ln, ld, nf * nl, s_tw, pl);
   __syncthreads();
   const T nz_inv = (T)(1.0 / (double)nz);
   if (a.mode == 0) {
@@ -1034,7 +1034,8 @@ void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_t = make_fastdiv(a.ty);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.nvar * a.g.mx * nty;
-  k_z_inv<T><<<grid, kThreads, smem, s>>>(a, pl);
+  if (a.g.nz == 256) k_z_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+  else k_z_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
 }
 template <typename T>
 void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
@@ -1043,7 +1044,8 @@ void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_t = make_fastdiv(a.tx);
   const int ntx = (a.g.mx + a.tx - 1) / a.tx;
   const int grid = a.nvar * a.g.nz * ntx;
-  k_y_inv<T><<<grid, kThreads, smem, s>>>(a, pl);
+  if (a.g.ny == 256) k_y_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+  else k_y_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
 }
 template <typename T>
 int x_pass_blocks(const XPassArgs<T>& a) {
@@ -1058,7 +1060,8 @@ void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaS
   a.fd_yp = make_fastdiv(a.yt / 2);
   a.fd_nx = make_fastdiv(a.g.nx);
   a.fd_y = make_fastdiv(a.yt);
-  k_x_pass<T><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
+  if (a.g.nx == 256) k_x_pass<T, kFft256><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
+  else k_x_pass<T, kFftGeneric><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
 }
 template <typename T>
 void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
@@ -1067,7 +1070,8 @@ void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_t = make_fastdiv(a.tz);
   const int ntz = (a.g.nz + a.tz - 1) / a.tz;
   const int grid = a.nvar * a.g.mx * ntz;
-  k_y_fwd<T><<<grid, kThreads, smem, s>>>(a, pl);
+  if (a.g.ny == 256) k_y_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+  else k_y_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
 }
 template <typename T>
 void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
@@ -1077,7 +1081,8 @@ void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_m = make_fastdiv(a.g.mz);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.g.mx * nty;
-  k_z_fwd<T><<<grid, kThreads, smem, s>>>(a, pl);
+  if (a.g.nz == 256) k_z_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+  else k_z_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
 }
 void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
                            double adv_cfl_limit, cudaStream_t s) {
@@ -1104,11 +1109,16 @@ void set_smem_limits() {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  allow_dynamic_smem((const void*)k_z_inv<T>, optin);
-  allow_dynamic_smem((const void*)k_y_inv<T>, optin);
-  allow_dynamic_smem((const void*)k_x_pass<T>, optin);
-  allow_dynamic_smem((const void*)k_y_fwd<T>, optin);
-  allow_dynamic_smem((const void*)k_z_fwd<T>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, kFft256>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, kFft256>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, kFft256>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, kFft256>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, kFft256>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, kFftGeneric>, optin);
 }
 
 #define SAMGPU_INST(T)                                                                           \
