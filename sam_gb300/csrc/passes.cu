@@ -474,7 +474,52 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
   // ---- vel_max partial sums (vel_max.f:158-168), FP64-accurate,
   // deterministic order (FP64 arithmetic in the FP64 form; error-free FP32
   // pairs in the FP32 form, turned into FP64 per warp)
-  if (a.partials) {
+  if (a.partials && a.max_only) {
+    // the FP32 form: max |u| and the non-finite flag here, the sums from
+    // wave space (k_parseval); all four fields in one reduction
+    T mx4[4] = {(T)0, (T)0, (T)0, (T)0};
+    int bad = 0;
+    for (int e = threadIdx.x; e < yp * nx; e += blockDim.x) {
+      const int c = (int)fdiv(e, a.fd_nx), x = e - c * nx;
+      const bool ra = y0 + 2 * c < ny, rb = y0 + 2 * c + 1 < ny;
+#pragma unroll
+      for (int f = 0; f < 4; ++f)
+        if (f < a.g.lu) {
+          const C v = s_in[(f * yp + c) * ld + sidx(x)];
+          if (ra) {
+            mx4[f] = fmax(mx4[f], fabs(v.x));
+            bad |= !isfinite(v.x);
+          }
+          if (rb) {
+            mx4[f] = fmax(mx4[f], fabs(v.y));
+            bad |= !isfinite(v.y);
+          }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int f = 0; f < 4; ++f) mx4[f] = fmax(mx4[f], __shfl_xor_sync(0xffffffffu, mx4[f], o));
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+      for (int f = 0; f < 4; ++f) s_red[w * 4 + f] = (double)mx4[f];
+      s_red[nw * 4 + w] = (double)bad;
+    }
+    __syncthreads();
+    if (threadIdx.x < a.g.lu) {
+      const int f = threadIdx.x;
+      double tm = 0, tb = 0;
+      for (int k = 0; k < nw; ++k) {
+        tm = fmax(tm, s_red[k * 4 + f]);
+        tb += s_red[nw * 4 + k];
+      }
+      double* dst = a.partials + ((long long)blockIdx.x * a.g.lu + f) * 4;
+      dst[0] = 0.0; dst[1] = 0.0; dst[2] = tm; dst[3] = tb;
+    }
+    __syncthreads();
+  } else if (a.partials) {
     for (int f = 0; f < a.g.lu; ++f) {
       double s1 = 0.0, s2 = 0.0;
       DF d1{0.f, 0.f}, d2{0.f, 0.f};
@@ -958,8 +1003,48 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_
 
 // ----------------------------------------------------- vel_max completion
 // vel_max.f:170-196 on the per-CTA partials written by k_x_pass.
+// Parseval sums of vel_max (see launch_parseval): FP64 products of the
+// stored modes, per-thread strided order, block tree, fixed launch shape.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict__ u, Grid g, FastDiv fd_plane,
+                                                       double* __restrict__ pv) {
+  __shared__ double red[4][kThreads];
+  const long long nm = (long long)g.mx * g.my * g.mz;
+  const int plane = g.my * g.mz;
+  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < nm; m += (long long)gridDim.x * blockDim.x) {
+    const double w = fdiv((uint32_t)m, fd_plane) == 0 ? 1.0 : 2.0;
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+      if (f < g.lu) {
+        const cx_t<T> v = u[f * nm + m];
+        const double re = (double)v.x, im = (double)v.y;
+        acc[f] = fma(w * re, re, fma(w * im, im, acc[f]));
+      }
+  }
+#pragma unroll
+  for (int f = 0; f < 4; ++f) red[f][threadIdx.x] = acc[f];
+  __syncthreads();
+  for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s)
+#pragma unroll
+      for (int f = 0; f < 4; ++f) red[f][threadIdx.x] += red[f][threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x < g.lu) pv[(long long)blockIdx.x * g.lu + threadIdx.x] = red[threadIdx.x][0];
+  if (blockIdx.x == 0 && threadIdx.x < g.lu) pv[(long long)gridDim.x * g.lu + threadIdx.x] = (double)u[threadIdx.x * nm].x;
+  (void)plane;
+}
+
+template <typename T>
+void launch_parseval(const cx_t<T>* u, const Grid& g, double* pv, cudaStream_t s) {
+  k_parseval<T><<<kParsevalBlocks, kThreads, 0, s>>>(u, g, make_fastdiv((uint32_t)(g.my * g.mz)), pv);
+}
+template void launch_parseval<float>(const float2*, const Grid&, double*, cudaStream_t);
+template void launch_parseval<double>(const double2*, const Grid&, double*, cudaStream_t);
+
 __global__ void k_vel_max_finish(const double* __restrict__ partials, int nblk, Grid g, DevState* st, int i_cfl,
-                                 double cfl0, double adv_cfl_limit) {
+                                 double cfl0, double adv_cfl_limit, const double* __restrict__ pv, int npv) {
   __shared__ double red[kThreads];
   __shared__ double fin[4][4];
   for (int f = 0; f < g.lu; ++f) {
@@ -977,6 +1062,25 @@ __global__ void k_vel_max_finish(const double* __restrict__ partials, int nblk, 
         __syncthreads();
       }
       if (threadIdx.x == 0) fin[f][q] = red[0];
+      __syncthreads();
+    }
+  }
+  if (pv) {
+    // sums from wave space: sum u = N u(0,0,0), sum u^2 = N sum w |u|^2
+    for (int f = 0; f < g.lu; ++f) {
+      double v = 0.0;
+      for (int b = threadIdx.x; b < npv; b += blockDim.x) v += pv[(long long)b * g.lu + f];
+      red[threadIdx.x] = v;
+      __syncthreads();
+      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        const double n = (double)g.nx * (double)g.ny * (double)g.nz;
+        fin[f][0] = pv[(long long)npv * g.lu + f] * n;
+        fin[f][1] = red[0] * n;
+      }
       __syncthreads();
     }
   }
@@ -1085,8 +1189,8 @@ void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   else k_z_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
 }
 void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
-                           double adv_cfl_limit, cudaStream_t s) {
-  k_vel_max_finish<<<1, kThreads, 0, s>>>(partials, nblk, g, st, i_cfl, cfl0, adv_cfl_limit);
+                           double adv_cfl_limit, cudaStream_t s, const double* pv, int npv) {
+  k_vel_max_finish<<<1, kThreads, 0, s>>>(partials, nblk, g, st, i_cfl, cfl0, adv_cfl_limit, pv, npv);
 }
 void launch_x2z(const double2* in, double2* out, const Grid& g, int nvar, int nx2, cudaStream_t s) {
   long long total = (long long)g.ny * g.mx * g.nz * nvar;

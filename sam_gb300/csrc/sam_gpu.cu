@@ -158,6 +158,7 @@ struct Ctx {
   void *U = nullptr, *R = nullptr, *P = nullptr, *S1 = nullptr, *S2 = nullptr, *S3 = nullptr;
   double* partials = nullptr;
   int partial_blocks = 0;
+  double* pv = nullptr;  // vel_max's wave-space sums (FP32 form)
   DevState* state = nullptr;
   Scratch sc[4];
   // tile choices
@@ -336,10 +337,16 @@ static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in
       c.partial_blocks = nblk;
     }
     a.partials = c.partials;
+    // the FP32 form takes vel_max's sums from wave space (Parseval, FP64
+    // arithmetic): the x pass then only forms max |u| and the NaN check
+    a.max_only = sizeof(T) == 4 && in_mode == 0 && in == c.S2;
   }
   launch_x_pass<T>(a, c.px.d, x_smem<T>(c, nin, a.yt, a.group), c.stream);
-  if (stats)
-    launch_vel_max_finish(c.partials, nblk, c.g, c.state, c.cfg.i_cfl, c.cfg.cfl0, c.adv_cfl_limit, c.stream);
+  if (stats) {
+    if (a.max_only) launch_parseval<T>((const cx_t<T>*)c.U, c.g, c.pv, c.stream);
+    launch_vel_max_finish(c.partials, nblk, c.g, c.state, c.cfg.i_cfl, c.cfg.cfl0, c.adv_cfl_limit, c.stream,
+                          a.max_only ? c.pv : nullptr, kParsevalBlocks);
+  }
   return 0;
 }
 
@@ -493,7 +500,7 @@ static void free_ctx(Ctx* c) {
   free_plan(c->px); free_plan(c->py); free_plan(c->pz);
   cudaFree(c->U); cudaFree(c->R); cudaFree(c->P);
   cudaFree(c->S1); cudaFree(c->S2); cudaFree(c->S3);
-  cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou);
+  cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou); cudaFree(c->pv);
   cudaFree(c->les_cds); cudaFree(c->les_phys); cudaFree(c->les_work);
   cudaFree(c->les_feat); cudaFree(c->les_coef);
   cudaFree(c->mlp_p); cudaFree(c->mlp_m); cudaFree(c->mlp_v); cudaFree(c->mlp_g); cudaFree(c->mlp_loss);
@@ -685,6 +692,7 @@ static int init_ctx(const sam_gpu_config* cfg) {
   // allocation ever happens inside a captured step
   c->partial_blocks = g.nz * g.ny;
   ok = ok && cudaMalloc(&c->partials, sizeof(double) * 4 * 4 * (size_t)c->partial_blocks) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->pv, sizeof(double) * 4 * ((size_t)kParsevalBlocks + 1)) == cudaSuccess;
   if (!ok) { free_ctx(c); g_ctx = nullptr; return fail(SAM_GPU_ECUDA, "device allocation failed"); }
   cudaMemset(c->U, 0, es * g.lu * nzmm);
   cudaMemset(c->R, 0, es * g.lu * nzmm);

@@ -245,3 +245,26 @@ def test_full_size_properties(gpu_lib):
     assert np.array_equal(g.download(), u1)  # deterministic replay
     st = g.stats()
     assert st["nonfinite"] == 0 and np.isfinite(st["energy"])
+
+
+def test_fp32_vel_max_sums_from_wave_space(gpu_lib):
+    """The FP32 form takes vel_max's sums from the state in wave space
+    (Parseval, FP64 arithmetic) and max |u| from the physical field: after
+    one step its statistics agree with the FP64 drop-in's physical-space
+    sums to the FP32 rounding of the field."""
+    cfg = dict(nx=32, ny=24, nz=40, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=1e-3, i_cfl=1, cfl0=0.5)
+    o = O.Oracle(**cfg)
+    u = o.init_random(13)
+    stats = []
+    for prec in (64, 32):
+        g = SamGpu(precision=prec, **cfg)
+        g.upload(u)
+        g.stage(1)
+        stats.append(g.stats())
+        g.close()
+    s64, s32 = stats
+    for key in ("u_avg", "u_var", "u_max"):
+        scale = np.abs(s64[key]).max()
+        assert np.abs(s32[key] - s64[key]).max() <= 1e-6 * scale, key
+    assert abs(s32["energy"] - s64["energy"]) <= 1e-6 * s64["energy"]
+    assert abs(s32["dt"] - s64["dt"]) <= 1e-6 * s64["dt"]
