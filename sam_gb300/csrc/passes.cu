@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
     const long long off = (long long)i * a.in_kx + (long long)j0 * a.in_ky;
     const C* srca = a.in + (long long)(vort || m < 6 ? fa : 3) * a.in_n + off;
     const C* srcb = a.in + (long long)(vort || m < 6 ? fb : 3) * a.in_n + off;
-    const double kxv = a.g.wave_x * (double)i;
+    const T kxv = (T)a.g.wave_x * (T)i;
     batched<C>(
         nl * nz,
         [&](int e) {
@@ -128,8 +128,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
           if (p <= km) q = p;
           else if (p >= nz - km) q = p - (nz - mz);
           if (q >= 0) {
-            const double kv[3] = {kxv, a.g.wave_y * (double)kwave(j0 + t, a.g.ky, my),
-                                  a.g.wave_z * (double)kwave(q, km, mz)};
+            const T kv[3] = {kxv, (T)a.g.wave_y * (T)kwave(j0 + t, a.g.ky, my), (T)a.g.wave_z * (T)kwave(q, km, mz)};
             const C ua = srca[(long long)t * a.in_ky + q];
             if (vort) {
               const C ub = srcb[(long long)t * a.in_ky + q];
@@ -677,7 +676,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
     }
     return;
   }
-  const T fn = (T)(0.5 / ((double)nx * (double)ny));  // 1/(Nx Ny) (xy_trans_f.f:20) and the 1/2 of the split
+  const T fn = a.fn;  // 1/(Nx Ny) (xy_trans_f.f:20) and the 1/2 of the split
   const int nout = a.out_mode == 1 ? nin : a.g.lr;
   // out_mode 1 transforms the input lines in place, all at once; out_mode 2
   // forms the products `group` fields at a time (group >= 1 by construction)
@@ -788,7 +787,7 @@ __device__ __forceinline__ EpiConst<W> epi_const(const ZFwdArgs<T>& a, double dt
   const StageConsts& sc = a.sc;
   EpiConst<W> e;
   e.wave_x = (W)a.g.wave_x; e.wave_y = (W)a.g.wave_y; e.wave_z = (W)a.g.wave_z;
-  e.nz_inv = (W)(1.0 / (double)a.g.nz);
+  e.nz_inv = (W)a.nz_inv;
   e.dt_fac1 = (W)(sc.gamma * dt);
   e.dt_fac2 = (W)(sc.zeta * dt);
   const double vis_f = sc.vis * (sc.gamma * dt + sc.zeta * dt);  // sam.f:293-295
@@ -955,7 +954,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_
   __syncthreads();
   fft_lines<-1, PATH>(s_ln, ld, nf * nl, s_tw, pl);
   __syncthreads();
-  const T nz_inv = (T)(1.0 / (double)nz);
+  const T nz_inv = a.nz_inv;
   if (a.mode == 0) {
     for (int e = threadIdx.x; e < nf * a.ty * mz; e += blockDim.x) {
       const int r = (int)fdiv(e, a.fd_m), k = e - r * mz;
@@ -970,7 +969,11 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_
   }
   double dt = 0.0;
   if (a.mode == 2) dt = a.state->dt;
-  const EpiConst<T> cw = epi_const<T>(a, dt);
+  // the epilogue constants once per CTA (FP64 arithmetic on one thread)
+  __shared__ EpiConst<T> s_cw;
+  if (threadIdx.x == 0) s_cw = epi_const<T>(a, dt);
+  __syncthreads();
+  const EpiConst<T> cw = s_cw;
   // two modes per iteration: their global loads are issued together
   for (int e0 = threadIdx.x; e0 < nl * mz; e0 += 2 * blockDim.x) {
     const int e1 = e0 + blockDim.x;
@@ -1164,6 +1167,7 @@ void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaS
   a.fd_yp = make_fastdiv(a.yt / 2);
   a.fd_nx = make_fastdiv(a.g.nx);
   a.fd_y = make_fastdiv(a.yt);
+  a.fn = (T)(0.5 / ((double)a.g.nx * (double)a.g.ny));
   if (a.g.nx == 256) k_x_pass<T, kFft256><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
   else k_x_pass<T, kFftGeneric><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
 }
@@ -1183,6 +1187,7 @@ void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_n = make_fastdiv(a.g.nz);
   a.fd_t = make_fastdiv(a.ty);
   a.fd_m = make_fastdiv(a.g.mz);
+  a.nz_inv = (T)(1.0 / (double)a.g.nz);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.g.mx * nty;
   if (a.g.nz == 256) k_z_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);

@@ -45,6 +45,7 @@ struct XPassArgs {
   int in_mode, out_mode, nin, yt, group, ld;
   // vel_max partials: max_only = 1 leaves the sums to k_parseval (FP32 form)
   int max_only;
+  T fn;  // 1/(2 Nx Ny): xy_trans_f.f:20's scale and the 1/2 of the pair split (launcher)
   // subgrid stress (les = 1): input fields Lu .. Lu+Lr-1 are the gradient
   // fields of the products; nu_t = C delta^2 |S| with C delta^2 read from
   // les_cds, kappa_t = nu_t * les_prt_inv
@@ -98,6 +99,7 @@ struct ZFwdArgs {
   long long u_ky, u_kx, u_n;
   DevState* state;
   StageConsts sc;
+  T nz_inv;                  // filled by the launcher: 1/Nz
   FastDiv fd_n, fd_t, fd_m;  // filled by the launcher: Nz, ty, Nz_min
 };
 
