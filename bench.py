@@ -330,6 +330,28 @@ def ensemble_form(K, W):
             "timing": "host clock around ensemble_step (it synchronises), after warm-up steps"}
 
 
+def run_probe(args):
+    """A short fixed launch sequence for ncu: init, 3 steps (each stage: the
+    five passes), nothing else; --les 3 uses the LES start with the learned
+    closure (network kernel launched once per stage)."""
+    from sam_gb300 import SamGpu, build as B
+    B.build()
+    if args.les:
+        params, _ = closure_params()
+        g = SamGpu(**les_cfg(args.precision))
+        g.init_random(3, 6, 1.0, 6, 0.1)
+        if args.les == 3:
+            g.mlp_set(params)
+        g.set_les(args.les)
+    else:
+        g = SamGpu(**workload_cfg(precision=args.precision))
+        g.init_packet(PACKET["seed"], PACKET["k0"], PACKET["sigma"], PACKET["amplitude"], PACKET["noise"])
+    g.step(3)
+    print(json.dumps({"probe": True, "time": g.stats()["time"], "precision": args.precision, "les": args.les}))
+    g.close()
+    return 0
+
+
 def run_reference(args):
     rank, _, ws = dist_env()
     if rank != 0:
@@ -363,6 +385,10 @@ def main():
     ap.add_argument("--grid", type=int, default=256, help="N of the N^3 box (profiling of smaller cases)")
     ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
                     help="precision of the timed run (32 for profiling the FP32 bulk form)")
+    ap.add_argument("--probe", action="store_true",
+                    help="profiling case: the workload's start state and 3 steps only (no timing, autotune or "
+                         "baselines); with --les 3 the learned-closure LES start")
+    ap.add_argument("--les", type=int, default=0, help="closure model of the --probe run")
     args = ap.parse_args()
     global N, WORKLOAD
     if args.grid != N:
@@ -370,6 +396,8 @@ def main():
         N = args.grid
     if args.impl == "reference":
         return run_reference(args)
+    if args.probe:
+        return run_probe(args)
 
     rank, local_rank, ws = dist_env()
     if ws > 1:

@@ -507,6 +507,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
       s_red[nw * 4 + w] = (double)bad;
     }
     __syncthreads();
+    // one atomic per field and CTA: the max of non-negative floats is the max
+    // of their bit patterns (order-independent, so deterministic)
     if (threadIdx.x < a.g.lu) {
       const int f = threadIdx.x;
       double tm = 0, tb = 0;
@@ -514,8 +516,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
         tm = fmax(tm, s_red[k * 4 + f]);
         tb += s_red[nw * 4 + k];
       }
-      double* dst = a.partials + ((long long)blockIdx.x * a.g.lu + f) * 4;
-      dst[0] = 0.0; dst[1] = 0.0; dst[2] = tm; dst[3] = tb;
+      atomicMax(a.vmax + f, __float_as_int((float)tm));
+      if (f == 0 && tb != 0.0) atomicOr(a.vmax + 4, 1);
     }
     __syncthreads();
   } else if (a.partials) {
@@ -1009,24 +1011,25 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_
 // Parseval sums of vel_max (see launch_parseval): FP64 products of the
 // stored modes, per-thread strided order, block tree, fixed launch shape.
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict__ u, Grid g, FastDiv fd_plane,
-                                                       double* __restrict__ pv) {
+__global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict__ u, Grid g, double* __restrict__ pv) {
   __shared__ double red[4][kThreads];
   const long long nm = (long long)g.mx * g.my * g.mz;
   const int plane = g.my * g.mz;
-  double acc[4] = {0.0, 0.0, 0.0, 0.0};
+  // kx = 0 modes count once, kx > 0 twice (their conjugates): separate sums
+  double acc0[4] = {0.0, 0.0, 0.0, 0.0}, acc1[4] = {0.0, 0.0, 0.0, 0.0};
   for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < nm; m += (long long)gridDim.x * blockDim.x) {
-    const double w = fdiv((uint32_t)m, fd_plane) == 0 ? 1.0 : 2.0;
+    const bool kx0 = m < plane;
 #pragma unroll
     for (int f = 0; f < 4; ++f)
       if (f < g.lu) {
         const cx_t<T> v = u[f * nm + m];
         const double re = (double)v.x, im = (double)v.y;
-        acc[f] = fma(w * re, re, fma(w * im, im, acc[f]));
+        if (kx0) acc0[f] = fma(re, re, fma(im, im, acc0[f]));
+        else acc1[f] = fma(re, re, fma(im, im, acc1[f]));
       }
   }
 #pragma unroll
-  for (int f = 0; f < 4; ++f) red[f][threadIdx.x] = acc[f];
+  for (int f = 0; f < 4; ++f) red[f][threadIdx.x] = acc0[f] + 2.0 * acc1[f];
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s)
@@ -1036,21 +1039,21 @@ __global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict
   }
   if (threadIdx.x < g.lu) pv[(long long)blockIdx.x * g.lu + threadIdx.x] = red[threadIdx.x][0];
   if (blockIdx.x == 0 && threadIdx.x < g.lu) pv[(long long)gridDim.x * g.lu + threadIdx.x] = (double)u[threadIdx.x * nm].x;
-  (void)plane;
 }
 
 template <typename T>
 void launch_parseval(const cx_t<T>* u, const Grid& g, double* pv, cudaStream_t s) {
-  k_parseval<T><<<kParsevalBlocks, kThreads, 0, s>>>(u, g, make_fastdiv((uint32_t)(g.my * g.mz)), pv);
+  k_parseval<T><<<kParsevalBlocks, kThreads, 0, s>>>(u, g, pv);
 }
 template void launch_parseval<float>(const float2*, const Grid&, double*, cudaStream_t);
 template void launch_parseval<double>(const double2*, const Grid&, double*, cudaStream_t);
 
 __global__ void k_vel_max_finish(const double* __restrict__ partials, int nblk, Grid g, DevState* st, int i_cfl,
-                                 double cfl0, double adv_cfl_limit, const double* __restrict__ pv, int npv) {
+                                 double cfl0, double adv_cfl_limit, const double* __restrict__ pv, int npv,
+                                 int* __restrict__ vmax) {
   __shared__ double red[kThreads];
   __shared__ double fin[4][4];
-  for (int f = 0; f < g.lu; ++f) {
+  for (int f = 0; f < g.lu && !pv; ++f) {
     for (int q = 0; q < 4; ++q) {
       double v = 0.0;
       for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
@@ -1083,9 +1086,13 @@ __global__ void k_vel_max_finish(const double* __restrict__ partials, int nblk, 
         const double n = (double)g.nx * (double)g.ny * (double)g.nz;
         fin[f][0] = pv[(long long)npv * g.lu + f] * n;
         fin[f][1] = red[0] * n;
+        fin[f][2] = (double)__int_as_float(vmax[f]);
+        fin[f][3] = (double)vmax[4];
       }
       __syncthreads();
     }
+    __syncthreads();
+    if (threadIdx.x < 8) vmax[threadIdx.x] = 0;  // ready for the next step's maxima
   }
   if (threadIdx.x == 0) {
     const double inv = 1.0 / ((double)g.nx * (double)g.ny * (double)g.nz);
@@ -1194,8 +1201,8 @@ void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   else k_z_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
 }
 void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
-                           double adv_cfl_limit, cudaStream_t s, const double* pv, int npv) {
-  k_vel_max_finish<<<1, kThreads, 0, s>>>(partials, nblk, g, st, i_cfl, cfl0, adv_cfl_limit, pv, npv);
+                           double adv_cfl_limit, cudaStream_t s, const double* pv, int npv, int* vmax) {
+  k_vel_max_finish<<<1, kThreads, 0, s>>>(partials, nblk, g, st, i_cfl, cfl0, adv_cfl_limit, pv, npv, vmax);
 }
 void launch_x2z(const double2* in, double2* out, const Grid& g, int nvar, int nx2, cudaStream_t s) {
   long long total = (long long)g.ny * g.mx * g.nz * nvar;

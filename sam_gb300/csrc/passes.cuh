@@ -45,6 +45,7 @@ struct XPassArgs {
   int in_mode, out_mode, nin, yt, group, ld;
   // vel_max partials: max_only = 1 leaves the sums to k_parseval (FP32 form)
   int max_only;
+  int* vmax;  // max_only: per-field max |u| (float bit patterns) and the NaN flag, atomically
   T fn;  // 1/(2 Nx Ny): xy_trans_f.f:20's scale and the 1/2 of the pair split (launcher)
   // subgrid stress (les = 1): input fields Lu .. Lu+Lr-1 are the gradient
   // fields of the products; nu_t = C delta^2 |S| with C delta^2 read from
@@ -111,7 +112,8 @@ template <typename T> void launch_y_fwd(const YFwdArgs<T>& a, const FftPlan* pl,
 template <typename T> void launch_z_fwd(const ZFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
 template <typename T> void set_smem_limits();
 void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
-                           double adv_cfl_limit, cudaStream_t s, const double* pv = nullptr, int npv = 0);
+                           double adv_cfl_limit, cudaStream_t s, const double* pv = nullptr, int npv = 0,
+                           int* vmax = nullptr);
 // vel_max's sums from wave space (Parseval), FP64 arithmetic on the state U
 // (Lu fields (kx, ky, kz)): pv[b * Lu + f] = block b's share of
 // sum w |u|^2 (w = 1 for kx = 0, 2 otherwise), pv[npv * Lu + f] = u(0,0,0).

@@ -340,12 +340,13 @@ static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in
     // the FP32 form takes vel_max's sums from wave space (Parseval, FP64
     // arithmetic): the x pass then only forms max |u| and the NaN check
     a.max_only = sizeof(T) == 4 && in_mode == 0 && in == c.S2;
+    a.vmax = reinterpret_cast<int*>(c.pv + 4 * ((size_t)kParsevalBlocks + 1));
   }
   launch_x_pass<T>(a, c.px.d, x_smem<T>(c, nin, a.yt, a.group), c.stream);
   if (stats) {
     if (a.max_only) launch_parseval<T>((const cx_t<T>*)c.U, c.g, c.pv, c.stream);
     launch_vel_max_finish(c.partials, nblk, c.g, c.state, c.cfg.i_cfl, c.cfg.cfl0, c.adv_cfl_limit, c.stream,
-                          a.max_only ? c.pv : nullptr, kParsevalBlocks);
+                          a.max_only ? c.pv : nullptr, kParsevalBlocks, a.vmax);
   }
   return 0;
 }
@@ -692,7 +693,8 @@ static int init_ctx(const sam_gpu_config* cfg) {
   // allocation ever happens inside a captured step
   c->partial_blocks = g.nz * g.ny;
   ok = ok && cudaMalloc(&c->partials, sizeof(double) * 4 * 4 * (size_t)c->partial_blocks) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->pv, sizeof(double) * 4 * ((size_t)kParsevalBlocks + 1)) == cudaSuccess;
+  ok = ok && cudaMalloc(&c->pv, sizeof(double) * (4 * ((size_t)kParsevalBlocks + 1) + 4)) == cudaSuccess;
+  if (ok) cudaMemset(c->pv, 0, sizeof(double) * (4 * ((size_t)kParsevalBlocks + 1) + 4));
   if (!ok) { free_ctx(c); g_ctx = nullptr; return fail(SAM_GPU_ECUDA, "device allocation failed"); }
   cudaMemset(c->U, 0, es * g.lu * nzmm);
   cudaMemset(c->R, 0, es * g.lu * nzmm);
