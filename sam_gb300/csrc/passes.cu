@@ -31,12 +31,12 @@ __device__ __forceinline__ void load_twiddles(cx_t<T>* s_tw, const cx_t<T>* __re
 constexpr int kBatch = 8;
 
 // Resident CTAs per SM each kernel's register budget is sized for (measured
-// at 256^3): the transpose passes gain from a third FP32 / second FP64 CTA to
-// cover their load phases; the x pass and the FP32 z_fwd epilogue lose more
-// to the tighter register cap than they gain.
+// at 256^3): in FP32 the transpose passes fit 64 registers (four CTAs) and
+// the x pass 80 (three CTAs) without spills; the FP32 z_fwd epilogue spills
+// below 128 and keeps two; FP64 CTAs are bound by the FP64 pipe.
 enum PassKind { kPassZInv, kPassYInv, kPassX, kPassYFwd, kPassZFwd };
 template <typename T, int K> struct MinBlocks {
-  static constexpr int value = (K == kPassX || K == kPassZFwd) ? 2 : 3;
+  static constexpr int value = K == kPassZFwd ? 2 : (K == kPassX ? 3 : 4);
 };
 template <int K> struct MinBlocks<double, K> {
   static constexpr int value = (K == kPassX) ? 1 : 2;
