@@ -989,15 +989,16 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_
       if (h == 1 && !has1) break;
       const int t = h ? t1 : t0, k = h ? k1 : k0, j = j0 + t;
       const C* ln = s_ln + t * ld + sidx(kpos(k, km, mz, nz));
-      if (sizeof(T) == 4 && i == 0 && j == 0 && k == 0) {
-        // the FP32 form keeps the mean (k = 0) mode in FP64
-        EpiIn<double> ind;
-        epi_load<double>(a, i, j, k, ind);
-        epi_mode<double, T>(a, ln, nl * ld, i, j, k, epi_const<double>(a, dt), ind);
-      } else {
-        epi_mode<T, T>(a, ln, nl * ld, i, j, k, cw, h ? in1 : in0);
-      }
+      // (the FP32 form treats the mean mode in FP64 below)
+      if (sizeof(T) == 8 || i != 0 || j != 0 || k != 0) epi_mode<T, T>(a, ln, nl * ld, i, j, k, cw, h ? in1 : in0);
     }
+  }
+  if (sizeof(T) == 4 && i == 0 && j0 == 0 && threadIdx.x == 0) {
+    // the FP32 form keeps the mean (k = 0) mode in FP64; one thread, outside
+    // the per-mode loop so that no FP64 instruction is issued per mode
+    EpiIn<double> ind;
+    epi_load<double>(a, 0, 0, 0, ind);
+    epi_mode<double, T>(a, s_ln + sidx(kpos(0, km, mz, nz)), nl * ld, 0, 0, 0, epi_const<double>(a, dt), ind);
   }
   if (a.mode == 2 && a.sc.last && blockIdx.x == 0 && threadIdx.x == 0) {
     // sam.f:318 time = time + dt, once per step (no CTA of this launch reads
