@@ -501,23 +501,27 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
       bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
     const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    // (FP32 and integer only: an FP64 conversion here is issued by every warp)
+    float* s_mx = reinterpret_cast<float*>(s_red);
+    int* s_bad = reinterpret_cast<int*>(s_mx + 4 * nw);
     if ((threadIdx.x & 31) == 0) {
 #pragma unroll
-      for (int f = 0; f < 4; ++f) s_red[w * 4 + f] = (double)mx4[f];
-      s_red[nw * 4 + w] = (double)bad;
+      for (int f = 0; f < 4; ++f) s_mx[w * 4 + f] = (float)mx4[f];
+      s_bad[w] = bad;
     }
     __syncthreads();
     // one atomic per field and CTA: the max of non-negative floats is the max
     // of their bit patterns (order-independent, so deterministic)
     if (threadIdx.x < a.g.lu) {
       const int f = threadIdx.x;
-      double tm = 0, tb = 0;
+      float tm = 0.f;
+      int tb = 0;
       for (int k = 0; k < nw; ++k) {
-        tm = fmax(tm, s_red[k * 4 + f]);
-        tb += s_red[nw * 4 + k];
+        tm = fmaxf(tm, s_mx[k * 4 + f]);
+        tb |= s_bad[k];
       }
-      atomicMax(a.vmax + f, __float_as_int((float)tm));
-      if (f == 0 && tb != 0.0) atomicOr(a.vmax + 4, 1);
+      atomicMax(a.vmax + f, __float_as_int(tm));
+      if (f == 0 && tb) atomicOr(a.vmax + 4, 1);
     }
     __syncthreads();
   } else if (a.partials) {
@@ -649,9 +653,10 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
         const int ya = min(y0 + 2 * c, ny - 1), yb = min(y0 + 2 * c + 1, ny - 1);
         const float2 ca = a.les_coef[((long long)z * ny + ya) * nx + x];
         const float2 cb = a.les_coef[((long long)z * ny + yb) * nx + x];
-        const double dsq = a.les_dsq;
-        sgs_point_c<T>(sx, lr, (T)((double)ca.x * dsq), (T)((double)ca.y * dsq));
-        sgs_point_c<T>(sy, lr, (T)((double)cb.x * dsq), (T)((double)cb.y * dsq));
+        // C delta^2 in the working precision (no FP64 per point in FP32)
+        const T dsq = (T)a.les_dsq;
+        sgs_point_c<T>(sx, lr, (T)ca.x * dsq, (T)ca.y * dsq);
+        sgs_point_c<T>(sy, lr, (T)cb.x * dsq, (T)cb.y * dsq);
       } else {
         sgs_point<T>(sx, lr, cds, prt);
         sgs_point<T>(sy, lr, cds, prt);
