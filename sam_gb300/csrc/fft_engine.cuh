@@ -357,9 +357,41 @@ __device__ __forceinline__ void fft256_lines(C* base, int ld, int nlines, const 
 
 // Code paths of the line transforms: kFftAny picks at run time (the plan's
 // length); kFft256 compiles only the 16 x 16 register path (n = 256) and
-// kFftGeneric only the Stockham stages, so a kernel built for one length
-// carries no registers for the other path.
+// kFftGeneric only the Stockham stages with the radix chosen at run time;
+// PATH = n (32, 64, 128, 512) compiles the Stockham stages of that length
+// with their radices fixed at compile time.  A kernel built for one length
+// thus carries no registers for another path.
 constexpr int kFftAny = 0, kFft256 = 1, kFftGeneric = 2;
+
+// The s-th radix of the plan for length n (build_plan's order: 8s, then 4,
+// 2, 3, 5) and the number of stages, at compile time.
+__host__ __device__ constexpr int ct_radix(int n, int s) {
+  int r = n, k = 0;
+  while (r % 8 == 0) { if (k == s) return 8; r /= 8; ++k; }
+  while (r % 4 == 0) { if (k == s) return 4; r /= 4; ++k; }
+  while (r % 2 == 0) { if (k == s) return 2; r /= 2; ++k; }
+  while (r % 3 == 0) { if (k == s) return 3; r /= 3; ++k; }
+  while (r % 5 == 0) { if (k == s) return 5; r /= 5; ++k; }
+  return 0;
+}
+__host__ __device__ constexpr int ct_nst(int n) {
+  int s = 0;
+  while (ct_radix(n, s) != 0) ++s;
+  return s;
+}
+// lengths with a compile-time path
+__host__ __device__ constexpr bool ct_length(int n) { return n == 32 || n == 64 || n == 128 || n == 512; }
+
+// Stages S.. of a compile-time length N on one line; stage 0 reads through first.
+template <int SIGN, int N, int S, typename C, typename First>
+__device__ __forceinline__ void fft_ct_stages(C* line, const C* __restrict__ tw, const FftPlan& pl, int tl, int TW,
+                                              First first) {
+  if constexpr (S < ct_nst(N)) {
+    if constexpr (S == 0) fft_stage<ct_radix(N, 0), SIGN>(line, tw, pl.st[0], N, tl, TW, first);
+    else fft_stage<ct_radix(N, S), SIGN>(line, tw, pl.st[S], N, tl, TW, LineLoad<C>{line});
+    fft_ct_stages<SIGN, N, S + 1>(line, tw, pl, tl, TW, first);
+  }
+}
 
 // Transform `nlines` lines of a CTA's shared-memory tile.  Line L starts at
 // base + L*ld.  Every thread of the CTA must call this with the same plan.
@@ -379,7 +411,12 @@ __device__ __forceinline__ void fft_lines(C* base, int ld, int nlines, const C* 
   for (int r = 0; r < rounds; ++r) {
     const int L = r * nteams + team;
     const bool active = L < nlines;
-    fft_line<SIGN>(base + (active ? L : 0) * ld, tw, pl, tl, active);
+    if constexpr (ct_length(PATH)) {
+      C* line = base + (active ? L : 0) * ld;
+      fft_ct_stages<SIGN, PATH, 0>(line, tw, pl, active ? tl : (1 << 20), TW, LineLoad<C>{line});
+    } else {
+      fft_line<SIGN>(base + (active ? L : 0) * ld, tw, pl, tl, active);
+    }
   }
 }
 
@@ -407,7 +444,11 @@ __device__ __forceinline__ void fft_lines_from(C* base, int ld, int nlines, cons
     const int L = r * nteams + team;
     const bool active = L < nlines;
     const int Lc = active ? L : 0;
-    fft_line_from<SIGN>(base + Lc * ld, tw, pl, tl, active, first(Lc));
+    if constexpr (ct_length(PATH)) {
+      fft_ct_stages<SIGN, PATH, 0>(base + Lc * ld, tw, pl, active ? tl : (1 << 20), TW, first(Lc));
+    } else {
+      fft_line_from<SIGN>(base + Lc * ld, tw, pl, tl, active, first(Lc));
+    }
   }
 }
 

@@ -34,12 +34,15 @@ constexpr int kBatch = 8;
 // at 256^3): in FP32 the transpose passes fit 64 registers (four CTAs) and
 // the x pass 80 (three CTAs) without spills; the FP32 z_fwd epilogue spills
 // below 128 and keeps two; FP64 CTAs are bound by the FP64 pipe.
+// The run-time-radix path (kFftGeneric, lengths without a compile-time
+// path) needs more registers: one x pass CTA per SM, two of the others.
 enum PassKind { kPassZInv, kPassYInv, kPassX, kPassYFwd, kPassZFwd };
-template <typename T, int K> struct MinBlocks {
-  static constexpr int value = K == kPassZFwd ? 2 : (K == kPassX ? 3 : 4);
+template <typename T, int K, int PATH = kFft256> struct MinBlocks {
+  static constexpr int value =
+      PATH == kFftGeneric ? (K == kPassX ? 1 : 2) : (K == kPassZFwd ? 2 : (K == kPassX ? 3 : 4));
 };
-template <int K> struct MinBlocks<double, K> {
-  static constexpr int value = (K == kPassX) ? 1 : 2;
+template <int K, int PATH> struct MinBlocks<double, K, PATH> {
+  static constexpr int value = (K == kPassX || PATH == kFftGeneric) ? 1 : 2;
 };
 template <typename V, typename Get, typename Put>
 __device__ __forceinline__ void batched(int count, Get get, Put put) {
@@ -62,7 +65,7 @@ __device__ __forceinline__ void batched(int count, Get get, Put put) {
 // Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
 // modes; output A(n, z, kx, ky) with ky fastest.
 template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -173,7 +176,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv>::value) k_z_
 // hold either Ny_min compact modes (zero band inserted here, as
 // x2z_decomp.f:111-124 does) or Ny values with the band already present.
 template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv>::value) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -396,7 +399,7 @@ __device__ __forceinline__ void product_pair(int m, int& a, int& b) {
 }
 
 template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX, PATH>::value) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -734,7 +737,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX>::value) k_x_pas
 // Tile: field m, kx column i, planes z0 .. z0+TZ-1.  Output D(m, kx, ky, z)
 // keeps |ky| <= ky_max (xy_trans_f.f:45-52).
 template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd>::value) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -927,7 +930,7 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
 //   mode 1: rhs epilogue (rhs.f:108-142) into r with u_sav from memory,
 //   mode 2: full stage epilogue: rhs, then sam.f:210-221 and 293-314.
 template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd>::value) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -1154,8 +1157,14 @@ void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_t = make_fastdiv(a.ty);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.nvar * a.g.mx * nty;
-  if (a.g.nz == 256) k_z_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
-  else k_z_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  switch (a.g.nz) {
+    case 256: k_z_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 32: k_z_inv<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 64: k_z_inv<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 128: k_z_inv<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 512: k_z_inv<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    default: k_z_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  }
 }
 template <typename T>
 void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
@@ -1164,8 +1173,14 @@ void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_t = make_fastdiv(a.tx);
   const int ntx = (a.g.mx + a.tx - 1) / a.tx;
   const int grid = a.nvar * a.g.nz * ntx;
-  if (a.g.ny == 256) k_y_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
-  else k_y_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  switch (a.g.ny) {
+    case 256: k_y_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 32: k_y_inv<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 64: k_y_inv<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 128: k_y_inv<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 512: k_y_inv<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    default: k_y_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  }
 }
 template <typename T>
 int x_pass_blocks(const XPassArgs<T>& a) {
@@ -1181,8 +1196,14 @@ void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaS
   a.fd_nx = make_fastdiv(a.g.nx);
   a.fd_y = make_fastdiv(a.yt);
   a.fn = (T)(0.5 / ((double)a.g.nx * (double)a.g.ny));
-  if (a.g.nx == 256) k_x_pass<T, kFft256><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
-  else k_x_pass<T, kFftGeneric><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
+  switch (a.g.nx) {
+    case 256: k_x_pass<T, kFft256><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
+    case 32: k_x_pass<T, 32><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
+    case 64: k_x_pass<T, 64><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
+    case 128: k_x_pass<T, 128><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
+    case 512: k_x_pass<T, 512><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
+    default: k_x_pass<T, kFftGeneric><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
+  }
 }
 template <typename T>
 void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
@@ -1191,8 +1212,14 @@ void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.fd_t = make_fastdiv(a.tz);
   const int ntz = (a.g.nz + a.tz - 1) / a.tz;
   const int grid = a.nvar * a.g.mx * ntz;
-  if (a.g.ny == 256) k_y_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
-  else k_y_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  switch (a.g.ny) {
+    case 256: k_y_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 32: k_y_fwd<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 64: k_y_fwd<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 128: k_y_fwd<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 512: k_y_fwd<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    default: k_y_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  }
 }
 template <typename T>
 void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
@@ -1203,8 +1230,14 @@ void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   a.nz_inv = (T)(1.0 / (double)a.g.nz);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.g.mx * nty;
-  if (a.g.nz == 256) k_z_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
-  else k_z_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  switch (a.g.nz) {
+    case 256: k_z_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 32: k_z_fwd<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 64: k_z_fwd<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 128: k_z_fwd<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 512: k_z_fwd<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    default: k_z_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
+  }
 }
 void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
                            double adv_cfl_limit, cudaStream_t s, const double* pv, int npv, int* vmax) {
@@ -1232,15 +1265,35 @@ void set_smem_limits() {
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   allow_dynamic_smem((const void*)k_z_inv<T, kFft256>, optin);
-  allow_dynamic_smem((const void*)k_y_inv<T, kFft256>, optin);
-  allow_dynamic_smem((const void*)k_x_pass<T, kFft256>, optin);
-  allow_dynamic_smem((const void*)k_y_fwd<T, kFft256>, optin);
-  allow_dynamic_smem((const void*)k_z_fwd<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_z_inv<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, 32>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, 64>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, 128>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, 32>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, 64>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, 128>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, 32>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, 64>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, 128>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, 32>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, 64>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, 128>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, kFftGeneric>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, 32>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, 64>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, 128>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, 512>, optin);
 }
 
 #define SAMGPU_INST(T)                                                                           \
