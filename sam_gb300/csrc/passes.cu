@@ -42,7 +42,7 @@ template <typename T, int K, int PATH = kFft256> struct MinBlocks {
       PATH == kFftGeneric ? (K == kPassX ? 1 : 2) : (K == kPassZFwd ? 2 : (K == kPassX ? 3 : 4));
 };
 template <int K, int PATH> struct MinBlocks<double, K, PATH> {
-  static constexpr int value = (K == kPassX || PATH == kFftGeneric) ? 1 : 2;
+  static constexpr int value = PATH == kFftGeneric ? 1 : 2;
 };
 template <typename V, typename Get, typename Put>
 __device__ __forceinline__ void batched(int count, Get get, Put put) {

@@ -274,9 +274,10 @@ static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
   const size_t red = sizeof(double) * 4 * (kThreads / 32) + 64;
   yt = c.yt_x;
   grp = out_mode == 2 ? c.grp_x : 0;
-  // FP32 tiles leave room for three CTAs per SM (80 registers each); FP64
-  // CTAs are bound to one per SM and take the whole budget
-  const size_t budget = sizeof(T) == 4 ? kSmemMax / 3 - 1024 : kSmemMax;
+  // FP32 tiles leave room for three CTAs per SM (80 registers each), FP64
+  // tiles for two (128 registers each): the FP64 pipe needs the second CTA's
+  // warps to cover its dependency latency
+  const size_t budget = sizeof(T) == 4 ? kSmemMax / 3 - 1024 : kSmemMax / 2 - 1024;
   for (;;) {
     const int lines = (nin + grp) * (yt / 2);
     if (tile_smem(c.px, lines, es) + red <= budget) break;
