@@ -29,6 +29,11 @@ GRIDS = [
     # length-256 lines take the 16 x 16 register path: x and y, then z
     dict(nx=256, ny=256, nz=12, i_strat=1),
     dict(nx=16, ny=20, nz=256, i_strat=1),
+    # compile-time radix paths (128, 64, 512) and the longest line (1024)
+    dict(nx=128, ny=64, nz=128, i_strat=1),
+    dict(nx=512, ny=6, nz=10, i_strat=0),
+    dict(nx=12, ny=10, nz=512, i_strat=1),
+    dict(nx=1024, ny=2, nz=6, i_strat=1),
 ]
 
 
@@ -271,3 +276,45 @@ def test_fp32_vel_max_sums_from_wave_space(gpu_lib):
         assert np.abs(s32[key] - s64[key]).max() <= 1e-6 * scale, key
     assert abs(s32["energy"] - s64["energy"]) <= 1e-6 * s64["energy"]
     assert abs(s32["dt"] - s64["dt"]) <= 1e-6 * s64["dt"]
+
+
+@pytest.mark.parametrize("n_dealias", [0, 1, 2])
+def test_dealias_variants(gpu_lib, n_dealias):
+    """The three truncation rules of init.f:49-62 (none, 2/3 in x, y, z;
+    2/3 in y and z only) through full resident steps."""
+    cfg = dict(nx=24, ny=20, nz=30, i_strat=1, n_dealias=n_dealias, vis=5e-3, buoy_fac_z=1.0, lapse=1.0,
+               i_cfl=1, cfl0=0.3)
+    g, o = SamGpu(**cfg), O.Oracle(**cfg)
+    u = o.init_random(5)
+    g.upload(u)
+    r = o.wave(o.d.lr)
+    o.steps(u, r, 5)
+    g.step(5)
+    ug = g.download()
+    for n in range(o.d.lu):
+        assert relerr(ug[..., n], u[..., n]) < TOL_RUN, (n_dealias, n)
+
+
+def test_nonfinite_field_is_reported(gpu_lib):
+    """A NaN planted in the host field before upload: vel_max flags it, the
+    CFL dt is not replaced by a value computed from it, and the call itself
+    still succeeds (the host decides, as stop_on_error.f would)."""
+    for prec in (64, 32):
+        cfg = dict(nx=16, ny=16, nz=16, i_cfl=1, cfl0=0.5, dt0=0.02, precision=prec)
+        g = SamGpu(**cfg)
+        g.init_taylor_green()
+        u = g.download()
+        u[3, 2, 1, 0] = complex(np.nan, 0.0)
+        g.upload(u)
+        g.step(1)
+        st = g.stats()
+        assert st["nonfinite"] == 1, prec
+        assert st["dt"] == 0.02, prec
+        g.close()
+
+
+def test_unsupported_lengths_are_rejected(gpu_lib):
+    from sam_gb300 import SamGpuError
+    for nx, ny, nz in ((14, 16, 16), (16, 22, 16), (16, 16, 2048)):
+        with pytest.raises(SamGpuError, match="EINVAL"):
+            SamGpu(nx=nx, ny=ny, nz=nz)
