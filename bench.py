@@ -188,6 +188,33 @@ def cpu_oracle_rate(n, steps, threads, warm_stages=1):
     return steps / dt, dt
 
 
+def band_errors(u, ref):
+    """Relative L2 error of u against ref per field and per spectral band of
+    the shell index |k| (wave numbers of the 2 pi box): [1, K/4), [K/4, K/2),
+    [K/2, sqrt(3) K] with K = k_max (arrays in the wave layout, Nze rows)."""
+    import numpy as np
+    mx, my, mz = dims()
+    k = (mx - 1)
+    kx = np.arange(mx)
+    ky = np.array([j if j <= k else j - my for j in range(my)])
+    kz = np.array([q if q <= k else q - mz for q in range(mz)])
+    KZ, KY, KX = np.meshgrid(kz, ky, kx, indexing="ij")
+    shell = np.sqrt(KX ** 2 + KY ** 2 + KZ ** 2)
+    w = np.where(KX == 0, 1.0, 2.0)  # conjugate modes of kx > 0
+    edges = [(1, k / 4), (k / 4, k / 2), (k / 2, np.sqrt(3) * k + 1)]
+    out = {}
+    for n in range(u.shape[-1]):
+        d, r = u[:mz, ..., n], ref[:mz, ..., n]
+        row = {}
+        for lo, hi in edges:
+            sel = (shell >= lo) & (shell < hi)
+            num = float((w[sel] * np.abs(d[sel] - r[sel]) ** 2).sum())
+            den = float((w[sel] * np.abs(r[sel]) ** 2).sum())
+            row[f"k{lo:.0f}-{hi:.0f}"] = (num / den) ** 0.5 if den > 0 else None
+        out[f"field{n}"] = row
+    return out
+
+
 def closure_params():
     """The trained closure network (sam_gb300/data/closure_mlp.npz, made by
     python -m sam_gb300.closure_data on the GPU) or, without it, the
@@ -503,10 +530,12 @@ def main():
         prof32 = [g32.profile_stage(nrk, max(2, K // 4)) for nrk in (1, 2, 3)]
         passes32 = {k: sum(p[k] for p in prof32) / 3 for k in prof32[0]}
         err = [float(np.abs(u32[..., n] - u_fp64[..., n]).max() / np.abs(u_fp64[..., n]).max()) for n in range(4)]
+        bands = band_errors(u32, u_fp64)
         g32.close()
         b32 = algorithmic_bytes_per_step(w=4)
         fp32 = {"value": ws * K / (ms32 / 1e3), "unit": "steps/s", "ms_per_step": ms32 / K,
-                "rel_err_vs_fp64_per_field": err, "after_steps": W + K,
+                "rel_err_vs_fp64_per_field": err, "rel_l2_err_vs_fp64_per_field_and_band": bands,
+                "after_steps": W + K,
                 "hbm_gbs": b32 / (ms32 / K / 1e3) / 1e9, "passes_ms": passes32, "tiles": tiles32}
 
     # ---- the LES forms of the same workload: FP64 drop-in with dm.f's
