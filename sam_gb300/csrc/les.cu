@@ -27,10 +27,13 @@ struct Halo {
     return (long long)i + (long long)(nx + 2) * ((long long)j + (long long)(ny + 2) * k);
   }
   __device__ __forceinline__ long long vol() const { return (long long)(nx + 2) * (ny + 2) * (nz + 2); }
-  // interior (periodic) index 0..n-1 of a wrapped coordinate
-  __device__ __forceinline__ int wx(int i) const { return (i % nx + nx) % nx; }
-  __device__ __forceinline__ int wy(int j) const { return (j % ny + ny) % ny; }
-  __device__ __forceinline__ int wz(int k) const { return (k % nz + nz) % nz; }
+  // interior (periodic) index 0..n-1 of a wrapped coordinate; the stencils
+  // reach one point past either side, so a conditional add or subtract
+  // replaces the integer remainder (valid for -n <= i < 2n)
+  __device__ __forceinline__ static int wrap(int i, int n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+  __device__ __forceinline__ int wx(int i) const { return wrap(i, nx); }
+  __device__ __forceinline__ int wy(int j) const { return wrap(j, ny); }
+  __device__ __forceinline__ int wz(int k) const { return wrap(k, nz); }
   __device__ __forceinline__ long long in(int i, int j, int k) const {
     return (long long)wx(i) + (long long)nx * ((long long)wy(j) + (long long)ny * wz(k));
   }
