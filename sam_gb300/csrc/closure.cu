@@ -15,6 +15,8 @@
 // Training: the backward pass of the loss mean (C - y)^2 and Adam run on the
 // CUDA cores in FP32 (the network is small; the weight gradients are
 // per-CTA partial sums reduced in a fixed order, so runs are reproducible).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>
@@ -97,23 +99,39 @@ __device__ __forceinline__ void epilogue(uint32_t tl, const float* __restrict__ 
 
 // Persistent CTAs of 128 threads; thread t owns row t of every tile (its
 // TMEM lane).  Optionally stores the activations for the backward pass.
-__global__ void __launch_bounds__(128, 7) k_mlp_fwd(const __nv_bfloat16* __restrict__ x16, long long n,
+// The input tiles arrive by TMA: a 2-D tensor map over x16 ([n][16] BF16,
+// 32-byte rows) with a box of 8 x 128 (16 bytes x 128 rows), loaded at
+// x = 0 and x = 8, writes the two K halves of a 128 x 16 tile one after the
+// other: element (r, k) at (k/8)*2048 + r*16 + (k%8)*2, the canonical
+// no-swizzle K-major layout with LBO = 2048 B and SBO = 128 B.  Two buffers:
+// the next tile's load runs during this tile's MMA chain.
+__global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUtensorMap xmap, long long n,
                                                  const MlpDev* __restrict__ P, float2* __restrict__ coef,
                                                  __nv_bfloat16* __restrict__ h1g, __nv_bfloat16* __restrict__ h2g,
                                                  float* __restrict__ og, int* err) {
   __shared__ __align__(1024) uint8_t sw1[kMlpH * kMlpK1 * 2];
   __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];
   __shared__ __align__(1024) uint8_t sw3[kMlpN3 * kMlpH * 2];
-  // the input tile (128 x 16) lives in the first 4 KB of the hidden tile:
-  // layer 1's output overwrites it only after its MMA has completed
+  __shared__ __align__(1024) uint8_t sa1[2][kMlpTile * kMlpK1 * 2];
   __shared__ __align__(1024) uint8_t sa2[kMlpTile * kMlpH * 2];
-  uint8_t* sa1 = sa2;
   __shared__ float sb1[kMlpH], sb2[kMlpH], sb3[kMlpN3];
-  __shared__ uint64_t bar;
+  __shared__ uint64_t bar, tbar[2];
   __shared__ uint32_t tbase;
   const int tid = threadIdx.x;
+  const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
+  constexpr uint32_t kTileBytes = kMlpTile * kMlpK1 * 2;
   if (tid < 32) tmem_alloc(&tbase, 64);
-  if (tid == 0) mbar_init(&bar, 1);
+  if (tid == 0) {
+    mbar_init(&bar, 1);
+    mbar_init(&tbar[0], 1);
+    mbar_init(&tbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (blockIdx.x < ntiles) {
+      mbar_expect_tx(&tbar[0], kTileBytes);
+      tma_load_2d(sa1[0], &xmap, 0, (int)(blockIdx.x * kMlpTile), &tbar[0]);
+      tma_load_2d(sa1[0] + kTileBytes / 2, &xmap, 8, (int)(blockIdx.x * kMlpTile), &tbar[0]);
+    }
+  }
   stage_matrix(sw1, P->w1, kMlpH, kMlpK1);
   stage_matrix(sw2, P->w2, kMlpH, kMlpH);
   stage_matrix(sw3, P->w3, kMlpN3, kMlpH);
@@ -128,38 +146,31 @@ __global__ void __launch_bounds__(128, 7) k_mlp_fwd(const __nv_bfloat16* __restr
   tc_fence_after();
   const uint32_t tm = tbase;
   const uint32_t tl = tm + ((uint32_t)(32 * (tid >> 5)) << 16);  // this warp's lanes
-  const uint32_t a1 = smem_u32(sa1), a2 = smem_u32(sa2);
+  const uint32_t a2 = smem_u32(sa2);
   const uint32_t w1 = smem_u32(sw1), w2 = smem_u32(sw2), w3 = smem_u32(sw3);
   const uint32_t id64 = idesc_bf16(kMlpTile, kMlpH), id16 = idesc_bf16(kMlpTile, kMlpN3);
   uint32_t phase = 0;
-  int bad = 0;
-  const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
-  // the inputs of the next tile are loaded while this tile's MMA chain runs
-  auto fetch = [&](long long t, uint4& q0, uint4& q1) {
-    const long long r = t * kMlpTile + tid;
-    q0 = make_uint4(0, 0, 0, 0);
-    q1 = q0;
-    if (t < ntiles && r < n) {
-      const uint4* src = reinterpret_cast<const uint4*>(x16 + r * kMlpK1);
-      q0 = src[0];
-      q1 = src[1];
-    }
-  };
-  uint4 q0, q1;
-  fetch(blockIdx.x, q0, q1);
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
+  int bad = 0, it = 0, pending = -1;  // pending: buffer of a TMA load not yet waited for
+  if (blockIdx.x < ntiles) pending = 0;
+  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
     const long long row = t * kMlpTile + tid;
     const bool live = row < n;
-    *reinterpret_cast<uint4*>(sa1 + kmaj(tid, 0, kMlpK1)) = q0;
-    *reinterpret_cast<uint4*>(sa1 + kmaj(tid, 8, kMlpK1)) = q1;
-    fetch(t + gridDim.x, q0, q1);
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
+    const int b = it & 1;
+    // the next tile's load into the other buffer (its previous MMA is done)
+    const long long tn = t + gridDim.x;
+    if (tid == 0 && tn < ntiles) {
+      mbar_expect_tx(&tbar[b ^ 1], kTileBytes);
+      tma_load_2d(sa1[b ^ 1], &xmap, 0, (int)(tn * kMlpTile), &tbar[b ^ 1]);
+      tma_load_2d(sa1[b ^ 1] + kTileBytes / 2, &xmap, 8, (int)(tn * kMlpTile), &tbar[b ^ 1]);
+    }
+    bad = mbar_wait(&tbar[b], (uint32_t)((it >> 1) & 1));
+    pending = tn < ntiles ? (b ^ 1) : -1;
+    if (__syncthreads_or(bad)) break;
+    const uint32_t a1 = smem_u32(sa1[b]);
     // layer 1: D = X W1^T (K = 16)
     if (tid == 0) {
-      mma_bf16(tm, sdesc(a1, 128, 256), sdesc(w1, 128, 256), id64, 0);
+      tc_fence_after();
+      mma_bf16(tm, sdesc(a1, 2048, 128), sdesc(w1, 128, 256), id64, 0);
       mma_commit(&bar);
     }
     bad = mbar_wait(&bar, phase);
@@ -215,6 +226,8 @@ __global__ void __launch_bounds__(128, 7) k_mlp_fwd(const __nv_bfloat16* __restr
     tc_fence_after();
   }
   if (bad && tid == 0) atomicExch(err, 1);
+  // a load still in flight (the loop left early) completes before exit
+  if (pending >= 0 && tid == 0) mbar_wait(&tbar[pending], (uint32_t)(((it + 1) >> 1) & 1));
   tc_fence_before();
   __syncthreads();
   if (tid < 32) {
@@ -223,14 +236,42 @@ __global__ void __launch_bounds__(128, 7) k_mlp_fwd(const __nv_bfloat16* __restr
   }
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against libcuda); the map of x16 as [n][16] BF16 with 8 x 128 boxes
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    cudaDriverEntryPointQueryResult q;
+    void* p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+static bool x16_map(const __nv_bfloat16* x16, long long n, CUtensorMap* m) {
+  PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+  if (!enc || (reinterpret_cast<uintptr_t>(x16) & 15)) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)kMlpK1, (cuuint64_t)n};
+  const cuuint64_t strides[1] = {(cuuint64_t)kMlpK1 * 2};
+  const cuuint32_t box[2] = {8, (cuuint32_t)kMlpTile};
+  const cuuint32_t estr[2] = {1, 1};
+  return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(x16), dims, strides, box, estr,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2* coef, const MlpBatch* batch,
                 int* err, cudaStream_t s) {
   const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
-  long long grid = 152 * 7;  // 28.7 KB of shared memory and 64 TMEM columns per CTA
+  long long grid = 152 * 6;  // 37 KB of shared memory and 64 TMEM columns per CTA
   if (grid > ntiles) grid = ntiles;
   if (grid < 1) return 0;
-  k_mlp_fwd<<<(int)grid, kMlpTile, 0, s>>>(x16, n, dev, coef, batch ? batch->h1 : nullptr,
-                                           batch ? batch->h2 : nullptr, batch ? batch->o : nullptr, err);
+  CUtensorMap m;
+  if (!x16_map(x16, n, &m)) return -1;
+  k_mlp_fwd<<<(int)grid, kMlpTile, 0, s>>>(m, n, dev, coef, batch ? batch->h1 : nullptr, batch ? batch->h2 : nullptr,
+                                           batch ? batch->o : nullptr, err);
   return (int)grid;
 }
 

@@ -45,9 +45,10 @@ struct MlpBatch {
 
 // params (FP32, kMlpParams) -> the BF16 device form
 void mlp_pack(const float* params, MlpDev* dev, cudaStream_t s);
-// x16: [n][16] BF16 inputs; coef: [n] (C_nu, C_kappa); batch (may be null)
-// receives the activations for the backward pass; err is set on a wait
-// timeout.  Returns the number of CTAs launched.
+// x16: [n][16] BF16 inputs (16-byte aligned; loaded by TMA); coef: [n]
+// (C_nu, C_kappa); batch (may be null) receives the activations for the
+// backward pass; err is set on a wait timeout.  Returns the number of CTAs
+// launched, or -1 when the tensor map cannot be built (nothing launched).
 int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2* coef, const MlpBatch* batch,
                 int* err, cudaStream_t s);
 // Gradient of L = mean over points and both outputs of (C - y)^2, written

@@ -444,8 +444,9 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
     rc = run_x_pass<T>(c, 0, 4, g.lr + 3, (const cx_t<T>*)c.S2 + g.lu * bn, nullptr, g.mx, (long long)g.ny * g.mx,
                        bn, nullptr, nullptr, 0, 0, 0, 0, 0, 0, false);
     if (rc) return rc;
-    mlp_forward((const __nv_bfloat16*)c.les_feat, (long long)g.nx * g.ny * g.nz, c.mlp_dev, c.les_coef, nullptr,
-                c.mlp_err, c.stream);
+    if (mlp_forward((const __nv_bfloat16*)c.les_feat, (long long)g.nx * g.ny * g.nz, c.mlp_dev, c.les_coef,
+                    nullptr, c.mlp_err, c.stream) < 0)
+      return fail(SAM_GPU_ECUDA, "closure network: no TMA tensor map (cuTensorMapEncodeTiled unavailable)");
   }
   // x pass: B -> C(m, z, kx, y) with vel_max at nrk = 1
   if (run(2))
@@ -1269,7 +1270,8 @@ int sam_gpu_mlp_forward(const float* feat, long long n, float* coef) {
   if (rc) return rc;
   __nv_bfloat16* x16;
   if ((rc = mlp_stage_inputs(c, feat, n, &x16)) || (rc = ensure(c.sc[1], sizeof(float2) * (size_t)n))) return rc;
-  mlp_forward(x16, n, c.mlp_dev, (float2*)c.sc[1].p, nullptr, c.mlp_err, c.stream);
+  if (mlp_forward(x16, n, c.mlp_dev, (float2*)c.sc[1].p, nullptr, c.mlp_err, c.stream) < 0)
+    return fail(SAM_GPU_ECUDA, "closure network: no TMA tensor map");
   CK(cudaMemcpyAsync(coef, c.sc[1].p, sizeof(float2) * (size_t)n, cudaMemcpyDeviceToHost, c.stream));
   return mlp_check_err(c);
 }
@@ -1311,7 +1313,8 @@ int sam_gpu_mlp_grad(const float* feat, const float* target, long long n, float*
   MlpWork w;
   if ((rc = mlp_stage_inputs(c, feat, n, &x16)) || (rc = mlp_work(c, n, w))) return rc;
   CK(cudaMemcpyAsync(w.y, target, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, c.stream));
-  mlp_forward(x16, n, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream);
+  if (mlp_forward(x16, n, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream) < 0)
+    return fail(SAM_GPU_ECUDA, "closure network: no TMA tensor map");
   mlp_backward(x16, w.y, n, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss, c.stream);
   CK(cudaMemcpyAsync(grad, c.mlp_g, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, c.stream));
   float ls = 0.f;
@@ -1341,7 +1344,8 @@ int sam_gpu_mlp_train(const float* feat, const float* target, long long n, int s
   std::vector<float> hist((size_t)steps);
   for (int s = 0; s < steps; ++s) {
     const long long off = (s % nchunks) * nb;
-    mlp_forward(x16 + off * kMlpK1, nb, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream);
+    if (mlp_forward(x16 + off * kMlpK1, nb, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream) < 0)
+      return fail(SAM_GPU_ECUDA, "closure network: no TMA tensor map");
     mlp_backward(x16 + off * kMlpK1, y_all + off, nb, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss + 0, c.stream);
     mlp_adam(c.mlp_p, c.mlp_m, c.mlp_v, c.mlp_g, ++c.mlp_step, lr, c.mlp_dev, c.stream);
     if (loss_hist) CK(cudaMemcpyAsync(&hist[s], c.mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, c.stream));
