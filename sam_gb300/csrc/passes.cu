@@ -61,6 +61,25 @@ __device__ __forceinline__ void batched(int count, Get get, Put put) {
   }
 }
 
+// First-stage loader reading element idx of a row in global memory.
+template <typename C> struct RowLoad {
+  const C* __restrict__ row;
+  __device__ __forceinline__ C operator()(int idx) const { return row[idx]; }
+};
+
+// First-stage loader of a row of stored modes 0..k, then -k..-1, padded to
+// the transform length: idx <= lo from row[idx], idx >= hi from
+// row[idx - gap], the band between as zero.
+template <typename C> struct BandRowLoad {
+  const C* __restrict__ row;
+  int lo, hi, gap;
+  __device__ __forceinline__ C operator()(int idx) const {
+    if (idx <= lo) return row[idx];
+    if (idx >= hi) return row[idx - gap];
+    return mk<C>((decltype(C::x))0, (decltype(C::x))0);
+  }
+};
+
 // --------------------------------------------------------------- z inverse
 // Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
 // modes; output A(n, z, kx, ky) with ky fastest.
@@ -88,17 +107,10 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
     const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
     s_ln[t * ld + sidx(p)] = v;
   };
-  if (!a.derive || n < a.g.lu) {
-    batched<C>(
-        nl * nz,
-        [&](int e) {
-          const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
-          C v = mk<C>((T)0, (T)0);
-          if (p <= km) v = src[(long long)t * a.in_ky + p];
-          else if (p >= nz - km) v = src[(long long)t * a.in_ky + p - (nz - mz)];
-          return v;
-        },
-        put);
+  const bool direct = !a.derive || n < a.g.lu;
+  if (direct) {
+    // the first stage reads the stored modes straight from the row, the
+    // truncated band as zero (no shared-memory staging)
   } else {
     // gradient field m of the subgrid stress: S_ab = (i/2)(k_b u_a + k_a u_b)
     // (i k_a u_a when a = b) for the six velocity products in rhs.f's order,
@@ -156,7 +168,11 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
         put);
   }
   __syncthreads();
-  fft_lines<+1, PATH>(s_ln, ld, nl, s_tw, pl);
+  if (direct)
+    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl,
+                             [&](int L) { return BandRowLoad<C>{src + (long long)L * a.in_ky, km, nz - km, nz - mz}; });
+  else
+    fft_lines<+1, PATH>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)i * a.out_kx + j0;
   batched<C>(
@@ -195,22 +211,14 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
   const int nl = min(a.tx, mx - i0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
   const C* src = a.in + (long long)n * a.in_n + (long long)z * a.in_z + (long long)i0 * a.in_kx;
-  batched<C>(
-      nl * ny,
-      [&](int e) {
-        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
-        C v = mk<C>((T)0, (T)0);
-        if (a.in_full) v = src[(long long)t * a.in_kx + p];
-        else if (p <= km) v = src[(long long)t * a.in_kx + p];
-        else if (p >= ny - km) v = src[(long long)t * a.in_kx + p - (ny - my)];
-        return v;
-      },
-      [&](int e, C v) {
-        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
-        s_ln[t * ld + sidx(p)] = v;
-      });
   __syncthreads();
-  fft_lines<+1, PATH>(s_ln, ld, nl, s_tw, pl);
+  // the first stage reads the rows straight from memory: all Ny values
+  // (in_full) or the stored modes with the truncated band as zero
+  if (a.in_full)
+    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl, [&](int L) { return RowLoad<C>{src + (long long)L * a.in_kx}; });
+  else
+    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl,
+                             [&](int L) { return BandRowLoad<C>{src + (long long)L * a.in_kx, km, ny - km, ny - my}; });
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)z * a.out_z + i0;
   batched<C>(
@@ -756,18 +764,11 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
   const int nl = min(a.tz, nz - z0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
   const C* src = a.in + (long long)m * a.in_n + (long long)i * a.in_kx + (long long)z0 * a.in_z;
-  batched<C>(
-      nl * ny,
-      [&](int e) {
-        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
-        return src[(long long)t * a.in_z + p];
-      },
-      [&](int e, C v) {
-        const int t = (int)fdiv(e, a.fd_n), p = e - t * ny;
-        s_ln[t * ld + sidx(p)] = v;
-      });
   __syncthreads();
-  fft_lines<-1, PATH>(s_ln, ld, nl, s_tw, pl);
+  // the first stage reads its inputs straight from the rows of C (no
+  // shared-memory staging); the rows are contiguous in y
+  fft_lines_from<-1, PATH>(s_ln, ld, nl, s_tw, pl,
+                           [&](int L) { return RowLoad<C>{src + (long long)L * a.in_z}; });
   __syncthreads();
   C* dst = a.out + (long long)m * a.out_n + (long long)i * a.out_kx + z0;
   batched<C>(
@@ -947,22 +948,13 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
   const int j0 = jt * a.ty;
   const int nl = min(a.ty, my - j0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_total);
-  // lines of all nf fields for the nl rows of this tile, packed as f * nl + t
-  batched<C>(
-      nf * a.ty * nz,
-      [&](int e) {
-        const int r = (int)fdiv(e, a.fd_n), p = e - r * nz;
-        const int f = (int)fdiv(r, a.fd_t), t = r - f * a.ty;
-        return t < nl ? a.in[(long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky + p]
-                      : mk<C>((T)0, (T)0);
-      },
-      [&](int e, C v) {
-        const int r = (int)fdiv(e, a.fd_n), p = e - r * nz;
-        const int f = (int)fdiv(r, a.fd_t), t = r - f * a.ty;
-        if (t < nl) s_ln[(f * nl + t) * ld + sidx(p)] = v;
-      });
+  // lines of all nf fields for the nl rows of this tile, packed as f * nl + t;
+  // the first stage reads the z-contiguous rows of D straight from memory
   __syncthreads();
-  fft_lines<-1, PATH>(s_ln, ld, nf * nl, s_tw, pl);
+  fft_lines_from<-1, PATH>(s_ln, ld, nf * nl, s_tw, pl, [&](int L) {
+    const int f = L / nl, t = L - f * nl;
+    return RowLoad<C>{a.in + (long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky};
+  });
   __syncthreads();
   const T nz_inv = a.nz_inv;
   if (a.mode == 0) {
