@@ -51,6 +51,7 @@ struct FftPlan {
   int team;     // threads per line in FP64 (at most 8 values per thread)
   int team_sp;  // threads per line in FP32 (at most 8 values per thread)
   int tw16_off; // n == 256: offset of the 16 x 16 table w_256^{f q} (else -1)
+  int tw_pass;  // twiddles the pass kernels load: the 16 x 16 table (at 0) for n = 256, else all
   FftStage st[10];
 };
 
@@ -67,9 +68,10 @@ __device__ __forceinline__ int div_m(int b, const FftStage& s) { return (int)(((
 // elements, so the stride-16 row reads of the 16 x 16 path (and the strided
 // reads of late Stockham stages) fall in distinct banks.
 __host__ __device__ __forceinline__ int sidx(int p) { return p + (p >> 4); }
-// Stride between consecutive lines (odd, so lines start in rotating banks).
+// Stride between consecutive lines: room for sidx(n - 1), rounded up to odd
+// so lines start in rotating banks.
 __host__ __device__ __forceinline__ int line_stride(int n) {
-  const int s = n + (n >> 4) + 1;
+  const int s = n + ((n - 1) >> 4);
   return s | 1;
 }
 

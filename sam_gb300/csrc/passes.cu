@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_total;
+  C* s_ln = s_tw + pl.tw_pass;
   const int nz = a.g.nz, mz = a.g.mz, km = a.g.kz, my = a.g.my;
   const int ld = a.ld;
   const int nty = (my + a.ty - 1) / a.ty;
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   const int n = b;
   const int j0 = jt * a.ty;
   const int nl = min(a.ty, my - j0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
   const C* src = a.in + (long long)n * a.in_n + (long long)i * a.in_kx + (long long)j0 * a.in_ky;
   auto put = [&](int e, C v) {
     const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_total;
+  C* s_ln = s_tw + pl.tw_pass;
   const int ny = a.g.ny, my = a.g.my, km = a.g.ky, mx = a.g.mx;
   const int ld = a.ld;
   const int ntx = (mx + a.tx - 1) / a.tx;
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
   const int n = b;
   const int i0 = it * a.tx;
   const int nl = min(a.tx, mx - i0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
   const C* src = a.in + (long long)n * a.in_n + (long long)z * a.in_z + (long long)i0 * a.in_kx;
   __syncthreads();
   // the first stage reads the rows straight from memory: all Ny values
@@ -407,25 +407,28 @@ __device__ __forceinline__ void product_pair(int m, int& a, int& b) {
 }
 
 template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX, PATH>::value) k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
+__global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256 ? 256 : 0), MinBlocks<T, kPassX, PATH>::value)
+    k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_in = s_tw + pl.tw_total;                  // nin * yp lines
+  C* s_in = s_tw + pl.tw_pass;                  // nin * yp lines
   const int nx = a.g.nx, ny = a.g.ny, kmx = a.g.kx, mx = a.g.mx;
   const int Y = a.yt, yp = Y / 2, ld = a.ld;
   const int nin = a.nin;
-  C* s_pr = s_in + nin * yp * ld;                // group * yp product lines
-  double* s_red = reinterpret_cast<double*>(s_pr + a.group * yp * ld);  // reduction scratch
+  C* s_pr = s_in + nin * yp * ld;                // group product lines
+  // vel_max's reduction scratch shares the product lines' space (it is done
+  // before the first product is formed)
+  double* s_red = reinterpret_cast<double*>(s_pr);
   const int nyt = (ny + Y - 1) / Y;
   const int yt = blockIdx.x % nyt;
   const int z = blockIdx.x / nyt;
   const int y0 = yt * Y;
   const int yv = min(Y, ny - y0);  // valid rows in the tile
-  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
 
   // ---- build the input lines
   if (a.in_mode == 0) {
@@ -433,6 +436,9 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX, PATH>::value) k
     // (the truncated band kx_max < p < Nx - kx_max is never stored: the
     // transform's first stage reads it as zero)
     // element e -> line L = (f, c) and kx; loads the two rows of the pair
+    // (staged through shared memory: reading the rows inside the first FFT
+    // stage instead measured slower here, the batched loads keep more of
+    // them in flight)
     struct Pair { C x, y; };
     batched<Pair>(
         nin * yp * mx,
@@ -695,47 +701,59 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassX, PATH>::value) k
     return;
   }
   const T fn = a.fn;  // 1/(Nx Ny) (xy_trans_f.f:20) and the 1/2 of the split
-  const int nout = a.out_mode == 1 ? nin : a.g.lr;
-  // out_mode 1 transforms the input lines in place, all at once; out_mode 2
-  // forms the products `group` fields at a time (group >= 1 by construction)
-  const int gstep = a.out_mode == 1 ? nin : max(a.group, 1);
-  for (int m0 = 0; m0 < nout; m0 += gstep) {
-    const int gm = min(gstep, nout - m0);
-    // out_mode 1: the input lines in place; out_mode 2 (rhs.f:46-60): the
-    // products of the physical lines, formed while the first FFT stage loads
-    // them, straight into the product lines
-    C* lines = a.out_mode == 1 ? s_in + m0 * yp * ld : s_pr;
-    fft_lines_from<-1, PATH>(lines, ld, gm * yp, s_tw, pl, [&](int L) {
+  // output line q = m * Y/2 + c: pair c of output field m.  out_mode 1
+  // transforms the input lines in place, all at once; out_mode 2 forms the
+  // products `group` lines at a time (group >= 1 by construction)
+  const int nlo = (a.out_mode == 1 ? nin : a.g.lr) * yp;
+  const int gstep = a.out_mode == 1 ? nlo : max(a.group, 1);
+  for (int l0 = 0; l0 < nlo; l0 += gstep) {
+    const int gl = min(gstep, nlo - l0);
+    // out_mode 2 (rhs.f:46-60): the products of the physical lines, formed
+    // while the first FFT stage loads them, straight into the product lines
+    C* lines = a.out_mode == 1 ? s_in : s_pr;
+    fft_lines_from<-1, PATH>(lines, ld, gl, s_tw, pl, [&](int L) {
       if (a.out_mode == 1) return ProductLoad<C>{lines + L * ld, nullptr, nullptr};
-      const int gi = L / yp, c = L - gi * yp;
+      const int q = l0 + L;
+      const int m = (int)fdiv(q, a.fd_yp), c = q - m * yp;
       int fa, fb;
-      product_pair(m0 + gi, fa, fb);
-      const C* gl = a.les ? s_in + ((a.g.lu + m0 + gi) * yp + c) * ld : nullptr;
-      return ProductLoad<C>{s_in + (fa * yp + c) * ld, s_in + (fb * yp + c) * ld, gl};
+      product_pair(m, fa, fb);
+      const C* gl_ = a.les ? s_in + ((a.g.lu + m) * yp + c) * ld : nullptr;
+      return ProductLoad<C>{s_in + (fa * yp + c) * ld, s_in + (fb * yp + c) * ld, gl_};
     });
     __syncthreads();
     // split the two real transforms, keep kx <= kx_max, scale, store
-    // C(m, z, kx, y): one thread writes the two rows y0+2c, y0+2c+1 of a pair
-    C* out_z = a.out + (long long)z * a.out_z + y0;
-    for (int e = threadIdx.x; e < gm * mx * yp; e += blockDim.x) {
-      const int r = (int)fdiv(e, a.fd_yp), c = e - r * yp;
-      const int gi = (int)fdiv(r, a.fd_mx), kx = r - gi * mx;
-      const C* ln = lines + (gi * yp + c) * ld;
-      const C z1 = ln[sidx(kx)];
-      const C z2 = ln[sidx(kx == 0 ? 0 : nx - kx)];
-      const C ve = mk<C>((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
-      const C vo = mk<C>((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
-      C* o = out_z + (long long)(m0 + gi) * a.out_n + (unsigned)kx * (unsigned)a.out_kx + 2 * c;
-      if (2 * c + 1 < yv) {
-        if ((reinterpret_cast<uintptr_t>(o) & (2 * sizeof(C) - 1)) == 0) {
-          store_pair(o, ve, vo);
-        } else {  // odd Ny: the pair straddles a vector boundary
-          o[0] = ve;
-          o[1] = vo;
+    // C(m, z, kx, y): a thread keeps one line (the rows y0+2c, y0+2c+1 of
+    // field m) and steps through kx with running pointers; consecutive
+    // threads take consecutive lines (rows, then fields) of one kx
+    {
+      const int span = min(gstep, (int)blockDim.x);
+      const int lanes = (int)blockDim.x / span;
+      const int lane = (int)threadIdx.x / span;
+      const long long ostep = (long long)lanes * a.out_kx;
+      if (lane < lanes)
+        for (int L = (int)threadIdx.x - lane * span; L < gl; L += span) {
+          const int q = l0 + L;
+          const int m = (int)fdiv(q, a.fd_yp), c = q - m * yp;
+          const C* ln = lines + L * ld;
+          C* o = a.out + (long long)z * a.out_z + y0 + (long long)m * a.out_n + (long long)lane * a.out_kx + 2 * c;
+          const bool two = 2 * c + 1 < yv, one = 2 * c < yv;
+          for (int kx = lane; kx < mx; kx += lanes, o += ostep) {
+            const C z1 = ln[sidx(kx)];
+            const C z2 = ln[sidx(kx == 0 ? 0 : nx - kx)];
+            const C ve = mk<C>((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
+            const C vo = mk<C>((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
+            if (two) {
+              if ((reinterpret_cast<uintptr_t>(o) & (2 * sizeof(C) - 1)) == 0) {
+                store_pair(o, ve, vo);
+              } else {  // odd Ny: the pair straddles a vector boundary
+                o[0] = ve;
+                o[1] = vo;
+              }
+            } else if (one) {
+              o[0] = ve;
+            }
+          }
         }
-      } else if (2 * c < yv) {
-        o[0] = ve;
-      }
     }
     __syncthreads();
   }
@@ -752,7 +770,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_total;
+  C* s_ln = s_tw + pl.tw_pass;
   const int ny = a.g.ny, my = a.g.my, km = a.g.ky, nz = a.g.nz;
   const int ld = a.ld;
   const int ntz = (nz + a.tz - 1) / a.tz;
@@ -762,7 +780,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
   const int m = b;
   const int z0 = zt * a.tz;
   const int nl = min(a.tz, nz - z0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
   const C* src = a.in + (long long)m * a.in_n + (long long)i * a.in_kx + (long long)z0 * a.in_z;
   __syncthreads();
   // the first stage reads its inputs straight from the rows of C (no
@@ -938,7 +956,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_total;
+  C* s_ln = s_tw + pl.tw_pass;
   const Grid& g = a.g;
   const int nz = g.nz, mz = g.mz, km = g.kz, my = g.my;
   const int ld = a.ld, nf = a.nf;
@@ -947,7 +965,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
   const int i = blockIdx.x / nty;
   const int j0 = jt * a.ty;
   const int nl = min(a.ty, my - j0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_total);
+  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
   // lines of all nf fields for the nl rows of this tile, packed as f * nl + t;
   // the first stage reads the z-contiguous rows of D straight from memory
   __syncthreads();
@@ -1181,15 +1199,13 @@ int x_pass_blocks(const XPassArgs<T>& a) {
 template <typename T>
 void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
   XPassArgs<T> a = a0;
-  const int nband = a.g.nx - 2 * a.g.kx - 1;
-  a.fd_band = make_fastdiv(nband > 0 ? nband : 1);
   a.fd_mx = make_fastdiv(a.g.mx);
   a.fd_yp = make_fastdiv(a.yt / 2);
   a.fd_nx = make_fastdiv(a.g.nx);
   a.fd_y = make_fastdiv(a.yt);
   a.fn = (T)(0.5 / ((double)a.g.nx * (double)a.g.ny));
   switch (a.g.nx) {
-    case 256: k_x_pass<T, kFft256><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
+    case 256: k_x_pass<T, kFft256><<<x_pass_blocks(a), x_threads(sizeof(T), 256), smem, s>>>(a, pl); break;
     case 32: k_x_pass<T, 32><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     case 64: k_x_pass<T, 64><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     case 128: k_x_pass<T, 128><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;

@@ -33,6 +33,12 @@ struct YInvArgs {
   FastDiv fd_n, fd_t;  // filled by the launcher: Ny, tx
 };
 
+// Threads of an x pass CTA.  In the FP32 n = 256 path a team of 16 threads
+// transforms one line, and an 8-row tile holds 4 x 4 input and 9 x 4 product
+// lines: 18 teams do them in one and two full rounds (16 teams would need a
+// third round a quarter full).  Other forms keep kThreads.
+__host__ __device__ constexpr int x_threads(int bytes, int n) { return bytes == 4 && n == 256 ? 288 : kThreads; }
+
 template <typename T>
 struct XPassArgs {
   Grid g;
@@ -42,6 +48,8 @@ struct XPassArgs {
   T* out_phys;         // out_mode 0: P(n, z, y, x)
   double* partials;    // vel_max partials (nblocks, lu, 4) or null
   const cx_t<T>* tw;
+  // group: product lines transformed per round of out_mode 2 (a multiple of
+  // the CTA's teams where it exceeds them), any split of the Lr * Y/2 lines
   int in_mode, out_mode, nin, yt, group, ld;
   // vel_max partials: max_only = 1 leaves the sums to k_parseval (FP32 form)
   int max_only;
@@ -67,7 +75,7 @@ struct XPassArgs {
   long long in_y, in_z, in_n;
   long long out_kx, out_z, out_n;
   long long out_py, out_pz, out_pn;
-  FastDiv fd_band, fd_mx, fd_yp, fd_nx, fd_y;  // filled by the launcher
+  FastDiv fd_mx, fd_yp, fd_nx, fd_y;  // filled by the launcher
 };
 
 template <typename T>

@@ -9,6 +9,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <initializer_list>
 #include <string>
 #include <vector>
@@ -86,6 +87,21 @@ static int build_plan(int n, Plan& P) {
   std::vector<float2> t32;
   int l = 1, off = 0;
   const long double two_pi = 6.283185307179586476925286766559005768L;
+  pl.tw16_off = -1;
+  if (n == 256) {
+    // the 16 x 16 register path (fft256_lines): w_256^{f q}, f, q in [0, 16),
+    // stored q-major so the 16 threads of a team read 16 consecutive entries;
+    // first in the table, so that kernels compiled for that path load only it
+    pl.tw16_off = 0;
+    for (int q = 0; q < 16; ++q)
+      for (int f = 0; f < 16; ++f) {
+        const long double a = two_pi * (long double)((f * q) % 256) / 256.0L;
+        const long double c = cosl(a), sn = -sinl(a);
+        t64.push_back(make_double2((double)c, (double)sn));
+        t32.push_back(make_float2((float)c, (float)sn));
+      }
+    off = 256;
+  }
   for (int s = 0; s < ns; ++s) {
     const int p = fac[s];
     FftStage& st = pl.st[s];
@@ -105,21 +121,8 @@ static int build_plan(int n, Plan& P) {
     off += l * (p - 1);
     l *= p;
   }
-  pl.tw16_off = -1;
-  if (n == 256) {
-    // the 16 x 16 register path (fft256_lines): w_256^{f q}, f, q in [0, 16),
-    // stored q-major so the 16 threads of a team read 16 consecutive entries
-    pl.tw16_off = off;
-    for (int q = 0; q < 16; ++q)
-      for (int f = 0; f < 16; ++f) {
-        const long double a = two_pi * (long double)((f * q) % 256) / 256.0L;
-        const long double c = cosl(a), sn = -sinl(a);
-        t64.push_back(make_double2((double)c, (double)sn));
-        t32.push_back(make_float2((float)c, (float)sn));
-      }
-    off += 256;
-  }
   pl.tw_total = off;
+  pl.tw_pass = n == 256 ? 256 : off;
   if (t64.empty()) { t64.push_back(make_double2(1, 0)); t32.push_back(make_float2(1, 0)); }
   CK(cudaMalloc(&P.d, sizeof(FftPlan)));
   CK(cudaMemcpy(P.d, &pl, sizeof(FftPlan), cudaMemcpyHostToDevice));
@@ -218,7 +221,7 @@ static int line_ld(int n) { return line_stride(n); }
 
 // shared memory of a tile of `lines` lines of length n plus the twiddles
 static size_t tile_smem(const Plan& P, int lines, size_t es) {
-  return es * ((size_t)P.h.tw_total + (size_t)lines * line_ld(P.h.n)) + 16;
+  return es * ((size_t)P.h.tw_pass + (size_t)lines * line_ld(P.h.n)) + 16;
 }
 
 // dynamic shared memory budget of one CTA: the opt-in limit (227 KB on
@@ -268,29 +271,51 @@ static int run_y_inv(Ctx& c, const void* in, void* out, int nvar, int in_full, l
   return 0;
 }
 
+// lines the reduction scratch of vel_max occupies (FP64 partials of each warp)
+template <typename T>
+static int x_red_lines(const Ctx& c) {
+  const size_t red = sizeof(double) * 4 * (x_threads((int)sizeof(T), c.g.nx) / 32) + 64;
+  const size_t line = sizeof(cx_t<T>) * (size_t)line_ld(c.g.nx);
+  return (int)((red + line - 1) / line);
+}
+
+// x pass tile: yt rows (yt/2 input lines per field) and `grp` product lines
+// per round of out_mode 2.  c.grp_x caps the round at that many product
+// fields; the round then takes as many lines as fit, in whole rounds of the
+// CTA's teams where it exceeds them.  vel_max's reduction scratch shares the
+// product lines' space (at least x_red_lines lines are allocated).
 template <typename T>
 static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
   const size_t es = sizeof(cx_t<T>);
-  const size_t red = sizeof(double) * 4 * (kThreads / 32) + 64;
-  yt = c.yt_x;
-  grp = out_mode == 2 ? c.grp_x : 0;
+  const int threads = x_threads((int)sizeof(T), c.g.nx);
+  const int team = c.g.nx == 256 ? 16 : (sizeof(T) == 4 ? c.px.h.team_sp : c.px.h.team);
+  const int teams = threads / team > 0 ? threads / team : 1;
   // FP32 tiles leave room for three CTAs per SM (80 registers each), FP64
   // tiles for two (128 registers each): the FP64 pipe needs the second CTA's
   // warps to cover its dependency latency
   const size_t budget = sizeof(T) == 4 ? kSmemMax / 3 - 1024 : kSmemMax / 2 - 1024;
-  for (;;) {
-    const int lines = (nin + grp) * (yt / 2);
-    if (tile_smem(c.px, lines, es) + red <= budget) break;
-    if (grp > 1) { grp = (grp + 1) / 2; continue; }
-    if (yt > 2) { yt /= 2; continue; }
-    return fail(SAM_GPU_EINVAL, "x pass does not fit in shared memory (Nx=%d)", c.g.nx);
+  const size_t line = es * (size_t)line_ld(c.g.nx);
+  const size_t rmin = line * (size_t)x_red_lines<T>(c);
+  for (yt = c.yt_x;; yt /= 2) {
+    const int yp = yt / 2;
+    const size_t base = tile_smem(c.px, nin * yp, es);
+    if (out_mode != 2) {
+      grp = 0;
+      if (base + rmin <= budget) return 0;
+    } else if (base + rmin <= budget) {
+      const int fit = (int)((budget - base) / line);
+      const int total = c.g.lr * yp;
+      grp = std::min(std::min(fit, std::max(c.grp_x, 1) * yp), total);
+      if (grp > teams && grp < total) grp -= grp % teams;
+      return 0;
+    }
+    if (yt <= 2) return fail(SAM_GPU_EINVAL, "x pass does not fit in shared memory (Nx=%d)", c.g.nx);
   }
-  return 0;
 }
 
 template <typename T>
 static size_t x_smem(Ctx& c, int nin, int yt, int grp) {
-  return tile_smem(c.px, (nin + grp) * (yt / 2), sizeof(cx_t<T>)) + sizeof(double) * 4 * (kThreads / 32) + 64;
+  return tile_smem(c.px, nin * (yt / 2) + std::max(grp, x_red_lines<T>(c)), sizeof(cx_t<T>));
 }
 
 template <typename T>
