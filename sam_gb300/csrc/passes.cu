@@ -435,33 +435,75 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256 ? 256 : 0
     // spectral rows of B(n, z, y, kx): Hermitian half spectra with kx <= kx_max
     // (the truncated band kx_max < p < Nx - kx_max is never stored: the
     // transform's first stage reads it as zero)
-    // element e -> line L = (f, c) and kx; loads the two rows of the pair
-    // (staged through shared memory: reading the rows inside the first FFT
-    // stage instead measured slower here, the batched loads keep more of
-    // them in flight)
-    struct Pair { C x, y; };
-    batched<Pair>(
-        nin * yp * mx,
-        [&](int e) {
-          const int L = (int)fdiv(e, a.fd_mx), kx = e - L * mx;
-          const int f = (int)fdiv(L, a.fd_yp), c = L - f * yp;
-          const int ya = y0 + 2 * c, yb = ya + 1;
-          const C* src = a.in + (long long)f * a.in_n + (long long)z * a.in_z;
-          Pair q;
-          q.x = ya < ny ? src[(long long)ya * a.in_y + kx] : mk<C>((T)0, (T)0);
-          q.y = yb < ny ? src[(long long)yb * a.in_y + kx] : mk<C>((T)0, (T)0);
-          return q;
-        },
-        [&](int e, Pair q) {
-          const int L = (int)fdiv(e, a.fd_mx), kx = e - L * mx;
-          C X = q.x, Yv = q.y;
-          if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
-            X.y = (T)0;
-            Yv.y = (T)0;
+    // FP32: a thread keeps one kx (consecutive threads: consecutive kx of a
+    // row) and takes the lines L = lane + u * lanes, u < kBatch: all loads of
+    // the batch (two rows per line) are issued before the first store.  (In
+    // FP64, 256 threads over Mx = 86 leave a third idle: measured slower
+    // there, so FP64 keeps the element-wise batches.)
+    if constexpr (sizeof(T) == 4) {
+      const int nl = nin * yp;
+      const int kspan = min(mx, (int)blockDim.x);
+      const int lanes = (int)blockDim.x / kspan;
+      const int lane = (int)threadIdx.x / kspan;
+      if (lane < lanes)
+        for (int kx = (int)threadIdx.x - lane * kspan; kx < mx; kx += kspan) {
+          const C* src0 = a.in + (long long)z * a.in_z + kx;
+          const int sa = sidx(kx), sb = sidx(kx == 0 ? 0 : nx - kx);
+          for (int L0 = lane; L0 < nl; L0 += kBatch * lanes) {
+            C X[kBatch], Yv[kBatch];
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+              const int L = L0 + u * lanes;
+              X[u] = mk<C>((T)0, (T)0);
+              Yv[u] = mk<C>((T)0, (T)0);
+              if (L < nl) {
+                const int f = (int)fdiv(L, a.fd_yp), c = L - f * yp;
+                const int ya = y0 + 2 * c;
+                const C* src = src0 + (long long)f * a.in_n + (long long)ya * a.in_y;
+                if (ya < ny) X[u] = src[0];
+                if (ya + 1 < ny) Yv[u] = src[a.in_y];
+              }
+            }
+#pragma unroll
+            for (int u = 0; u < kBatch; ++u) {
+              const int L = L0 + u * lanes;
+              if (L < nl) {
+                if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
+                  X[u].y = (T)0;
+                  Yv[u].y = (T)0;
+                }
+                s_in[L * ld + sa] = mk<C>(X[u].x - Yv[u].y, X[u].y + Yv[u].x);
+                if (kx > 0) s_in[L * ld + sb] = mk<C>(X[u].x + Yv[u].y, Yv[u].x - X[u].y);
+              }
+            }
           }
-          s_in[L * ld + sidx(kx)] = mk<C>(X.x - Yv.y, X.y + Yv.x);
-          if (kx > 0) s_in[L * ld + sidx(nx - kx)] = mk<C>(X.x + Yv.y, Yv.x - X.y);
-        });
+        }
+    } else {
+      // element e -> line L = (f, c) and kx; loads the two rows of the pair
+      struct Pair { C x, y; };
+      batched<Pair>(
+          nin * yp * mx,
+          [&](int e) {
+            const int L = (int)fdiv(e, a.fd_mx), kx = e - L * mx;
+            const int f = (int)fdiv(L, a.fd_yp), c = L - f * yp;
+            const int ya = y0 + 2 * c, yb = ya + 1;
+            const C* src = a.in + (long long)f * a.in_n + (long long)z * a.in_z;
+            Pair q;
+            q.x = ya < ny ? src[(long long)ya * a.in_y + kx] : mk<C>((T)0, (T)0);
+            q.y = yb < ny ? src[(long long)yb * a.in_y + kx] : mk<C>((T)0, (T)0);
+            return q;
+          },
+          [&](int e, Pair q) {
+            const int L = (int)fdiv(e, a.fd_mx), kx = e - L * mx;
+            C X = q.x, Yv = q.y;
+            if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
+              X.y = (T)0;
+              Yv.y = (T)0;
+            }
+            s_in[L * ld + sidx(kx)] = mk<C>(X.x - Yv.y, X.y + Yv.x);
+            if (kx > 0) s_in[L * ld + sidx(nx - kx)] = mk<C>(X.x + Yv.y, Yv.x - X.y);
+          });
+    }
     __syncthreads();
     fft_lines_from<+1, PATH>(s_in, ld, nin * yp, s_tw, pl,
                        [&](int L) { return BandLoad<C>{s_in + L * ld, kmx, nx - kmx}; });
