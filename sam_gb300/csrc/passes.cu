@@ -80,6 +80,34 @@ template <typename C> struct BandRowLoad {
   }
 };
 
+// First-stage loader of a subgrid gradient field in k_z_inv: element p of
+// the z line is i (alpha u_a + beta u_b) at the stored mode of p (zero in
+// the truncated band), alpha = a0 + a1 kz and beta = b0 + b1 kz with kz the
+// wave number of p; rb is null when beta = 0.
+template <typename C> struct DeriveLoad {
+  const C* __restrict__ ra;
+  const C* __restrict__ rb;
+  decltype(C::x) a0, a1, b0, b1;
+  int km, nz, gap;
+  __device__ __forceinline__ C operator()(int p) const {
+    using T = decltype(C::x);
+    if (p > km && p < nz - km) return mk<C>((T)0, (T)0);
+    const bool lo = p <= km;
+    const int q = lo ? p : p - gap;
+    const T kz = (T)(lo ? p : p - nz);
+    const C ua = ra[q];
+    const T al = a0 + a1 * kz;
+    T zr = al * ua.x, zi = al * ua.y;
+    if (rb) {
+      const C ub = rb[q];
+      const T be = b0 + b1 * kz;
+      zr += be * ub.x;
+      zi += be * ub.y;
+    }
+    return mk<C>(-zi, zr);
+  }
+};
+
 // --------------------------------------------------------------- z inverse
 // Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
 // modes; output A(n, z, kx, ky) with ky fastest.
@@ -103,20 +131,19 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   const int nl = min(a.ty, my - j0);
   load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
   const C* src = a.in + (long long)n * a.in_n + (long long)i * a.in_kx + (long long)j0 * a.in_ky;
-  auto put = [&](int e, C v) {
-    const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
-    s_ln[t * ld + sidx(p)] = v;
-  };
-  const bool direct = !a.derive || n < a.g.lu;
-  if (direct) {
+  __syncthreads();
+  if (!a.derive || n < a.g.lu) {
     // the first stage reads the stored modes straight from the row, the
     // truncated band as zero (no shared-memory staging)
+    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl,
+                             [&](int L) { return BandRowLoad<C>{src + (long long)L * a.in_ky, km, nz - km, nz - mz}; });
   } else {
     // gradient field m of the subgrid stress: S_ab = (i/2)(k_b u_a + k_a u_b)
     // (i k_a u_a when a = b) for the six velocity products in rhs.f's order,
     // i k_a T for the three buoyancy products
     // (fields m >= Lr: the vorticity w_a = i (k_b u_c - k_c u_b), (a, b, c)
-    // cyclic, which only the learned closure's invariants use)
+    // cyclic, which only the learned closure's invariants use); formed from
+    // the rows of u_a and u_b while the first stage loads them
     const int m = n - a.g.lu;
     const bool vort = m >= a.g.lr;
     int fa, fb;
@@ -133,46 +160,33 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
     const long long off = (long long)i * a.in_kx + (long long)j0 * a.in_ky;
     const C* srca = a.in + (long long)(vort || m < 6 ? fa : 3) * a.in_n + off;
     const C* srcb = a.in + (long long)(vort || m < 6 ? fb : 3) * a.in_n + off;
-    const T kxv = (T)a.g.wave_x * (T)i;
-    batched<C>(
-        nl * nz,
-        [&](int e) {
-          const int t = (int)fdiv(e, a.fd_n), p = e - t * nz;
-          C v = mk<C>((T)0, (T)0);
-          int q = -1;
-          if (p <= km) q = p;
-          else if (p >= nz - km) q = p - (nz - mz);
-          if (q >= 0) {
-            const T kv[3] = {kxv, (T)a.g.wave_y * (T)kwave(j0 + t, a.g.ky, my), (T)a.g.wave_z * (T)kwave(q, km, mz)};
-            const C ua = srca[(long long)t * a.in_ky + q];
-            if (vort) {
-              const C ub = srcb[(long long)t * a.in_ky + q];
-              const T kb = (T)kv[fb], kc = (T)kv[fa];  // w_a = i (k_b u_c - k_c u_b)
-              const T zr = kb * ua.x - kc * ub.x, zi = kb * ua.y - kc * ub.y;
-              v = mk<C>(-zi, zr);
-            } else if (m >= 6) {
-              const T k = (T)kv[fa];
-              v = mk<C>(-k * ua.y, k * ua.x);
-            } else if (fa == fb) {
-              const T k = (T)kv[fa];
-              v = mk<C>(-k * ua.y, k * ua.x);
-            } else {
-              const C ub = srcb[(long long)t * a.in_ky + q];
-              const T ka = (T)kv[fa], kb = (T)kv[fb];
-              const T zr = kb * ua.x + ka * ub.x, zi = kb * ua.y + ka * ub.y;
-              v = mk<C>((T)-0.5 * zi, (T)0.5 * zr);
-            }
-          }
-          return v;
-        },
-        put);
+    // alpha multiplies u_a, beta u_b: wave-number component and scale of each
+    int da, db;
+    T sa, sb;
+    if (vort) {
+      da = fb; sa = (T)1; db = fa; sb = (T)-1;
+    } else if (m >= 6 || fa == fb) {
+      da = fa; sa = (T)1; db = -1; sb = (T)0;
+    } else {
+      da = fb; sa = (T)0.5; db = fa; sb = (T)0.5;
+    }
+    const T kxv = (T)a.g.wave_x * (T)i, wz = (T)a.g.wave_z;
+    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl, [&](int L) {
+      const T kyv = (T)a.g.wave_y * (T)kwave(j0 + L, a.g.ky, my);
+      const T kfix = da == 0 ? kxv : kyv, kfixb = db == 0 ? kxv : kyv;
+      DeriveLoad<C> d;
+      d.ra = srca + (long long)L * a.in_ky;
+      d.rb = db >= 0 ? srcb + (long long)L * a.in_ky : nullptr;
+      d.a0 = da < 2 ? sa * kfix : (T)0;
+      d.a1 = da < 2 ? (T)0 : sa * wz;
+      d.b0 = db >= 0 && db < 2 ? sb * kfixb : (T)0;
+      d.b1 = db == 2 ? sb * wz : (T)0;
+      d.km = km;
+      d.nz = nz;
+      d.gap = nz - mz;
+      return d;
+    });
   }
-  __syncthreads();
-  if (direct)
-    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl,
-                             [&](int L) { return BandRowLoad<C>{src + (long long)L * a.in_ky, km, nz - km, nz - mz}; });
-  else
-    fft_lines<+1, PATH>(s_ln, ld, nl, s_tw, pl);
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)i * a.out_kx + j0;
   batched<C>(
@@ -1205,7 +1219,6 @@ __global__ void k_x2z(const double2* __restrict__ in, double2* __restrict__ out,
 template <typename T>
 void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
   ZInvArgs<T> a = a0;
-  a.fd_n = make_fastdiv(a.g.nz);
   a.fd_t = make_fastdiv(a.ty);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.nvar * a.g.mx * nty;

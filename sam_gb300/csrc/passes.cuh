@@ -18,7 +18,7 @@ struct ZInvArgs {
   int derive;
   long long in_ky, in_kx, in_n;
   long long out_kx, out_z, out_n;
-  FastDiv fd_n, fd_t;  // filled by the launcher: Nz, ty
+  FastDiv fd_t;  // filled by the launcher: ty
 };
 
 template <typename T>
