@@ -77,22 +77,29 @@ void mlp_mma_selftest(const __nv_bfloat16* a, const __nv_bfloat16* b, float* d, 
 
 // ------------------------------------------------------------ forward pass
 // One hidden layer's epilogue for this thread's row: TMEM -> +bias, ReLU ->
-// BF16 K-major operand tile (and, when hg is given, the activations).
+// BF16 K-major operand tile (and, when hg is given, the activations).  The
+// bias is added as FP32 pairs; the ReLU is the conversion's (cvt.relu).
 __device__ __forceinline__ void epilogue(uint32_t tl, const float* __restrict__ bias, uint8_t* tile, int r,
                                          __nv_bfloat16* __restrict__ hg, long long row, bool live) {
 #pragma unroll
-  for (int c0 = 0; c0 < kMlpH; c0 += 16) {
-    float h[16];
-    tmem_ld16(tl + (uint32_t)c0, h);
+  for (int c0 = 0; c0 < kMlpH; c0 += 32) {
+    float h[32];
+    tmem_ld32(tl + (uint32_t)c0, h);
+    uint32_t q[16];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) h[k] = fmaxf(h[k] + bias[c0 + k], 0.f);
-    st_row8(tile, r, c0, kMlpH, h);
-    st_row8(tile, r, c0 + 8, kMlpH, h + 8);
+    for (int k = 0; k < 16; ++k) {
+      const float2 b2 = reinterpret_cast<const float2*>(bias + c0)[k];
+      const float2 v = add_f32x2(make_float2(h[2 * k], h[2 * k + 1]), b2);
+      q[k] = pack_relu_bf16(v.x, v.y);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      *reinterpret_cast<uint4*>(tile + kmaj(r, c0 + 8 * j, kMlpH)) =
+          make_uint4(q[4 * j], q[4 * j + 1], q[4 * j + 2], q[4 * j + 3]);
     if (hg && live) {
       uint4* dst = reinterpret_cast<uint4*>(hg + row * kMlpH + c0);
-      dst[0] = make_uint4(pack_bf16(h[0], h[1]), pack_bf16(h[2], h[3]), pack_bf16(h[4], h[5]), pack_bf16(h[6], h[7]));
-      dst[1] = make_uint4(pack_bf16(h[8], h[9]), pack_bf16(h[10], h[11]), pack_bf16(h[12], h[13]),
-                          pack_bf16(h[14], h[15]));
+#pragma unroll
+      for (int j = 0; j < 4; ++j) dst[j] = make_uint4(q[4 * j], q[4 * j + 1], q[4 * j + 2], q[4 * j + 3]);
     }
   }
 }
@@ -114,7 +121,7 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
   __shared__ __align__(1024) uint8_t sw3[kMlpN3 * kMlpH * 2];
   __shared__ __align__(1024) uint8_t sa1[2][kMlpTile * kMlpK1 * 2];
   __shared__ __align__(1024) uint8_t sa2[kMlpTile * kMlpH * 2];
-  __shared__ float sb1[kMlpH], sb2[kMlpH], sb3[kMlpN3];
+  __shared__ __align__(16) float sb1[kMlpH], sb2[kMlpH], sb3[kMlpN3];
   __shared__ uint64_t bar, tbar[2];
   __shared__ uint32_t tbase;
   const int tid = threadIdx.x;
@@ -211,8 +218,8 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
     phase ^= 1;
     tc_fence_after();
     if (__syncthreads_or(bad)) break;
-    float o[16];
-    tmem_ld16(tl, o);
+    float o[2];
+    tmem_ld2(tl, o);
     if (live) {
       const float o0 = o[0] + sb3[0], o1 = o[1] + sb3[1];
       coef[row] = make_float2(kMlpScale * softplus(o0), kMlpScale * softplus(o1));
