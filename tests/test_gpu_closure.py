@@ -34,12 +34,16 @@ def test_mma_known_answer(gpu_lib, ctx):
     assert np.array_equal(d, CL.bf16(b).T[np.arange(128) % 16])
 
 
-def test_forward_matches_oracle(gpu_lib, ctx):
+# 1000 points: 8 tiles, not a multiple of the 128-point tile; 850: 7 tiles
+# (the last pair of tiles has one); 200037: 1563 tiles, so that CTAs of the
+# persistent grid take several pairs
+@pytest.mark.parametrize("npts", [1000, 850, 200037])
+def test_forward_matches_oracle(gpu_lib, ctx, npts):
     rng = np.random.default_rng(1)
     p = CL.init_params(2)
     p[CL.OFF_W3:CL.OFF_B3] *= 10
     p[CL.OFF_B1:CL.OFF_W2] = 0.1 * rng.standard_normal(CL.N_H)
-    x = rng.standard_normal((1000, CL.N_IN)).astype(np.float32)  # not a multiple of the 128-point tile
+    x = rng.standard_normal((npts, CL.N_IN)).astype(np.float32)
     ctx.mlp_set(p)
     assert np.array_equal(ctx.mlp_get(), p)
     got = ctx.mlp_forward(x)
