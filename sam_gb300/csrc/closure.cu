@@ -170,9 +170,12 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
       tma_load_2d(sa1[b ^ 1], &xmap, 0, (int)(tn * kMlpTile), &tbar[b ^ 1]);
       tma_load_2d(sa1[b ^ 1] + kTileBytes / 2, &xmap, 8, (int)(tn * kMlpTile), &tbar[b ^ 1]);
     }
-    bad = mbar_wait(&tbar[b], (uint32_t)((it >> 1) & 1));
+    // one thread polls each barrier; the others wait at the CTA barrier
+    // (bad is then the same in every thread)
+    bad = tid == 0 ? mbar_wait(&tbar[b], (uint32_t)((it >> 1) & 1)) : 0;
     pending = tn < ntiles ? (b ^ 1) : -1;
-    if (__syncthreads_or(bad)) break;
+    bad = __syncthreads_or(bad);
+    if (bad) break;
     const uint32_t a1 = smem_u32(sa1[b]);
     // layer 1: D = X W1^T (K = 16)
     if (tid == 0) {
@@ -180,10 +183,11 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
       mma_bf16(tm, sdesc(a1, 2048, 128), sdesc(w1, 128, 256), id64, 0);
       mma_commit(&bar);
     }
-    bad = mbar_wait(&bar, phase);
+    bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
     phase ^= 1;
+    bad = __syncthreads_or(bad);
     tc_fence_after();
-    if (__syncthreads_or(bad)) break;
+    if (bad) break;
     // epilogue in chunks of 16 columns: bias, ReLU, BF16 into the next
     // operand tile (and the activations for the backward pass)
     epilogue(tl, sb1, sa2, tid, h1g, row, live);
@@ -198,10 +202,11 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
         mma_bf16(tm, sdesc(a2 + 256 * kk, 128, 1024), sdesc(w2 + 256 * kk, 128, 1024), id64, kk > 0);
       mma_commit(&bar);
     }
-    bad = mbar_wait(&bar, phase);
+    bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
     phase ^= 1;
+    bad = __syncthreads_or(bad);
     tc_fence_after();
-    if (__syncthreads_or(bad)) break;
+    if (bad) break;
     epilogue(tl, sb2, sa2, tid, h2g, row, live);
     fence_async_smem();
     tc_fence_before();
@@ -214,10 +219,11 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
         mma_bf16(tm, sdesc(a2 + 256 * kk, 128, 1024), sdesc(w3 + 256 * kk, 128, 1024), id16, kk > 0);
       mma_commit(&bar);
     }
-    bad = mbar_wait(&bar, phase);
+    bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
     phase ^= 1;
+    bad = __syncthreads_or(bad);
     tc_fence_after();
-    if (__syncthreads_or(bad)) break;
+    if (bad) break;
     float o[2];
     tmem_ld2(tl, o);
     if (live) {
