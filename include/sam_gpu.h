@@ -266,8 +266,9 @@ int sam_gpu_mlp_train(const float* features, const float* target, long long n, i
  * by f): out(Nx/f, Ny/f, Nz/f, Lu+Lr) holds the block means of u, v, w, [T],
  * then of the products u_a u_b (rhs.f:49-54 order) and [u_a T].
  * sam_gpu_closure_inputs: the invariants the learned closure sees for the
- * resident field, feat[(z Ny + y) Nx + x][16] as BF16 bit patterns (12
- * used), and grads(Nx, Ny, Nz, Lr+3) the physical S (6, product order),
+ * resident field, feat[(z Ny + y) Nx + x][16] as BF16 bit patterns (the
+ * 12 invariants, then 1.0 three times: the network's bias inputs, then 0),
+ * and grads(Nx, Ny, Nz, Lr+3) the physical S (6, product order),
  * [dT/dx_a (3)] and vorticity (3) they are formed from; either may be NULL. */
 int sam_gpu_box_filter(int f, double* out);
 int sam_gpu_closure_inputs(unsigned short* feat, double* grads);

@@ -76,25 +76,22 @@ void mlp_mma_selftest(const __nv_bfloat16* a, const __nv_bfloat16* b, float* d, 
 }
 
 // ------------------------------------------------------------ forward pass
-// One hidden layer's epilogue for this thread's row: TMEM -> +bias, ReLU ->
-// BF16 K-major operand tile (and, when hg is given, the activations).  The
-// bias is added as FP32 pairs; the ReLU is the conversion's (cvt.relu).
-__device__ __forceinline__ void epilogue(uint32_t tl, const float* __restrict__ bias, uint8_t* tile, int r,
-                                         __nv_bfloat16* __restrict__ hg, long long row, bool live) {
+// One hidden layer's epilogue for this thread's row: TMEM (the bias is
+// already in the accumulator) -> ReLU -> BF16 K-major operand tile columns
+// 0..63 (and, when hg is given, the activations); the ReLU is the
+// conversion's (cvt.relu).
+__device__ __forceinline__ void epilogue(uint32_t tl, uint8_t* tile, int r, __nv_bfloat16* __restrict__ hg,
+                                         long long row, bool live) {
 #pragma unroll
   for (int c0 = 0; c0 < kMlpH; c0 += 32) {
     float h[32];
     tmem_ld32(tl + (uint32_t)c0, h);
     uint32_t q[16];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      const float2 b2 = reinterpret_cast<const float2*>(bias + c0)[k];
-      const float2 v = add_f32x2(make_float2(h[2 * k], h[2 * k + 1]), b2);
-      q[k] = pack_relu_bf16(v.x, v.y);
-    }
+    for (int k = 0; k < 16; ++k) q[k] = pack_relu_bf16(h[2 * k], h[2 * k + 1]);
 #pragma unroll
     for (int j = 0; j < 4; ++j)
-      *reinterpret_cast<uint4*>(tile + kmaj(r, c0 + 8 * j, kMlpH)) =
+      *reinterpret_cast<uint4*>(tile + kmaj(r, c0 + 8 * j, kMlpK2)) =
           make_uint4(q[4 * j], q[4 * j + 1], q[4 * j + 2], q[4 * j + 3]);
     if (hg && live) {
       uint4* dst = reinterpret_cast<uint4*>(hg + row * kMlpH + c0);
@@ -111,17 +108,19 @@ __device__ __forceinline__ void epilogue(uint32_t tl, const float* __restrict__ 
 // x = 0 and x = 8, writes the two K halves of a 128 x 16 tile one after the
 // other: element (r, k) at (k/8)*2048 + r*16 + (k%8)*2, the canonical
 // no-swizzle K-major layout with LBO = 2048 B and SBO = 128 B.  Two buffers:
-// the next tile's load runs during this tile's MMA chain.
-__global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUtensorMap xmap, long long n,
+// the next tile's load runs during this tile's MMA chain.  The hidden
+// operand tile is 128 x 80: columns 64..66 hold 1.0 (the bias inputs of
+// layers 2 and 3), 67..79 zero, written once.
+constexpr int kMlpFwdCtas = 5;  // per SM: 43 KB of shared memory, 64 TMEM columns each
+__global__ void __launch_bounds__(128, kMlpFwdCtas) k_mlp_fwd(const __grid_constant__ CUtensorMap xmap, long long n,
                                                  const MlpDev* __restrict__ P, float2* __restrict__ coef,
                                                  __nv_bfloat16* __restrict__ h1g, __nv_bfloat16* __restrict__ h2g,
                                                  float* __restrict__ og, int* err) {
   __shared__ __align__(1024) uint8_t sw1[kMlpH * kMlpK1 * 2];
-  __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpH * 2];
-  __shared__ __align__(1024) uint8_t sw3[kMlpN3 * kMlpH * 2];
+  __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpK2 * 2];
+  __shared__ __align__(1024) uint8_t sw3[kMlpN3 * kMlpK2 * 2];
   __shared__ __align__(1024) uint8_t sa1[2][kMlpTile * kMlpK1 * 2];
-  __shared__ __align__(1024) uint8_t sa2[kMlpTile * kMlpH * 2];
-  __shared__ __align__(16) float sb1[kMlpH], sb2[kMlpH], sb3[kMlpN3];
+  __shared__ __align__(1024) uint8_t sa2[kMlpTile * kMlpK2 * 2];
   __shared__ uint64_t bar, tbar[2];
   __shared__ uint32_t tbase;
   const int tid = threadIdx.x;
@@ -140,13 +139,14 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
     }
   }
   stage_matrix(sw1, P->w1, kMlpH, kMlpK1);
-  stage_matrix(sw2, P->w2, kMlpH, kMlpH);
-  stage_matrix(sw3, P->w3, kMlpN3, kMlpH);
-  if (tid < kMlpH) {
-    sb1[tid] = P->b1[tid];
-    sb2[tid] = P->b2[tid];
+  stage_matrix(sw2, P->w2, kMlpH, kMlpK2);
+  stage_matrix(sw3, P->w3, kMlpN3, kMlpK2);
+  {
+    // the constant columns of this thread's row of the hidden operand tile
+    const uint32_t one = 0x3F80u;  // 1.0 in BF16
+    *reinterpret_cast<uint4*>(sa2 + kmaj(tid, kMlpH, kMlpK2)) = make_uint4(one | (one << 16), one, 0u, 0u);
+    *reinterpret_cast<uint4*>(sa2 + kmaj(tid, kMlpH + 8, kMlpK2)) = make_uint4(0u, 0u, 0u, 0u);
   }
-  if (tid < kMlpN3) sb3[tid] = P->b3[tid];
   fence_async_smem();
   tc_fence_before();
   __syncthreads();
@@ -190,16 +190,17 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
     if (bad) break;
     // epilogue in chunks of 16 columns: bias, ReLU, BF16 into the next
     // operand tile (and the activations for the backward pass)
-    epilogue(tl, sb1, sa2, tid, h1g, row, live);
+    epilogue(tl, sa2, tid, h1g, row, live);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    // layer 2: D = H1 W2^T (K = 64 as four K = 16 steps)
+    // layer 2: D = H1 W2^T (K = 80 as five K = 16 steps, the last with the
+    // bias columns)
     if (tid == 0) {
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, 1024), sdesc(w2 + 256 * kk, 128, 1024), id64, kk > 0);
+      for (int kk = 0; kk < kMlpK2 / 16; ++kk)
+        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w2 + 256 * kk, 128, kMlpK2 * 16), id64, kk > 0);
       mma_commit(&bar);
     }
     bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
@@ -207,16 +208,16 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
     bad = __syncthreads_or(bad);
     tc_fence_after();
     if (bad) break;
-    epilogue(tl, sb2, sa2, tid, h2g, row, live);
+    epilogue(tl, sa2, tid, h2g, row, live);
     fence_async_smem();
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
-    // layer 3: D = H2 W3^T (N = 16, two rows used)
+    // layer 3: D = H2 W3^T (N = 16, two rows used; K = 80 as for layer 2)
     if (tid == 0) {
 #pragma unroll
-      for (int kk = 0; kk < 4; ++kk)
-        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, 1024), sdesc(w3 + 256 * kk, 128, 1024), id16, kk > 0);
+      for (int kk = 0; kk < kMlpK2 / 16; ++kk)
+        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w3 + 256 * kk, 128, kMlpK2 * 16), id16, kk > 0);
       mma_commit(&bar);
     }
     bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
@@ -227,7 +228,7 @@ __global__ void __launch_bounds__(128, 6) k_mlp_fwd(const __grid_constant__ CUte
     float o[2];
     tmem_ld2(tl, o);
     if (live) {
-      const float o0 = o[0] + sb3[0], o1 = o[1] + sb3[1];
+      const float o0 = o[0], o1 = o[1];
       coef[row] = make_float2(kMlpScale * softplus(o0), kMlpScale * softplus(o1));
       if (og) {
         og[2 * row] = o0;
@@ -278,7 +279,7 @@ static bool x16_map(const __nv_bfloat16* x16, long long n, CUtensorMap* m) {
 int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2* coef, const MlpBatch* batch,
                 int* err, cudaStream_t s) {
   const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
-  long long grid = 152 * 6;  // 37 KB of shared memory and 64 TMEM columns per CTA
+  long long grid = 152 * kMlpFwdCtas;  // persistent: one wave
   if (grid > ntiles) grid = ntiles;
   if (grid < 1) return 0;
   CUtensorMap m;
@@ -289,26 +290,40 @@ int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2
 }
 
 // -------------------------------------------------------------- parameters
+// part j (0, 1, 2) of the exact split of b into three BF16 values:
+// b = hi + mid + lo, each part the nearest BF16 of what the previous left
+__device__ __forceinline__ __nv_bfloat16 bias_part(float b, int j) {
+  __nv_bfloat16 h = __float2bfloat16_rn(b);
+  for (int i = 0; i < j; ++i) {
+    b -= __bfloat162float(h);
+    h = __float2bfloat16_rn(b);
+  }
+  return h;
+}
+
 __global__ void k_mlp_pack(const float* __restrict__ p, MlpDev* __restrict__ d) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const __nv_bfloat16 z = __float2bfloat16_rn(0.f);
   if (i < kMlpH * kMlpK1) {
     const int r = i / kMlpK1, k = i - r * kMlpK1;
-    d->w1[i] = __float2bfloat16_rn(k < kMlpIn ? p[kMlpOffW1 + r * kMlpIn + k] : 0.f);
+    d->w1[i] = k < kMlpIn ? __float2bfloat16_rn(p[kMlpOffW1 + r * kMlpIn + k])
+                          : (k < kMlpOne + 3 ? bias_part(p[kMlpOffB1 + r], k - kMlpOne) : z);
   }
-  if (i < kMlpH * kMlpH) d->w2[i] = __float2bfloat16_rn(p[kMlpOffW2 + i]);
-  if (i < kMlpN3 * kMlpH) {
-    const int r = i / kMlpH;
-    d->w3[i] = __float2bfloat16_rn(r < kMlpOut ? p[kMlpOffW3 + i] : 0.f);
+  if (i < kMlpH * kMlpK2) {
+    const int r = i / kMlpK2, k = i - r * kMlpK2;
+    d->w2[i] = k < kMlpH ? __float2bfloat16_rn(p[kMlpOffW2 + r * kMlpH + k])
+                         : (k < kMlpH + 3 ? bias_part(p[kMlpOffB2 + r], k - kMlpH) : z);
   }
-  if (i < kMlpH) {
-    d->b1[i] = p[kMlpOffB1 + i];
-    d->b2[i] = p[kMlpOffB2 + i];
+  if (i < kMlpN3 * kMlpK2) {
+    const int r = i / kMlpK2, k = i - r * kMlpK2;
+    d->w3[i] = r >= kMlpOut ? z
+                            : (k < kMlpH ? __float2bfloat16_rn(p[kMlpOffW3 + r * kMlpH + k])
+                                         : (k < kMlpH + 3 ? bias_part(p[kMlpOffB3 + r], k - kMlpH) : z));
   }
-  if (i < kMlpN3) d->b3[i] = i < kMlpOut ? p[kMlpOffB3 + i] : 0.f;
 }
 
 void mlp_pack(const float* params, MlpDev* dev, cudaStream_t s) {
-  k_mlp_pack<<<(kMlpH * kMlpH + 255) / 256, 256, 0, s>>>(params, dev);
+  k_mlp_pack<<<(kMlpH * kMlpK2 + 255) / 256, 256, 0, s>>>(params, dev);
 }
 
 __global__ void k_features_bf16(const float* __restrict__ f, __nv_bfloat16* __restrict__ x, long long n) {
@@ -316,7 +331,7 @@ __global__ void k_features_bf16(const float* __restrict__ f, __nv_bfloat16* __re
        e += (long long)gridDim.x * blockDim.x) {
     const long long r = e / kMlpK1;
     const int k = (int)(e - r * kMlpK1);
-    x[e] = __float2bfloat16_rn(k < kMlpIn ? f[r * kMlpIn + k] : 0.f);
+    x[e] = __float2bfloat16_rn(k < kMlpIn ? f[r * kMlpIn + k] : (k < kMlpOne + 3 ? 1.f : 0.f));
   }
 }
 
@@ -352,8 +367,9 @@ __global__ void __launch_bounds__(128) k_mlp_bwd(const __nv_bfloat16* __restrict
   float* w3 = w2 + kMlpH * kBwdLd;        // [2][64]
   __shared__ float s_loss[4];
   const int tid = threadIdx.x;
-  for (int e = tid; e < kMlpH * kMlpH; e += blockDim.x) w2[(e / kMlpH) * kBwdLd + e % kMlpH] = __bfloat162float(P->w2[e]);
-  for (int e = tid; e < kMlpOut * kMlpH; e += blockDim.x) w3[e] = __bfloat162float(P->w3[e]);
+  for (int e = tid; e < kMlpH * kMlpH; e += blockDim.x)
+    w2[(e / kMlpH) * kBwdLd + e % kMlpH] = __bfloat162float(P->w2[(e / kMlpH) * kMlpK2 + e % kMlpH]);
+  for (int e = tid; e < kMlpOut * kMlpH; e += blockDim.x) w3[e] = __bfloat162float(P->w3[(e / kMlpH) * kMlpK2 + e % kMlpH]);
   __syncthreads();
   const long long row = (long long)blockIdx.x * kMlpTile + tid;
   const bool live = row < n;

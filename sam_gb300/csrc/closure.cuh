@@ -14,6 +14,12 @@ constexpr int kMlpK1 = 16;   // padded input width (one K = 16 MMA step)
 constexpr int kMlpH = 64;    // hidden width
 constexpr int kMlpOut = 2;   // C_nu, C_kappa
 constexpr int kMlpN3 = 16;   // padded output width (N = 16 MMA)
+constexpr int kMlpK2 = 80;   // hidden width plus the bias inputs (K = 5 x 16)
+// The biases ride in the MMAs: each FP32 bias b is split exactly into three
+// BF16 parts (b = hi + mid + lo) stored as weight columns that multiply
+// inputs fixed at 1.0 (input columns 12..14 of the features, hidden columns
+// 64..66 of the operand tiles).
+constexpr int kMlpOne = 12;  // first constant-1 input column
 // FP32 parameter vector: W1 (64 x 12), b1, W2 (64 x 64), b2, W3 (2 x 64), b3
 constexpr int kMlpOffW1 = 0;
 constexpr int kMlpOffB1 = kMlpOffW1 + kMlpH * kMlpIn;
@@ -27,13 +33,12 @@ constexpr float kMlpScale = 0.02f;
 constexpr int kMlpTile = 128;  // points per MMA tile (M = 128)
 
 // Device copy of the network as the tensor cores read it: BF16 weights in
-// row-major [n][k] with the input padded to 16 and the output to 16 rows
-// (padding zero), FP32 biases.
+// row-major [n][k], the bias parts in columns 12..14 of w1 and 64..66 of w2
+// and w3, the output padded to 16 rows (padding zero).
 struct MlpDev {
   __nv_bfloat16 w1[kMlpH * kMlpK1];
-  __nv_bfloat16 w2[kMlpH * kMlpH];
-  __nv_bfloat16 w3[kMlpN3 * kMlpH];
-  float b1[kMlpH], b2[kMlpH], b3[kMlpN3];
+  __nv_bfloat16 w2[kMlpH * kMlpK2];
+  __nv_bfloat16 w3[kMlpN3 * kMlpK2];
 };
 
 // Training buffers of one minibatch (device).
@@ -45,7 +50,8 @@ struct MlpBatch {
 
 // params (FP32, kMlpParams) -> the BF16 device form
 void mlp_pack(const float* params, MlpDev* dev, cudaStream_t s);
-// x16: [n][16] BF16 inputs (16-byte aligned; loaded by TMA); coef: [n]
+// x16: [n][16] BF16 inputs, columns 12..14 equal to 1.0 and 15 zero
+// (16-byte aligned; loaded by TMA); coef: [n]
 // (C_nu, C_kappa); batch (may be null) receives the activations for the
 // backward pass; err is set on a wait timeout.  Returns the number of CTAs
 // launched, or -1 when the tensor map cannot be built (nothing launched).
@@ -60,7 +66,7 @@ void mlp_backward(const __nv_bfloat16* x16, const float2* y, long long n, const 
 // One Adam step on params (m, v moments), then the BF16 repack.
 void mlp_adam(float* params, float* m, float* v, const float* grad, int step, float lr, MlpDev* dev,
               cudaStream_t s);
-// FP32 features [n][12] -> BF16 [n][16] (zero padded)
+// FP32 features [n][12] -> BF16 [n][16] (columns 12..14 = 1.0, 15 = 0)
 void mlp_features_bf16(const float* f, __nv_bfloat16* x16, long long n, cudaStream_t s);
 // Self-test of one tensor-core tile: D(128 x 64) = A(128 x 16) B(64 x 16)^T
 // in BF16 with FP32 accumulation, for the known-answer test of the MMA path.

@@ -398,8 +398,8 @@ __device__ __forceinline__ void store_features(void* feat, long long pt, const f
     const __nv_bfloat162 h = __floats2bfloat162_rn(f[2 * i], f[2 * i + 1]);
     q[i] = *reinterpret_cast<const uint32_t*>(&h);
   }
-  q[6] = 0u;
-  q[7] = 0u;
+  q[6] = 0x3F803F80u;  // columns 12, 13: 1.0 (the network's bias inputs)
+  q[7] = 0x00003F80u;  // column 14: 1.0, column 15: 0
   uint4* dst = reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(feat) + pt * 16);
   dst[0] = make_uint4(q[0], q[1], q[2], q[3]);
   dst[1] = make_uint4(q[4], q[5], q[6], q[7]);

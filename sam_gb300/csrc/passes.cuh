@@ -67,9 +67,9 @@ struct XPassArgs {
   const float2* les_coef;
   double les_dsq;
   // out_mode 4: the closure's 12 invariants of point (z Ny + y) Nx + x as
-  // BF16 [16] (zero padded) from the input fields S (6), dT/dx (3, when
-  // Lr = 9) and w (3); f_bz = buoy_fac_z, f_n2 = N^2, f_dsq = delta^2,
-  // f_nu = viscosity
+  // BF16 [16] (columns 12..14 = 1.0, the network's bias inputs; 15 = 0)
+  // from the input fields S (6), dT/dx (3, when Lr = 9) and w (3);
+  // f_bz = buoy_fac_z, f_n2 = N^2, f_dsq = delta^2, f_nu = viscosity
   void* feat;
   double f_bz, f_n2, f_dsq, f_nu;
   long long in_y, in_z, in_n;
