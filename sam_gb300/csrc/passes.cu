@@ -1128,23 +1128,46 @@ __global__ void k_vel_max_finish(const double* __restrict__ partials, int nblk, 
                                  int* __restrict__ vmax) {
   __shared__ double red[kThreads];
   __shared__ double fin[4][4];
-  for (int f = 0; f < g.lu && !pv; ++f) {
-    for (int q = 0; q < 4; ++q) {
-      double v = 0.0;
-      for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
-        const double x = partials[((long long)b * g.lu + f) * 4 + q];
-        v = (q == 2) ? fmax(v, x) : v + x;
-      }
-      red[threadIdx.x] = v;
-      __syncthreads();
-      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) red[threadIdx.x] = (q == 2) ? fmax(red[threadIdx.x], red[threadIdx.x + s])
-                                                         : red[threadIdx.x] + red[threadIdx.x + s];
-        __syncthreads();
-      }
-      if (threadIdx.x == 0) fin[f][q] = red[0];
+  if (!pv) {
+    // a thread reads whole per-CTA records (lu x 4 doubles, contiguous) of
+    // the CTAs b = t, t + 256, ... into 16 accumulators, then one fixed-order
+    // tree per quantity: deterministic for a given number of CTAs
+    __shared__ double redq[16][kThreads / 2];
+    double v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = 0.0;
+    const int nq = 4 * g.lu;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+      const double2* rec = reinterpret_cast<const double2*>(partials + (long long)b * nq);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (2 * i < nq) {
+          const double2 x = rec[i];
+          v[2 * i] = ((2 * i) % 4 == 2) ? fmax(v[2 * i], x.x) : v[2 * i] + x.x;
+          v[2 * i + 1] = ((2 * i + 1) % 4 == 2) ? fmax(v[2 * i + 1], x.y) : v[2 * i + 1] + x.y;
+        }
+    }
+    // first tree level straight from the registers (threads t and t + 128)
+    const int h = blockDim.x / 2;
+    if (threadIdx.x >= h)
+#pragma unroll
+      for (int i = 0; i < 16; ++i) redq[i][threadIdx.x - h] = v[i];
+    __syncthreads();
+    if (threadIdx.x < h)
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        redq[i][threadIdx.x] = (i % 4 == 2) ? fmax(v[i], redq[i][threadIdx.x]) : v[i] + redq[i][threadIdx.x];
+    __syncthreads();
+    for (int st = h / 2; st > 0; st >>= 1) {
+      if (threadIdx.x < st)
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          redq[i][threadIdx.x] = (i % 4 == 2) ? fmax(redq[i][threadIdx.x], redq[i][threadIdx.x + st])
+                                              : redq[i][threadIdx.x] + redq[i][threadIdx.x + st];
       __syncthreads();
     }
+    if (threadIdx.x < nq) fin[threadIdx.x / 4][threadIdx.x % 4] = redq[threadIdx.x][0];
+    __syncthreads();
   }
   if (pv) {
     // sums from wave space: sum u = N u(0,0,0), sum u^2 = N sum w |u|^2
