@@ -62,6 +62,26 @@ __device__ __forceinline__ void batched(int count, Get get, Put put) {
 }
 
 // First-stage loader reading element idx of a row in global memory.
+// Store phase of the transposes: line t (t < nl) of a tile of `tile` lines
+// in shared memory goes to dst[r * ostride + t] for output rows r < nr,
+// taking its element at line position pos(r).  A thread keeps one line and
+// walks r with a running pointer (consecutive threads: consecutive t of one
+// row, so the stores coalesce); no division per element.
+template <typename C, typename Pos>
+__device__ __forceinline__ void store_tile_rows(C* __restrict__ dst, long long ostride, const C* s_ln, int ld, int tile,
+                                                int nl, int nr, Pos pos) {
+  const int span = min(tile, (int)blockDim.x);  // lines per sweep
+  const int rs = (int)blockDim.x / span, r0 = (int)threadIdx.x / span;
+  if (r0 >= rs) return;
+  const long long step = (long long)rs * ostride;
+  for (int t = (int)threadIdx.x - r0 * span; t < nl; t += span) {
+    const C* src = s_ln + t * ld;
+    C* o = dst + (long long)r0 * ostride + t;
+#pragma unroll 4
+    for (int r = r0; r < nr; r += rs, o += step) *o = src[sidx(pos(r))];
+  }
+}
+
 template <typename C> struct RowLoad {
   const C* __restrict__ row;
   __device__ __forceinline__ C operator()(int idx) const { return row[idx]; }
@@ -188,17 +208,10 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
     });
   }
   __syncthreads();
+  // store: a thread keeps row t of the tile and walks z with a running
+  // pointer; consecutive threads write consecutive ky of one z
   C* dst = a.out + (long long)n * a.out_n + (long long)i * a.out_kx + j0;
-  batched<C>(
-      a.ty * nz,
-      [&](int e) {
-        const int z = (int)fdiv(e, a.fd_t), t = e - z * a.ty;
-        return t < nl ? s_ln[t * ld + sidx(z)] : mk<C>((T)0, (T)0);
-      },
-      [&](int e, C v) {
-        const int z = (int)fdiv(e, a.fd_t), t = e - z * a.ty;
-        if (t < nl) dst[(long long)z * a.out_z + t] = v;
-      });
+  store_tile_rows(dst, a.out_z, s_ln, ld, a.ty, nl, nz, [](int z) { return z; });
 }
 
 // --------------------------------------------------------------- y inverse
@@ -235,16 +248,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
                              [&](int L) { return BandRowLoad<C>{src + (long long)L * a.in_kx, km, ny - km, ny - my}; });
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)z * a.out_z + i0;
-  batched<C>(
-      a.tx * ny,
-      [&](int e) {
-        const int y = (int)fdiv(e, a.fd_t), t = e - y * a.tx;
-        return t < nl ? s_ln[t * ld + sidx(y)] : mk<C>((T)0, (T)0);
-      },
-      [&](int e, C v) {
-        const int y = (int)fdiv(e, a.fd_t), t = e - y * a.tx;
-        if (t < nl) dst[(long long)y * a.out_y + t] = v;
-      });
+  store_tile_rows(dst, a.out_y, s_ln, ld, a.tx, nl, ny, [](int y) { return y; });
 }
 
 // Two adjacent complex values in one store (one 16-byte store in FP32, two in
@@ -845,16 +849,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
                            [&](int L) { return RowLoad<C>{src + (long long)L * a.in_z}; });
   __syncthreads();
   C* dst = a.out + (long long)m * a.out_n + (long long)i * a.out_kx + z0;
-  batched<C>(
-      a.tz * my,
-      [&](int e) {
-        const int j = (int)fdiv(e, a.fd_t), t = e - j * a.tz;
-        return t < nl ? s_ln[t * ld + sidx(kpos(j, km, my, ny))] : mk<C>((T)0, (T)0);
-      },
-      [&](int e, C v) {
-        const int j = (int)fdiv(e, a.fd_t), t = e - j * a.tz;
-        if (t < nl) dst[(long long)j * a.out_ky + t] = v;
-      });
+  store_tile_rows(dst, a.out_ky, s_ln, ld, a.tz, nl, my, [&](int j) { return kpos(j, km, my, ny); });
 }
 
 __device__ __forceinline__ double wexp(double x) { return exp(x); }
@@ -1242,7 +1237,6 @@ __global__ void k_x2z(const double2* __restrict__ in, double2* __restrict__ out,
 template <typename T>
 void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
   ZInvArgs<T> a = a0;
-  a.fd_t = make_fastdiv(a.ty);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.nvar * a.g.mx * nty;
   switch (a.g.nz) {
@@ -1257,8 +1251,6 @@ void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
 template <typename T>
 void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
   YInvArgs<T> a = a0;
-  a.fd_n = make_fastdiv(a.g.ny);
-  a.fd_t = make_fastdiv(a.tx);
   const int ntx = (a.g.mx + a.tx - 1) / a.tx;
   const int grid = a.nvar * a.g.nz * ntx;
   switch (a.g.ny) {
@@ -1294,8 +1286,6 @@ void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaS
 template <typename T>
 void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
   YFwdArgs<T> a = a0;
-  a.fd_n = make_fastdiv(a.g.ny);
-  a.fd_t = make_fastdiv(a.tz);
   const int ntz = (a.g.nz + a.tz - 1) / a.tz;
   const int grid = a.nvar * a.g.mx * ntz;
   switch (a.g.ny) {
@@ -1310,7 +1300,6 @@ void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
 template <typename T>
 void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
   ZFwdArgs<T> a = a0;
-  a.fd_n = make_fastdiv(a.g.nz);
   a.fd_t = make_fastdiv(a.ty);
   a.fd_m = make_fastdiv(a.g.mz);
   a.nz_inv = (T)(1.0 / (double)a.g.nz);

@@ -18,7 +18,6 @@ struct ZInvArgs {
   int derive;
   long long in_ky, in_kx, in_n;
   long long out_kx, out_z, out_n;
-  FastDiv fd_t;  // filled by the launcher: ty
 };
 
 template <typename T>
@@ -30,7 +29,6 @@ struct YInvArgs {
   int nvar, tx, ld, in_full;
   long long in_kx, in_z, in_n;
   long long out_y, out_z, out_n;
-  FastDiv fd_n, fd_t;  // filled by the launcher: Ny, tx
 };
 
 // Threads of an x pass CTA.  In the FP32 n = 256 path a team of 16 threads
@@ -87,7 +85,6 @@ struct YFwdArgs {
   int nvar, tz, ld;
   long long in_kx, in_z, in_n;
   long long out_ky, out_kx, out_n;
-  FastDiv fd_n, fd_t;  // filled by the launcher: Ny, tz
 };
 
 template <typename T>
@@ -109,7 +106,7 @@ struct ZFwdArgs {
   DevState* state;
   StageConsts sc;
   T nz_inv;                  // filled by the launcher: 1/Nz
-  FastDiv fd_n, fd_t, fd_m;  // filled by the launcher: Nz, ty, Nz_min
+  FastDiv fd_t, fd_m;  // filled by the launcher: ty, Nz_min
 };
 
 template <typename T> void launch_z_inv(const ZInvArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
