@@ -1245,6 +1245,7 @@ void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
     case 64: k_z_inv<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_z_inv<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 512: k_z_inv<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 96: k_z_inv<T, 96><<<grid, kThreads, smem, s>>>(a, pl); break;
     default: k_z_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
   }
 }
@@ -1259,6 +1260,7 @@ void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
     case 64: k_y_inv<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_y_inv<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 512: k_y_inv<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 96: k_y_inv<T, 96><<<grid, kThreads, smem, s>>>(a, pl); break;
     default: k_y_inv<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
   }
 }
@@ -1280,6 +1282,7 @@ void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaS
     case 64: k_x_pass<T, 64><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     case 128: k_x_pass<T, 128><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     case 512: k_x_pass<T, 512><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
+    case 96: k_x_pass<T, 96><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     default: k_x_pass<T, kFftGeneric><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl);
   }
 }
@@ -1294,6 +1297,7 @@ void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
     case 64: k_y_fwd<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_y_fwd<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 512: k_y_fwd<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 96: k_y_fwd<T, 96><<<grid, kThreads, smem, s>>>(a, pl); break;
     default: k_y_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
   }
 }
@@ -1311,6 +1315,7 @@ void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
     case 64: k_z_fwd<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_z_fwd<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 512: k_z_fwd<T, 512><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 96: k_z_fwd<T, 96><<<grid, kThreads, smem, s>>>(a, pl); break;
     default: k_z_fwd<T, kFftGeneric><<<grid, kThreads, smem, s>>>(a, pl);
   }
 }
@@ -1345,30 +1350,35 @@ void set_smem_limits() {
   allow_dynamic_smem((const void*)k_z_inv<T, 64>, optin);
   allow_dynamic_smem((const void*)k_z_inv<T, 128>, optin);
   allow_dynamic_smem((const void*)k_z_inv<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, 96>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, 32>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, 64>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, 128>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, 96>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 32>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 64>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 128>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, 96>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, 32>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, 64>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, 128>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, 96>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, 32>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, 64>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, 128>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, 512>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, 96>, optin);
 }
 
 #define SAMGPU_INST(T)                                                                           \

@@ -29,11 +29,13 @@ GRIDS = [
     # length-256 lines take the 16 x 16 register path: x and y, then z
     dict(nx=256, ny=256, nz=12, i_strat=1),
     dict(nx=16, ny=20, nz=256, i_strat=1),
-    # compile-time radix paths (128, 64, 512) and the longest line (1024)
+    # compile-time radix paths (128, 64, 512, 96; 96 in z above) and the
+    # longest line (1024)
     dict(nx=128, ny=64, nz=128, i_strat=1),
     dict(nx=512, ny=6, nz=10, i_strat=0),
     dict(nx=12, ny=10, nz=512, i_strat=1),
     dict(nx=1024, ny=2, nz=6, i_strat=1),
+    dict(nx=96, ny=96, nz=8, i_strat=1),
 ]
 
 
