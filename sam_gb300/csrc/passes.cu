@@ -1078,28 +1078,58 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
 
 // ----------------------------------------------------- vel_max completion
 // vel_max.f:170-196 on the per-CTA partials written by k_x_pass.
-// Parseval sums of vel_max (see launch_parseval): FP64 products of the
-// stored modes, per-thread strided order, block tree, fixed launch shape.
+// Parseval sums of vel_max (see launch_parseval): sums of the stored modes'
+// squares, FP64-accurate, per-thread strided order, block tree, fixed launch
+// shape.  The FP32 form (the only user) accumulates the exact squares of its
+// FP32 values in error-free FP32 pairs (about 48 bits: FP64 arithmetic, one
+// instruction per value pair of the 1/64-rate FP64 pipe plus a conversion,
+// made this kernel FP64-bound); the FP64 form would use FP64.
+__device__ __forceinline__ DF df_add_wsq(DF a, float v, float w) {
+  // a + w v^2 with w a power of two (exact scaling of the exact square p + e)
+  const float p = v * v;
+  const float e = fmaf(v, v, -p);
+  return df_add(df_add(a, p * w), e * w);
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict__ u, Grid g, double* __restrict__ pv) {
   __shared__ double red[4][kThreads];
   const long long nm = (long long)g.mx * g.my * g.mz;
   const int plane = g.my * g.mz;
-  // kx = 0 modes count once, kx > 0 twice (their conjugates): separate sums
-  double acc0[4] = {0.0, 0.0, 0.0, 0.0}, acc1[4] = {0.0, 0.0, 0.0, 0.0};
-  for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < nm; m += (long long)gridDim.x * blockDim.x) {
-    const bool kx0 = m < plane;
+  if constexpr (sizeof(T) == 4) {
+    // kx = 0 modes count once, kx > 0 twice (their conjugates): sum w |u|^2
+    // with w = 1/2 for kx = 0 and 1 otherwise, then double
+    DF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < nm;
+         m += (long long)gridDim.x * blockDim.x) {
+      const float w = m < plane ? 0.5f : 1.0f;
 #pragma unroll
-    for (int f = 0; f < 4; ++f)
-      if (f < g.lu) {
-        const cx_t<T> v = u[f * nm + m];
-        const double re = (double)v.x, im = (double)v.y;
-        if (kx0) acc0[f] = fma(re, re, fma(im, im, acc0[f]));
-        else acc1[f] = fma(re, re, fma(im, im, acc1[f]));
-      }
+      for (int f = 0; f < 4; ++f)
+        if (f < g.lu) {
+          const cx_t<T> v = u[f * nm + m];
+          acc[f] = df_add_wsq(df_add_wsq(acc[f], v.y, w), v.x, w);
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < 4; ++f) red[f][threadIdx.x] = 2.0 * ((double)acc[f].hi + (double)acc[f].lo);
+  } else {
+    // kx = 0 modes count once, kx > 0 twice (their conjugates): separate sums
+    double acc0[4] = {0.0, 0.0, 0.0, 0.0}, acc1[4] = {0.0, 0.0, 0.0, 0.0};
+    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < nm;
+         m += (long long)gridDim.x * blockDim.x) {
+      const bool kx0 = m < plane;
+#pragma unroll
+      for (int f = 0; f < 4; ++f)
+        if (f < g.lu) {
+          const cx_t<T> v = u[f * nm + m];
+          const double re = (double)v.x, im = (double)v.y;
+          if (kx0) acc0[f] = fma(re, re, fma(im, im, acc0[f]));
+          else acc1[f] = fma(re, re, fma(im, im, acc1[f]));
+        }
+    }
+#pragma unroll
+    for (int f = 0; f < 4; ++f) red[f][threadIdx.x] = acc0[f] + 2.0 * acc1[f];
   }
-#pragma unroll
-  for (int f = 0; f < 4; ++f) red[f][threadIdx.x] = acc0[f] + 2.0 * acc1[f];
   __syncthreads();
   for (int s = blockDim.x / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s)
