@@ -358,6 +358,11 @@ __device__ __forceinline__ void sgs_point_c(T* s, int nf, T cnu, T ckap) {
 //   f4 asinh(b g_z / |S|^2)           f10 log(1 + |S| delta^2 / nu)
 //   f5 log(1 + |b| |g_h| / |S|^2)     f11 4 (S13^2 + S23^2) / |S|^2
 // (b = buoy_fac_z, g_h the horizontal part of g).
+// Division in the invariants: exact in FP64; in FP32 the 2-ulp fast
+// division (the invariants are rounded to BF16, 2^-8 relative, afterwards)
+__device__ __forceinline__ double fdv(double a, double b) { return a / b; }
+__device__ __forceinline__ float fdv(float a, float b) { return __fdividef(a, b); }
+
 template <typename T>
 __device__ __forceinline__ void closure_invariants(const T* S, const T* g, const T* w, T bz, T n2, T dsq, T nu,
                                                    float* f) {
@@ -380,18 +385,18 @@ __device__ __forceinline__ void closure_invariants(const T* S, const T* g, const
   const T sn = sqrt(s2);
   const T w2 = w[0] * w[0] + w[1] * w[1] + w[2] * w[2], wn = sqrt(w2);
   const T g2 = g[0] * g[0] + g[1] * g[1] + g[2] * g[2], gn = sqrt(g2);
-  const T inv_s2 = (T)1 / (s2 + eps);
+  const T inv_s2 = fdv((T)1, s2 + eps);
   f[0] = (float)log1p(w2 * inv_s2);
-  f[1] = (float)(tr3 / (s2 * sn + eps));
-  f[2] = (float)(wSw / (sn * w2 + eps));
+  f[1] = (float)fdv(tr3, s2 * sn + eps);
+  f[2] = (float)fdv(wSw, sn * w2 + eps);
   f[3] = (float)log1p(fabs(n2) * inv_s2);
   f[4] = (float)asinh(bz * g[2] * inv_s2);
   f[5] = (float)log1p(fabs(bz) * sqrt(g[0] * g[0] + g[1] * g[1]) * inv_s2);
-  f[6] = (float)(M[2][2] / (sn + eps));
-  f[7] = (float)(w[2] / (sn + wn + eps));
-  f[8] = (float)(gSg / (sn * g2 + eps));
-  f[9] = (float)((w[0] * g[0] + w[1] * g[1] + w[2] * g[2]) / (wn * gn + eps));
-  f[10] = (float)log1p(sn * dsq / nu);
+  f[6] = (float)fdv(M[2][2], sn + eps);
+  f[7] = (float)fdv(w[2], sn + wn + eps);
+  f[8] = (float)fdv(gSg, sn * g2 + eps);
+  f[9] = (float)fdv(w[0] * g[0] + w[1] * g[1] + w[2] * g[2], wn * gn + eps);
+  f[10] = (float)log1p(fdv(sn * dsq, nu));
   f[11] = (float)((T)4 * (S[3] * S[3] + S[4] * S[4]) * inv_s2);
 }
 
