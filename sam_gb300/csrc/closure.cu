@@ -78,175 +78,186 @@ void mlp_mma_selftest(const __nv_bfloat16* a, const __nv_bfloat16* b, float* d, 
 // ------------------------------------------------------------ forward pass
 // One hidden layer's epilogue for this thread's row: TMEM (the bias is
 // already in the accumulator) -> ReLU -> BF16 K-major operand tile columns
-// 0..63 (and, when hg is given, the activations); the ReLU is the
-// conversion's (cvt.relu).
+// 0..63 (and, when hg is given, the activations), 16 columns at a time; the
+// ReLU is the conversion's (cvt.relu).
 __device__ __forceinline__ void epilogue(uint32_t tl, uint8_t* tile, int r, __nv_bfloat16* __restrict__ hg,
                                          long long row, bool live) {
 #pragma unroll
-  for (int c0 = 0; c0 < kMlpH; c0 += 32) {
-    float h[32];
-    tmem_ld32(tl + (uint32_t)c0, h);
-    uint32_t q[16];
+  for (int c0 = 0; c0 < kMlpH; c0 += 16) {
+    float h[16];
+    tmem_ld16(tl + (uint32_t)c0, h);
+    uint32_t q[8];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) q[k] = pack_relu_bf16(h[2 * k], h[2 * k + 1]);
+    for (int k = 0; k < 8; ++k) q[k] = pack_relu_bf16(h[2 * k], h[2 * k + 1]);
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < 2; ++j)
       *reinterpret_cast<uint4*>(tile + kmaj(r, c0 + 8 * j, kMlpK2)) =
           make_uint4(q[4 * j], q[4 * j + 1], q[4 * j + 2], q[4 * j + 3]);
     if (hg && live) {
       uint4* dst = reinterpret_cast<uint4*>(hg + row * kMlpH + c0);
 #pragma unroll
-      for (int j = 0; j < 4; ++j) dst[j] = make_uint4(q[4 * j], q[4 * j + 1], q[4 * j + 2], q[4 * j + 3]);
+      for (int j = 0; j < 2; ++j) dst[j] = make_uint4(q[4 * j], q[4 * j + 1], q[4 * j + 2], q[4 * j + 3]);
     }
   }
 }
 
-// Persistent CTAs of 128 threads; thread t owns row t of every tile (its
-// TMEM lane).  Optionally stores the activations for the backward pass.
-// The input tiles arrive by TMA: a 2-D tensor map over x16 ([n][16] BF16,
-// 32-byte rows) with a box of 8 x 128 (16 bytes x 128 rows), loaded at
-// x = 0 and x = 8, writes the two K halves of a 128 x 16 tile one after the
-// other: element (r, k) at (k/8)*2048 + r*16 + (k%8)*2, the canonical
-// no-swizzle K-major layout with LBO = 2048 B and SBO = 128 B.  Two buffers:
-// the next tile's load runs during this tile's MMA chain.  The hidden
-// operand tile is 128 x 80: columns 64..66 hold 1.0 (the bias inputs of
-// layers 2 and 3), 67..79 zero, written once.
-constexpr int kMlpFwdCtas = 5;  // per SM: 43 KB of shared memory, 64 TMEM columns each
-__global__ void __launch_bounds__(128, kMlpFwdCtas) k_mlp_fwd(const __grid_constant__ CUtensorMap xmap, long long n,
-                                                 const MlpDev* __restrict__ P, float2* __restrict__ coef,
-                                                 __nv_bfloat16* __restrict__ h1g, __nv_bfloat16* __restrict__ h2g,
-                                                 float* __restrict__ og, int* err) {
-  __shared__ __align__(1024) uint8_t sw1[kMlpH * kMlpK1 * 2];
-  __shared__ __align__(1024) uint8_t sw2[kMlpH * kMlpK2 * 2];
-  __shared__ __align__(1024) uint8_t sw3[kMlpN3 * kMlpK2 * 2];
-  __shared__ __align__(1024) uint8_t sa1[2][kMlpTile * kMlpK1 * 2];
-  __shared__ __align__(1024) uint8_t sa2[kMlpTile * kMlpK2 * 2];
-  __shared__ uint64_t bar, tbar[2];
-  __shared__ uint32_t tbase;
-  const int tid = threadIdx.x;
+// Shared memory of the forward kernel: the BF16 weights in the K-major
+// layout (shared by the CTA's warpgroups), then per warpgroup its input tile
+// and its 128 x 80 hidden operand tile (columns 64..66 hold 1.0, the bias
+// inputs of layers 2 and 3; 67..79 zero), and the barriers.  Every operand
+// starts on a 128-byte boundary.
+constexpr int kMlpWG = 4;  // warpgroups per CTA, each with its own tiles
+struct MlpWgTiles {
+  uint8_t a1[kMlpTile * kMlpK1 * 2];
+  uint8_t a2[kMlpTile * kMlpK2 * 2];
+};
+struct MlpFwdSmem {
+  uint8_t w1[kMlpH * kMlpK1 * 2];
+  uint8_t w2[kMlpH * kMlpK2 * 2];
+  uint8_t w3[kMlpN3 * kMlpK2 * 2];
+  MlpWgTiles wg[kMlpWG];
+  uint64_t mbar[kMlpWG], tbar[kMlpWG];
+  uint32_t tbase;
+};
+constexpr size_t kMlpFwdSmemBytes = sizeof(MlpFwdSmem) + 1024;  // + room to align the base to 1024 bytes
+constexpr int kMlpFwdCtas = 2;  // per SM: 112 KB of shared memory and 256 TMEM columns each
+
+// Persistent CTAs of four warpgroups; each warpgroup runs its own tiles of
+// 128 points (thread r of the warpgroup owns row r: its TMEM lane) through
+// the three layers with its own TMEM columns (64 per warpgroup), barriers
+// and named-barrier synchronisation, so a CTA keeps four independent MMA
+// chains in flight and an SM eight.  Optionally stores the activations for
+// the backward pass.  The input tiles arrive by TMA: a 2-D tensor map over
+// x16 ([n][16] BF16, 32-byte rows) with a box of 8 x 128 (16 bytes x 128
+// rows), loaded at x = 0 and x = 8, writes the two K halves of a 128 x 16
+// tile one after the other: element (r, k) at (k/8)*2048 + r*16 + (k%8)*2,
+// the canonical no-swizzle K-major layout with LBO = 2048 B and SBO = 128 B.
+// A warpgroup's next input is loaded as soon as its layer-1 MMA has read the
+// current one.
+__global__ void __launch_bounds__(128 * kMlpWG, kMlpFwdCtas)
+    k_mlp_fwd(const __grid_constant__ CUtensorMap xmap, long long n, const MlpDev* __restrict__ P,
+              float2* __restrict__ coef, __nv_bfloat16* __restrict__ h1g, __nv_bfloat16* __restrict__ h2g,
+              float* __restrict__ og, int* err) {
+  extern __shared__ __align__(1024) uint8_t mlp_smem[];
+  MlpFwdSmem& S = *reinterpret_cast<MlpFwdSmem*>(mlp_smem + ((1024u - (smem_u32(mlp_smem) & 1023u)) & 1023u));
+  const int tid = threadIdx.x, g = tid >> 7, r = tid & 127;
+  const int bid = 1 + g;  // this warpgroup's named barrier (0 is __syncthreads)
   const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
+  const long long nslots = (long long)gridDim.x * kMlpWG;
+  const long long first = (long long)blockIdx.x * kMlpWG + g;
   constexpr uint32_t kTileBytes = kMlpTile * kMlpK1 * 2;
-  if (tid < 32) tmem_alloc(&tbase, 64);
-  if (tid == 0) {
-    mbar_init(&bar, 1);
-    mbar_init(&tbar[0], 1);
-    mbar_init(&tbar[1], 1);
+  uint8_t* a1 = S.wg[g].a1;
+  uint8_t* a2 = S.wg[g].a2;
+  auto load_tile = [&](long long t) {
+    mbar_expect_tx(&S.tbar[g], kTileBytes);
+    tma_load_2d(a1, &xmap, 0, (int)(t * kMlpTile), &S.tbar[g]);
+    tma_load_2d(a1 + kTileBytes / 2, &xmap, 8, (int)(t * kMlpTile), &S.tbar[g]);
+  };
+  if (tid < 32) tmem_alloc(&S.tbase, 64 * kMlpWG);
+  if (r == 0) {
+    mbar_init(&S.mbar[g], 1);
+    mbar_init(&S.tbar[g], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    if (blockIdx.x < ntiles) {
-      mbar_expect_tx(&tbar[0], kTileBytes);
-      tma_load_2d(sa1[0], &xmap, 0, (int)(blockIdx.x * kMlpTile), &tbar[0]);
-      tma_load_2d(sa1[0] + kTileBytes / 2, &xmap, 8, (int)(blockIdx.x * kMlpTile), &tbar[0]);
-    }
+    if (first < ntiles) load_tile(first);
   }
-  stage_matrix(sw1, P->w1, kMlpH, kMlpK1);
-  stage_matrix(sw2, P->w2, kMlpH, kMlpK2);
-  stage_matrix(sw3, P->w3, kMlpN3, kMlpK2);
+  stage_matrix(S.w1, P->w1, kMlpH, kMlpK1);
+  stage_matrix(S.w2, P->w2, kMlpH, kMlpK2);
+  stage_matrix(S.w3, P->w3, kMlpN3, kMlpK2);
   {
-    // the constant columns of this thread's row of the hidden operand tile
+    // the constant columns of this thread's row of its hidden operand tile
     const uint32_t one = 0x3F80u;  // 1.0 in BF16
-    *reinterpret_cast<uint4*>(sa2 + kmaj(tid, kMlpH, kMlpK2)) = make_uint4(one | (one << 16), one, 0u, 0u);
-    *reinterpret_cast<uint4*>(sa2 + kmaj(tid, kMlpH + 8, kMlpK2)) = make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4*>(a2 + kmaj(r, kMlpH, kMlpK2)) = make_uint4(one | (one << 16), one, 0u, 0u);
+    *reinterpret_cast<uint4*>(a2 + kmaj(r, kMlpH + 8, kMlpK2)) = make_uint4(0u, 0u, 0u, 0u);
   }
   fence_async_smem();
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
-  const uint32_t tm = tbase;
-  const uint32_t tl = tm + ((uint32_t)(32 * (tid >> 5)) << 16);  // this warp's lanes
-  const uint32_t a2 = smem_u32(sa2);
-  const uint32_t w1 = smem_u32(sw1), w2 = smem_u32(sw2), w3 = smem_u32(sw3);
+  const uint32_t tm = S.tbase + 64u * (uint32_t)g;                    // this warpgroup's columns
+  const uint32_t tl = tm + ((uint32_t)(32 * ((tid >> 5) & 3)) << 16);  // this warp's lanes
+  const uint32_t sa1 = smem_u32(a1), sa2 = smem_u32(a2);
+  const uint32_t w1 = smem_u32(S.w1), w2 = smem_u32(S.w2), w3 = smem_u32(S.w3);
   const uint32_t id64 = idesc_bf16(kMlpTile, kMlpH), id16 = idesc_bf16(kMlpTile, kMlpN3);
-  uint32_t phase = 0;
-  int bad = 0, it = 0, pending = -1;  // pending: buffer of a TMA load not yet waited for
-  if (blockIdx.x < ntiles) pending = 0;
-  for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++it) {
-    const long long row = t * kMlpTile + tid;
-    const bool live = row < n;
-    const int b = it & 1;
-    // the next tile's load into the other buffer (its previous MMA is done)
-    const long long tn = t + gridDim.x;
-    if (tid == 0 && tn < ntiles) {
-      mbar_expect_tx(&tbar[b ^ 1], kTileBytes);
-      tma_load_2d(sa1[b ^ 1], &xmap, 0, (int)(tn * kMlpTile), &tbar[b ^ 1]);
-      tma_load_2d(sa1[b ^ 1] + kTileBytes / 2, &xmap, 8, (int)(tn * kMlpTile), &tbar[b ^ 1]);
-    }
-    // one thread polls each barrier; the others wait at the CTA barrier
-    // (bad is then the same in every thread)
-    bad = tid == 0 ? mbar_wait(&tbar[b], (uint32_t)((it >> 1) & 1)) : 0;
-    pending = tn < ntiles ? (b ^ 1) : -1;
-    bad = __syncthreads_or(bad);
-    if (bad) break;
-    const uint32_t a1 = smem_u32(sa1[b]);
-    // layer 1: D = X W1^T (K = 16)
-    if (tid == 0) {
-      tc_fence_after();
-      mma_bf16(tm, sdesc(a1, 2048, 128), sdesc(w1, 128, 256), id64, 0);
-      mma_commit(&bar);
-    }
-    bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
-    phase ^= 1;
-    bad = __syncthreads_or(bad);
+  uint32_t mph = 0, tph = 0;
+  int bad = 0;
+  bool pend = first < ntiles;  // a TMA load not yet waited for (the same in every thread of the warpgroup)
+  // one thread polls each barrier; the warpgroup's named barrier releases
+  // the others and makes bad the same in all of them
+  auto wait_mma = [&]() {
+    int b = r == 0 ? mbar_wait(&S.mbar[g], mph) : 0;
+    mph ^= 1u;
+    b = bar_named_or(bid, 128, b);
     tc_fence_after();
-    if (bad) break;
-    // epilogue in chunks of 16 columns: bias, ReLU, BF16 into the next
-    // operand tile (and the activations for the backward pass)
-    epilogue(tl, sa2, tid, h1g, row, live);
+    return b;
+  };
+  auto to_mma = [&]() {  // operand tile written: visible to the tensor cores
     fence_async_smem();
     tc_fence_before();
-    __syncthreads();
+    bar_named(bid, 128);
     tc_fence_after();
+  };
+  for (long long t = first; t < ntiles; t += nslots) {
+    const long long row = t * kMlpTile + r;
+    const bool live = row < n;
+    bad = r == 0 ? mbar_wait(&S.tbar[g], tph) : 0;
+    bad = bar_named_or(bid, 128, bad);
+    if (bad) break;
+    tph ^= 1u;
+    pend = false;
+    // layer 1: D = X W1^T (K = 16; the bias through input columns 12..14)
+    if (r == 0) {
+      tc_fence_after();
+      mma_bf16(tm, sdesc(sa1, 2048, 128), sdesc(w1, 128, 256), id64, 0);
+      mma_commit(&S.mbar[g]);
+    }
+    if ((bad = wait_mma())) break;
+    // the input tile has been read: the next one loads during this tile's chain
+    const long long tn = t + nslots;
+    pend = tn < ntiles;
+    if (r == 0 && pend) load_tile(tn);
+    epilogue(tl, a2, r, h1g, row, live);
+    to_mma();
     // layer 2: D = H1 W2^T (K = 80 as five K = 16 steps, the last with the
     // bias columns)
-    if (tid == 0) {
+    if (r == 0) {
 #pragma unroll
       for (int kk = 0; kk < kMlpK2 / 16; ++kk)
-        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w2 + 256 * kk, 128, kMlpK2 * 16), id64, kk > 0);
-      mma_commit(&bar);
+        mma_bf16(tm, sdesc(sa2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w2 + 256 * kk, 128, kMlpK2 * 16), id64, kk > 0);
+      mma_commit(&S.mbar[g]);
     }
-    bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
-    phase ^= 1;
-    bad = __syncthreads_or(bad);
-    tc_fence_after();
-    if (bad) break;
-    epilogue(tl, sa2, tid, h2g, row, live);
-    fence_async_smem();
-    tc_fence_before();
-    __syncthreads();
-    tc_fence_after();
+    if ((bad = wait_mma())) break;
+    epilogue(tl, a2, r, h2g, row, live);
+    to_mma();
     // layer 3: D = H2 W3^T (N = 16, two rows used; K = 80 as for layer 2)
-    if (tid == 0) {
+    if (r == 0) {
 #pragma unroll
       for (int kk = 0; kk < kMlpK2 / 16; ++kk)
-        mma_bf16(tm, sdesc(a2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w3 + 256 * kk, 128, kMlpK2 * 16), id16, kk > 0);
-      mma_commit(&bar);
+        mma_bf16(tm, sdesc(sa2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w3 + 256 * kk, 128, kMlpK2 * 16), id16, kk > 0);
+      mma_commit(&S.mbar[g]);
     }
-    bad = tid == 0 ? mbar_wait(&bar, phase) : 0;
-    phase ^= 1;
-    bad = __syncthreads_or(bad);
-    tc_fence_after();
-    if (bad) break;
+    if ((bad = wait_mma())) break;
     float o[2];
     tmem_ld2(tl, o);
     if (live) {
-      const float o0 = o[0], o1 = o[1];
-      coef[row] = make_float2(kMlpScale * softplus(o0), kMlpScale * softplus(o1));
+      coef[row] = make_float2(kMlpScale * softplus(o[0]), kMlpScale * softplus(o[1]));
       if (og) {
-        og[2 * row] = o0;
-        og[2 * row + 1] = o1;
+        og[2 * row] = o[0];
+        og[2 * row + 1] = o[1];
       }
     }
+    // the accumulator is read before the next tile's layer 1 writes it
     tc_fence_before();
-    __syncthreads();
+    bar_named(bid, 128);
     tc_fence_after();
   }
-  if (bad && tid == 0) atomicExch(err, 1);
+  if (bad && r == 0) atomicExch(err, 1);
   // a load still in flight (the loop left early) completes before exit
-  if (pending >= 0 && tid == 0) mbar_wait(&tbar[pending], (uint32_t)(((it + 1) >> 1) & 1));
+  if (pend && r == 0) mbar_wait(&S.tbar[g], tph);
   tc_fence_before();
   __syncthreads();
   if (tid < 32) {
     tc_fence_after();
-    tmem_dealloc(tm, 64);
+    tmem_dealloc(S.tbase, 64 * kMlpWG);
   }
 }
 
@@ -280,12 +291,20 @@ int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2
                 int* err, cudaStream_t s) {
   const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
   long long grid = 152 * kMlpFwdCtas;  // persistent: one wave
-  if (grid > ntiles) grid = ntiles;
+  if (grid > (ntiles + kMlpWG - 1) / kMlpWG) grid = (ntiles + kMlpWG - 1) / kMlpWG;
   if (grid < 1) return 0;
   CUtensorMap m;
   if (!x16_map(x16, n, &m)) return -1;
-  k_mlp_fwd<<<(int)grid, kMlpTile, 0, s>>>(m, n, dev, coef, batch ? batch->h1 : nullptr, batch ? batch->h2 : nullptr,
-                                           batch ? batch->o : nullptr, err);
+  static bool attr = false;
+  if (!attr) {
+    if (cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpFwdSmemBytes) !=
+        cudaSuccess)
+      return -1;
+    attr = true;
+  }
+  k_mlp_fwd<<<(int)grid, 128 * kMlpWG, kMlpFwdSmemBytes, s>>>(m, n, dev, coef, batch ? batch->h1 : nullptr,
+                                                              batch ? batch->h2 : nullptr, batch ? batch->o : nullptr,
+                                                              err);
   return (int)grid;
 }
 

@@ -89,6 +89,22 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// Named barrier of `count` threads (a multiple of 32) and its OR reduction
+// of pred (the same result in every participating thread).
+__device__ __forceinline__ void bar_named(int id, int count) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ int bar_named_or(int id, int count, int pred) {
+  int r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.s32 p, %1, 0;\n\tbar.red.or.pred q, %2, %3, p;\n\t"
+      "selp.s32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(pred), "r"(id), "r"(count)
+      : "memory");
+  return r;
+}
+
 // 32 consecutive columns of this warp's 32 TMEM lanes (one value per thread
 // and column), then one wait
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
