@@ -105,24 +105,6 @@ __device__ __forceinline__ int bar_named_or(int id, int count, int pred) {
   return r;
 }
 
-// 32 consecutive columns of this warp's 32 TMEM lanes (one value per thread
-// and column), then one wait
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
-  uint32_t r[32];
-  asm volatile(
-      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
-      "%15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
-      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
-        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
-        "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
-        "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-      : "r"(taddr)
-      : "memory");
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
-}
-
 // two consecutive columns
 __device__ __forceinline__ void tmem_ld2(uint32_t taddr, float* v) {
   uint32_t r0, r1;
@@ -132,37 +114,11 @@ __device__ __forceinline__ void tmem_ld2(uint32_t taddr, float* v) {
   v[1] = __uint_as_float(r1);
 }
 
-// (a + c, b + d) as one packed FP32 pair addition
-__device__ __forceinline__ float2 add_f32x2(float2 x, float2 y) {
-  unsigned long long p, q, s;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(p) : "f"(x.x), "f"(x.y));
-  asm("mov.b64 %0, {%1, %2};" : "=l"(q) : "f"(y.x), "f"(y.y));
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(s) : "l"(p), "l"(q));
-  float2 r;
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(s));
-  return r;
-}
-
 // BF16 pair (a in the low half) of max(a, 0), max(b, 0), rounded to nearest
 __device__ __forceinline__ uint32_t pack_relu_bf16(float a, float b) {
   uint32_t r;
   asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
   return r;
-}
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-  return *reinterpret_cast<const uint32_t*>(&h);
-}
-
-// eight values of row r, columns k0..k0+7, into a K-major tile as one 16 B store
-__device__ __forceinline__ void st_row8(uint8_t* tile, int r, int k0, int K, const float* v) {
-  uint4 q;
-  q.x = pack_bf16(v[0], v[1]);
-  q.y = pack_bf16(v[2], v[3]);
-  q.z = pack_bf16(v[4], v[5]);
-  q.w = pack_bf16(v[6], v[7]);
-  *reinterpret_cast<uint4*>(tile + kmaj(r, k0, K)) = q;
 }
 
 // copy a row-major [R][K] BF16 matrix into a K-major tile
