@@ -1,5 +1,5 @@
-// tcgen05 / TMEM / mbarrier helpers (inline PTX for sm_103a) shared by the
-// closure network kernels and the fused x pass.  The BF16 operand tiles use
+// tcgen05 / TMEM / mbarrier / TMA helpers (inline PTX for sm_103a) of the
+// closure network kernels (closure.cu).  The BF16 operand tiles use
 // the canonical K-major no-swizzle layout: element (r, k) of an R x K tile at
 // (r/8)*(K/8)*128 + (k/8)*128 + (r%8)*16 + (k%8)*2 bytes, i.e. 8 x 16-byte
 // core matrices with LBO = 128 B between K neighbours and SBO = (K/8)*128 B
