@@ -32,8 +32,9 @@ constexpr int kBatch = 8;
 
 // Resident CTAs per SM each kernel's register budget is sized for (measured
 // at 256^3): in FP32 the transpose passes fit 64 registers (four CTAs) and
-// the x pass 80 (three CTAs) without spills; the FP32 z_fwd epilogue spills
-// below 128 and keeps two; FP64 CTAs are bound by the FP64 pipe.
+// the x pass 72 (three CTAs of 288 threads) without spills; the FP32 z_fwd
+// epilogue spills below 128 and keeps two (three measured slower); FP64 CTAs
+// are bound by the FP64 pipe.
 // The run-time-radix path (kFftGeneric, lengths without a compile-time
 // path) needs more registers: one x pass CTA per SM, two of the others.
 enum PassKind { kPassZInv, kPassYInv, kPassX, kPassYFwd, kPassZFwd };

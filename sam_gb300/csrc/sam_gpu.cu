@@ -290,9 +290,10 @@ static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
   const int threads = x_threads((int)sizeof(T), c.g.nx);
   const int team = c.g.nx == 256 ? 16 : (sizeof(T) == 4 ? c.px.h.team_sp : c.px.h.team);
   const int teams = threads / team > 0 ? threads / team : 1;
-  // FP32 tiles leave room for three CTAs per SM (80 registers each), FP64
-  // tiles for two (128 registers each): the FP64 pipe needs the second CTA's
-  // warps to cover its dependency latency
+  // FP32 tiles leave room for three CTAs per SM (72 registers each; two
+  // CTAs with 16-row tiles measured slower), FP64 tiles for two (up to 128
+  // registers each): the FP64 pipe needs the second CTA's warps to cover its
+  // dependency latency
   const size_t budget = sizeof(T) == 4 ? kSmemMax / 3 - 1024 : kSmemMax / 2 - 1024;
   const size_t line = es * (size_t)line_ld(c.g.nx);
   const size_t rmin = line * (size_t)x_red_lines<T>(c);
