@@ -1,16 +1,18 @@
 // Learned subgrid closure: the 12 -> 64 -> 64 -> 2 MLP on sm_103a.
 //
-// Inference: one CTA of 128 threads (one warpgroup) per tile of 128 points.
-// The inputs and the weights sit in shared memory in the canonical K-major
-// no-swizzle layout of the tensor cores (8 x 16-byte core matrices: element
-// (r, k) at (r/8)*SBO + (k/8)*LBO + (r%8)*16 + (k%8)*2 with LBO = 128 B and
-// SBO = (K/8)*128 B).  One thread issues tcgen05.mma (kind::f16, BF16 x BF16
-// -> FP32 in TMEM, M = 128), tcgen05.commit arrives on an mbarrier, all four
-// warps wait on it and read their 32 TMEM lanes back with tcgen05.ld; the
-// bias and ReLU epilogue writes the next layer's BF16 operand into shared
-// memory.  Three MMA groups per tile (K = 16, then 4 x K = 16 twice).  Every
-// wait is bounded: on timeout the kernel sets *err, frees its TMEM and
-// returns.
+// Inference: a warpgroup (128 threads) per tile of 128 points, four
+// warpgroups per CTA, each with its own tiles.  The inputs and the weights
+// sit in shared memory in the canonical K-major no-swizzle layout of the
+// tensor cores (8 x 16-byte core matrices: element (r, k) at (r/8)*SBO +
+// (k/8)*LBO + (r%8)*16 + (k%8)*2 with LBO = 128 B and SBO = (K/8)*128 B).
+// One thread per warpgroup issues tcgen05.mma (kind::f16, BF16 x BF16 ->
+// FP32 in TMEM, M = 128), tcgen05.commit arrives on an mbarrier, the
+// warpgroup's four warps read their 32 TMEM lanes back with tcgen05.ld; the
+// ReLU epilogue writes the next layer's BF16 operand into shared memory (the
+// biases are in the MMAs, against constant-1 input columns).  Three MMA
+// groups per tile (K = 16, then 5 x K = 16 twice).  Every wait is bounded:
+// on timeout the kernel sets *err, waits for its loads in flight, frees its
+// TMEM and returns.
 //
 // Training: the backward pass of the loss mean (C - y)^2 and Adam run on the
 // CUDA cores in FP32 (the network is small; the weight gradients are
