@@ -164,6 +164,23 @@ def profile_traffic(name="x_pass_traffic.json"):
         return None
 
 
+def max_over_ranks(x, pg):
+    """The largest value of x over the ranks of pg (x itself with one rank):
+    the timed region of the job is the slowest replica's."""
+    if not pg:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t[0])
+
+
+def whole_job_rate(steps, seconds, ws):
+    """Steps per second of the whole job: ws replicas each ran `steps` steps
+    (weak scaling) in `seconds`, the slowest rank's time."""
+    return ws * steps / seconds
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
@@ -467,12 +484,8 @@ def main():
             e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-    ms = e0.elapsed_time(e1)
-    if pg:
-        t = torch.tensor([ms], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t[0])
-    value = ws * K / (ms / 1e3)
+    ms = max_over_ranks(e0.elapsed_time(e1), pg)
+    value = whole_job_rate(K, ms / 1e3, ws)
     st = g.stats()
     launches_per_step = 3 * 5 + 1  # five passes per stage, vel_max completion at stage 1
     u_fp64 = g.download()
@@ -500,14 +513,10 @@ def main():
         g.step(1)
         g.download(out=uh)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if pg:
-        t = torch.tensor([e2e_s], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        e2e_s = float(t[0])
+    e2e_s = max_over_ranks(time.perf_counter() - t0, pg)
     mx, my, mz = dims()
     io_bytes = 4 * mx * my * mz * 16
-    e2e = {"value": ws * Ke / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": io_bytes,
+    e2e = {"value": whole_job_rate(Ke, e2e_s, ws), "unit": "steps/s", "h2d_bytes_per_step": io_bytes,
            "d2h_bytes_per_step": io_bytes,
            "path": "sam_gpu_upload + sam_gpu_step(1) + sam_gpu_download on pinned host arrays"}
     g.close()
