@@ -25,6 +25,28 @@ template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype
 
 template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
 template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+// FP32 complex sums as one packed instruction (add/sub.rn.f32x2: two IEEE
+// round-to-nearest operations, the same results as the scalar pair)
+__device__ __forceinline__ unsigned long long f2_pack(float2 a) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a.x), "f"(a.y));
+  return r;
+}
+__device__ __forceinline__ float2 f2_unpack(unsigned long long r) {
+  float2 a;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a.x), "=f"(a.y) : "l"(r));
+  return a;
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
+  return f2_unpack(r);
+}
 // a * w (SIGN=-1) or a * conj(w) (SIGN=+1)
 template <int SIGN, typename C> __device__ __forceinline__ C ctw(C a, C w) {
   if (SIGN < 0) return mk<C>(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
