@@ -145,15 +145,23 @@ int sam_gpu_step(int nsteps);
  * ms5 = {z inverse, y inverse, x pass (+ vel_max), y forward, z forward+update}.
  * The state advances as in sam_gpu_stage. */
 int sam_gpu_profile_stage(int nrk, int reps, float* ms5);
-/* Tile autotuner (no counterpart in the reference): times candidate tile
- * sizes of each pass on the resident state (best of reps) and keeps the
- * fastest; u and r are restored afterwards.  Call after upload, before
- * stepping; results do not depend on the tiling beyond the summation order
- * of the vel_max partial sums. out6 of sam_gpu_tiles receives the choice:
- * z-inverse rows, y-inverse columns, x-pass rows, x-pass product group,
- * y-forward planes, z-forward rows. */
+/* Tile and FFT-schedule autotuner (no counterpart in the reference): times
+ * candidate tile sizes of each pass, and for passes along a length-256
+ * dimension both FFT schedules, on the resident state (best of reps) and
+ * keeps the fastest; u and r are restored afterwards.  Call after upload,
+ * before stepping; results do not depend on the tiling beyond the summation
+ * order of the vel_max partial sums. out6 of sam_gpu_tiles receives the
+ * tiles: z-inverse rows, y-inverse columns, x-pass rows, x-pass product
+ * group, y-forward planes, z-forward rows.
+ * sam_gpu_set_fft_schedule / sam_gpu_fft_schedule: the FFT schedule of each
+ * pass (z inverse, y inverse, x, y forward, z forward) for lines of length
+ * 256: 0 the 16 x 16 register path, 1 compile-time Stockham stages of radix
+ * 8, 8, 4 (other lengths have one schedule and ignore the value); values
+ * other than 0 and 1 are rejected (SAM_GPU_EINVAL). */
 int sam_gpu_autotune(int reps);
 int sam_gpu_tiles(int* out6);
+int sam_gpu_set_fft_schedule(const int* sched5);
+int sam_gpu_fft_schedule(int* out5);
 /* Measurement hook: FP64 FMA throughput of this GPU (TFLOP/s), the ALU
  * roofline of the FP64 drop-in.  No counterpart in the reference. */
 int sam_gpu_measure_fp64_peak(double* tflops);

@@ -382,7 +382,7 @@ __device__ __forceinline__ void fft256_lines(C* base, int ld, int nlines, const 
 // Code paths of the line transforms: kFftAny picks at run time (the plan's
 // length); kFft256 compiles only the 16 x 16 register path (n = 256) and
 // kFftGeneric only the Stockham stages with the radix chosen at run time;
-// PATH = n (32, 64, 96, 128, 512) compiles the Stockham stages of that length
+// PATH = n (32, 64, 96, 128, 256, 512) compiles the Stockham stages of that length
 // with their radices fixed at compile time.  A kernel built for one length
 // thus carries no registers for another path.
 constexpr int kFftAny = 0, kFft256 = 1, kFftGeneric = 2;
@@ -404,7 +404,14 @@ __host__ __device__ constexpr int ct_nst(int n) {
   return s;
 }
 // lengths with a compile-time path
-__host__ __device__ constexpr bool ct_length(int n) { return n == 32 || n == 64 || n == 96 || n == 128 || n == 512; }
+__host__ __device__ constexpr bool ct_length(int n) {
+  return n == 32 || n == 64 || n == 96 || n == 128 || n == 256 || n == 512;
+}
+// Twiddles a kernel compiled for PATH loads: the 16 x 16 table alone (at the
+// start of the table) for the register path, all of them otherwise.
+template <int PATH> __device__ __forceinline__ int tw_load(const FftPlan& pl) {
+  return PATH == kFft256 ? pl.tw_pass : pl.tw_total;
+}
 
 // Stages S.. of a compile-time length N on one line; stage 0 reads through first.
 template <int SIGN, int N, int S, typename C, typename First>

@@ -140,7 +140,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_pass;
+  C* s_ln = s_tw + tw_load<PATH>(pl);
   const int nz = a.g.nz, mz = a.g.mz, km = a.g.kz, my = a.g.my;
   const int ld = a.ld;
   const int nty = (my + a.ty - 1) / a.ty;
@@ -150,7 +150,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   const int n = b;
   const int j0 = jt * a.ty;
   const int nl = min(a.ty, my - j0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
+  load_twiddles<T>(s_tw, a.tw, tw_load<PATH>(pl));
   const C* src = a.in + (long long)n * a.in_n + (long long)i * a.in_kx + (long long)j0 * a.in_ky;
   __syncthreads();
   if (!a.derive || n < a.g.lu) {
@@ -227,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_pass;
+  C* s_ln = s_tw + tw_load<PATH>(pl);
   const int ny = a.g.ny, my = a.g.my, km = a.g.ky, mx = a.g.mx;
   const int ld = a.ld;
   const int ntx = (mx + a.tx - 1) / a.tx;
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
   const int n = b;
   const int i0 = it * a.tx;
   const int nl = min(a.tx, mx - i0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
+  load_twiddles<T>(s_tw, a.tw, tw_load<PATH>(pl));
   const C* src = a.in + (long long)n * a.in_n + (long long)z * a.in_z + (long long)i0 * a.in_kx;
   __syncthreads();
   // the first stage reads the rows straight from memory: all Ny values
@@ -431,7 +431,7 @@ __device__ __forceinline__ void product_pair(int m, int& a, int& b) {
 }
 
 template <typename T, int PATH>
-__global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256 ? 256 : 0), MinBlocks<T, kPassX, PATH>::value)
+__global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBlocks<T, kPassX, PATH>::value)
     k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -439,7 +439,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256 ? 256 : 0
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_in = s_tw + pl.tw_pass;                  // nin * yp lines
+  C* s_in = s_tw + tw_load<PATH>(pl);                  // nin * yp lines
   const int nx = a.g.nx, ny = a.g.ny, kmx = a.g.kx, mx = a.g.mx;
   const int Y = a.yt, yp = Y / 2, ld = a.ld;
   const int nin = a.nin;
@@ -452,7 +452,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256 ? 256 : 0
   const int z = blockIdx.x / nyt;
   const int y0 = yt * Y;
   const int yv = min(Y, ny - y0);  // valid rows in the tile
-  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
+  load_twiddles<T>(s_tw, a.tw, tw_load<PATH>(pl));
 
   // ---- build the input lines
   if (a.in_mode == 0) {
@@ -836,7 +836,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_pass;
+  C* s_ln = s_tw + tw_load<PATH>(pl);
   const int ny = a.g.ny, my = a.g.my, km = a.g.ky, nz = a.g.nz;
   const int ld = a.ld;
   const int ntz = (nz + a.tz - 1) / a.tz;
@@ -846,7 +846,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
   const int m = b;
   const int z0 = zt * a.tz;
   const int nl = min(a.tz, nz - z0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
+  load_twiddles<T>(s_tw, a.tw, tw_load<PATH>(pl));
   const C* src = a.in + (long long)m * a.in_n + (long long)i * a.in_kx + (long long)z0 * a.in_z;
   __syncthreads();
   // the first stage reads its inputs straight from the rows of C (no
@@ -1013,7 +1013,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
   load_plan(&pl, gpl);
   __syncthreads();
   C* s_tw = reinterpret_cast<C*>(smem_raw);
-  C* s_ln = s_tw + pl.tw_pass;
+  C* s_ln = s_tw + tw_load<PATH>(pl);
   const Grid& g = a.g;
   const int nz = g.nz, mz = g.mz, km = g.kz, my = g.my;
   const int ld = a.ld, nf = a.nf;
@@ -1022,7 +1022,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
   const int i = blockIdx.x / nty;
   const int j0 = jt * a.ty;
   const int nl = min(a.ty, my - j0);
-  load_twiddles<T>(s_tw, a.tw, pl.tw_pass);
+  load_twiddles<T>(s_tw, a.tw, tw_load<PATH>(pl));
   // lines of all nf fields for the nl rows of this tile, packed as f * nl + t;
   // the first stage reads the z-contiguous rows of D straight from memory
   __syncthreads();
@@ -1276,7 +1276,10 @@ void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.nvar * a.g.mx * nty;
   switch (a.g.nz) {
-    case 256: k_z_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 256:
+      if (a.sched) k_z_inv<T, 256><<<grid, kThreads, smem, s>>>(a, pl);
+      else k_z_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+      break;
     case 32: k_z_inv<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 64: k_z_inv<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_z_inv<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
@@ -1291,7 +1294,10 @@ void launch_y_inv(const YInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   const int ntx = (a.g.mx + a.tx - 1) / a.tx;
   const int grid = a.nvar * a.g.nz * ntx;
   switch (a.g.ny) {
-    case 256: k_y_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 256:
+      if (a.sched) k_y_inv<T, 256><<<grid, kThreads, smem, s>>>(a, pl);
+      else k_y_inv<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+      break;
     case 32: k_y_inv<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 64: k_y_inv<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_y_inv<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
@@ -1313,7 +1319,10 @@ void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaS
   a.fd_y = make_fastdiv(a.yt);
   a.fn = (T)(0.5 / ((double)a.g.nx * (double)a.g.ny));
   switch (a.g.nx) {
-    case 256: k_x_pass<T, kFft256><<<x_pass_blocks(a), x_threads(sizeof(T), 256), smem, s>>>(a, pl); break;
+    case 256:
+      if (a.sched) k_x_pass<T, 256><<<x_pass_blocks(a), x_threads(sizeof(T), false), smem, s>>>(a, pl);
+      else k_x_pass<T, kFft256><<<x_pass_blocks(a), x_threads(sizeof(T), true), smem, s>>>(a, pl);
+      break;
     case 32: k_x_pass<T, 32><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     case 64: k_x_pass<T, 64><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     case 128: k_x_pass<T, 128><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
@@ -1328,7 +1337,10 @@ void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   const int ntz = (a.g.nz + a.tz - 1) / a.tz;
   const int grid = a.nvar * a.g.mx * ntz;
   switch (a.g.ny) {
-    case 256: k_y_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 256:
+      if (a.sched) k_y_fwd<T, 256><<<grid, kThreads, smem, s>>>(a, pl);
+      else k_y_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+      break;
     case 32: k_y_fwd<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 64: k_y_fwd<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_y_fwd<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
@@ -1346,7 +1358,10 @@ void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.g.mx * nty;
   switch (a.g.nz) {
-    case 256: k_z_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl); break;
+    case 256:
+      if (a.sched) k_z_fwd<T, 256><<<grid, kThreads, smem, s>>>(a, pl);
+      else k_z_fwd<T, kFft256><<<grid, kThreads, smem, s>>>(a, pl);
+      break;
     case 32: k_z_fwd<T, 32><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 64: k_z_fwd<T, 64><<<grid, kThreads, smem, s>>>(a, pl); break;
     case 128: k_z_fwd<T, 128><<<grid, kThreads, smem, s>>>(a, pl); break;
@@ -1387,6 +1402,7 @@ void set_smem_limits() {
   allow_dynamic_smem((const void*)k_z_inv<T, 128>, optin);
   allow_dynamic_smem((const void*)k_z_inv<T, 512>, optin);
   allow_dynamic_smem((const void*)k_z_inv<T, 96>, optin);
+  allow_dynamic_smem((const void*)k_z_inv<T, 256>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, 32>, optin);
@@ -1394,6 +1410,7 @@ void set_smem_limits() {
   allow_dynamic_smem((const void*)k_y_inv<T, 128>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, 512>, optin);
   allow_dynamic_smem((const void*)k_y_inv<T, 96>, optin);
+  allow_dynamic_smem((const void*)k_y_inv<T, 256>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 32>, optin);
@@ -1401,6 +1418,7 @@ void set_smem_limits() {
   allow_dynamic_smem((const void*)k_x_pass<T, 128>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 512>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 96>, optin);
+  allow_dynamic_smem((const void*)k_x_pass<T, 256>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, 32>, optin);
@@ -1408,6 +1426,7 @@ void set_smem_limits() {
   allow_dynamic_smem((const void*)k_y_fwd<T, 128>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, 512>, optin);
   allow_dynamic_smem((const void*)k_y_fwd<T, 96>, optin);
+  allow_dynamic_smem((const void*)k_y_fwd<T, 256>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, 32>, optin);
@@ -1415,6 +1434,7 @@ void set_smem_limits() {
   allow_dynamic_smem((const void*)k_z_fwd<T, 128>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, 512>, optin);
   allow_dynamic_smem((const void*)k_z_fwd<T, 96>, optin);
+  allow_dynamic_smem((const void*)k_z_fwd<T, 256>, optin);
 }
 
 #define SAMGPU_INST(T)                                                                           \

@@ -8,6 +8,9 @@ namespace samgpu {
 template <typename T>
 struct ZInvArgs {
   Grid g;
+  // FFT schedule of length-256 lines: 0 the 16 x 16 register path, 1 the
+  // compile-time Stockham stages (radix 8, 8, 4); chosen by the autotuner
+  int sched;
   const cx_t<T>* in;   // rows of Nz_min modes
   cx_t<T>* out;        // A(n, z, kx, ky)
   const cx_t<T>* tw;   // twiddles of the Nz plan
@@ -23,6 +26,9 @@ struct ZInvArgs {
 template <typename T>
 struct YInvArgs {
   Grid g;
+  // FFT schedule of length-256 lines: 0 the 16 x 16 register path, 1 the
+  // compile-time Stockham stages (radix 8, 8, 4); chosen by the autotuner
+  int sched;
   const cx_t<T>* in;  // rows (one per kx) of Ny_min modes or Ny values
   cx_t<T>* out;       // B(n, z, y, kx)
   const cx_t<T>* tw;
@@ -31,15 +37,19 @@ struct YInvArgs {
   long long out_y, out_z, out_n;
 };
 
-// Threads of an x pass CTA.  In the FP32 n = 256 path a team of 16 threads
-// transforms one line, and an 8-row tile holds 4 x 4 input and 9 x 4 product
-// lines: 18 teams do them in one and two full rounds (16 teams would need a
-// third round a quarter full).  Other forms keep kThreads.
-__host__ __device__ constexpr int x_threads(int bytes, int n) { return bytes == 4 && n == 256 ? 288 : kThreads; }
+// Threads of an x pass CTA.  In the FP32 16 x 16 register path (n = 256) a
+// team of 16 threads transforms one line, and an 8-row tile holds 4 x 4
+// input and 9 x 4 product lines: 18 teams do them in one and two full rounds
+// (16 teams would need a third round a quarter full).  Other forms keep
+// kThreads.
+__host__ __device__ constexpr int x_threads(int bytes, bool reg16) { return bytes == 4 && reg16 ? 288 : kThreads; }
 
 template <typename T>
 struct XPassArgs {
   Grid g;
+  // FFT schedule of length-256 lines: 0 the 16 x 16 register path, 1 the
+  // compile-time Stockham stages (radix 8, 8, 4); chosen by the autotuner
+  int sched;
   const cx_t<T>* in;   // in_mode 0: B(n, z, y, kx)
   const T* in_phys;    // in_mode 1: P(n, z, y, x)
   cx_t<T>* out;        // out_mode 1/2: C(m, z, kx, y)
@@ -79,6 +89,9 @@ struct XPassArgs {
 template <typename T>
 struct YFwdArgs {
   Grid g;
+  // FFT schedule of length-256 lines: 0 the 16 x 16 register path, 1 the
+  // compile-time Stockham stages (radix 8, 8, 4); chosen by the autotuner
+  int sched;
   const cx_t<T>* in;  // C(m, z, kx, y)
   cx_t<T>* out;       // D(m, kx, ky, z)
   const cx_t<T>* tw;
@@ -90,6 +103,9 @@ struct YFwdArgs {
 template <typename T>
 struct ZFwdArgs {
   Grid g;
+  // FFT schedule of length-256 lines: 0 the 16 x 16 register path, 1 the
+  // compile-time Stockham stages (radix 8, 8, 4); chosen by the autotuner
+  int sched;
   cx_t<T>* in;  // D(m, kx, ky, z); mode 0 writes the result back here
   const cx_t<T>* tw;
   int mode, nf, ty, ld;

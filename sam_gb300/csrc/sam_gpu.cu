@@ -166,6 +166,9 @@ struct Ctx {
   Scratch sc[4];
   // tile choices
   int ty_zi = 16, tx_yi = 16, yt_x = 8, grp_x = 9, tz_yf = 16, ty_zf = 4;
+  // FFT schedule of each pass for length-256 lines (z_inv, y_inv, x, y_fwd,
+  // z_fwd): 0 the 16 x 16 register path, 1 compile-time Stockham (8, 8, 4)
+  int sched[5] = {0, 0, 0, 0, 0};
   OuForcing* ou = nullptr;  // device OU forcing state, null when off
   // subgrid closure coupled into the stage (sam_gpu_set_les)
   int les_model = 0;
@@ -220,17 +223,19 @@ static size_t csize(const Ctx& c) { return c.cfg.precision == 32 ? sizeof(float2
 static int line_ld(int n) { return line_stride(n); }
 
 // shared memory of a tile of `lines` lines of length n plus the twiddles
-static size_t tile_smem(const Plan& P, int lines, size_t es) {
-  return es * ((size_t)P.h.tw_pass + (size_t)lines * line_ld(P.h.n)) + 16;
+// the kernel loads (schedule 1 of a length-256 pass loads the whole table)
+static size_t tile_smem(const Plan& P, int lines, size_t es, int sched = 0) {
+  const int ntw = sched && P.h.n == 256 ? P.h.tw_total : P.h.tw_pass;
+  return es * ((size_t)ntw + (size_t)lines * line_ld(P.h.n)) + 16;
 }
 
 // dynamic shared memory budget of one CTA: the opt-in limit (227 KB on
 // GB300) less room for the kernels' static shared memory
 static size_t kSmemMax = 227 * 1024 - 2048;
 
-static int pick_tile(const Plan& P, int want, int lines_per_unit, size_t es, size_t extra = 0) {
+static int pick_tile(const Plan& P, int want, int lines_per_unit, size_t es, int sched = 0) {
   int t = want;
-  while (t > 1 && tile_smem(P, t * lines_per_unit, es) + extra > kSmemMax) t /= 2;
+  while (t > 1 && tile_smem(P, t * lines_per_unit, es, sched) > kSmemMax) t /= 2;
   return t;
 }
 
@@ -245,11 +250,12 @@ static int run_z_inv(Ctx& c, const void* in, void* out, int nvar, long long in_k
   a.out = (cx_t<T>*)out;
   a.tw = tw_of<T>(c.pz);
   a.nvar = nvar;
-  a.ty = pick_tile(c.pz, c.ty_zi, 1, sizeof(cx_t<T>));
+  a.sched = c.sched[0];
+  a.ty = pick_tile(c.pz, c.ty_zi, 1, sizeof(cx_t<T>), a.sched);
   a.ld = line_ld(c.g.nz);
   a.in_ky = in_ky; a.in_kx = in_kx; a.in_n = in_n;
   a.out_kx = out_kx; a.out_z = out_z; a.out_n = out_n;
-  launch_z_inv<T>(a, c.pz.d, tile_smem(c.pz, a.ty, sizeof(cx_t<T>)), c.stream);
+  launch_z_inv<T>(a, c.pz.d, tile_smem(c.pz, a.ty, sizeof(cx_t<T>), a.sched), c.stream);
   return 0;
 }
 
@@ -262,19 +268,23 @@ static int run_y_inv(Ctx& c, const void* in, void* out, int nvar, int in_full, l
   a.out = (cx_t<T>*)out;
   a.tw = tw_of<T>(c.py);
   a.nvar = nvar;
-  a.tx = pick_tile(c.py, c.tx_yi, 1, sizeof(cx_t<T>));
+  a.sched = c.sched[1];
+  a.tx = pick_tile(c.py, c.tx_yi, 1, sizeof(cx_t<T>), a.sched);
   a.ld = line_ld(c.g.ny);
   a.in_full = in_full;
   a.in_kx = in_kx; a.in_z = in_z; a.in_n = in_n;
   a.out_y = out_y; a.out_z = out_z; a.out_n = out_n;
-  launch_y_inv<T>(a, c.py.d, tile_smem(c.py, a.tx, sizeof(cx_t<T>)), c.stream);
+  launch_y_inv<T>(a, c.py.d, tile_smem(c.py, a.tx, sizeof(cx_t<T>), a.sched), c.stream);
   return 0;
 }
+
+// whether the x pass runs the 16 x 16 register path
+static bool x_reg16(const Ctx& c) { return c.g.nx == 256 && c.sched[2] == 0; }
 
 // lines the reduction scratch of vel_max occupies (FP64 partials of each warp)
 template <typename T>
 static int x_red_lines(const Ctx& c) {
-  const size_t red = sizeof(double) * 4 * (x_threads((int)sizeof(T), c.g.nx) / 32) + 64;
+  const size_t red = sizeof(double) * 4 * (x_threads((int)sizeof(T), x_reg16(c)) / 32) + 64;
   const size_t line = sizeof(cx_t<T>) * (size_t)line_ld(c.g.nx);
   return (int)((red + line - 1) / line);
 }
@@ -287,8 +297,8 @@ static int x_red_lines(const Ctx& c) {
 template <typename T>
 static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
   const size_t es = sizeof(cx_t<T>);
-  const int threads = x_threads((int)sizeof(T), c.g.nx);
-  const int team = c.g.nx == 256 ? 16 : (sizeof(T) == 4 ? c.px.h.team_sp : c.px.h.team);
+  const int threads = x_threads((int)sizeof(T), x_reg16(c));
+  const int team = x_reg16(c) ? 16 : (sizeof(T) == 4 ? c.px.h.team_sp : c.px.h.team);
   const int teams = threads / team > 0 ? threads / team : 1;
   // FP32 tiles leave room for three CTAs per SM (72 registers each; two
   // CTAs with 16-row tiles measured slower), FP64 tiles for two (up to 128
@@ -299,7 +309,7 @@ static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
   const size_t rmin = line * (size_t)x_red_lines<T>(c);
   for (yt = c.yt_x;; yt /= 2) {
     const int yp = yt / 2;
-    const size_t base = tile_smem(c.px, nin * yp, es);
+    const size_t base = tile_smem(c.px, nin * yp, es, c.sched[2]);
     if (out_mode != 2) {
       grp = 0;
       if (base + rmin <= budget) return 0;
@@ -316,7 +326,7 @@ static int x_tile(Ctx& c, int nin, int out_mode, int& yt, int& grp) {
 
 template <typename T>
 static size_t x_smem(Ctx& c, int nin, int yt, int grp) {
-  return tile_smem(c.px, nin * (yt / 2) + std::max(grp, x_red_lines<T>(c)), sizeof(cx_t<T>));
+  return tile_smem(c.px, nin * (yt / 2) + std::max(grp, x_red_lines<T>(c)), sizeof(cx_t<T>), c.sched[2]);
 }
 
 template <typename T>
@@ -348,6 +358,7 @@ static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in
   a.in_mode = in_mode;
   a.out_mode = out_mode;
   a.nin = nin;
+  a.sched = c.sched[2];
   int rc = x_tile<T>(c, nin, out_mode, a.yt, a.group);
   if (rc) return rc;
   a.ld = line_ld(c.g.nx);
@@ -387,11 +398,12 @@ static int run_y_fwd(Ctx& c, const void* in, void* out, int nvar, long long in_k
   a.out = (cx_t<T>*)out;
   a.tw = tw_of<T>(c.py);
   a.nvar = nvar;
-  a.tz = pick_tile(c.py, c.tz_yf, 1, sizeof(cx_t<T>));
+  a.sched = c.sched[3];
+  a.tz = pick_tile(c.py, c.tz_yf, 1, sizeof(cx_t<T>), a.sched);
   a.ld = line_ld(c.g.ny);
   a.in_kx = in_kx; a.in_z = in_z; a.in_n = in_n;
   a.out_ky = out_ky; a.out_kx = out_kx; a.out_n = out_n;
-  launch_y_fwd<T>(a, c.py.d, tile_smem(c.py, a.tz, sizeof(cx_t<T>)), c.stream);
+  launch_y_fwd<T>(a, c.py.d, tile_smem(c.py, a.tz, sizeof(cx_t<T>), a.sched), c.stream);
   return 0;
 }
 
@@ -422,8 +434,9 @@ static int run_z_fwd(Ctx& c, ZFwdArgs<T>& a) {
   a.g = c.g;
   a.tw = tw_of<T>(c.pz);
   a.ld = line_ld(c.g.nz);
-  a.ty = pick_tile(c.pz, c.ty_zf, a.nf, sizeof(cx_t<T>));
-  launch_z_fwd<T>(a, c.pz.d, tile_smem(c.pz, a.ty * a.nf, sizeof(cx_t<T>)), c.stream);
+  a.sched = c.sched[4];
+  a.ty = pick_tile(c.pz, c.ty_zf, a.nf, sizeof(cx_t<T>), a.sched);
+  launch_z_fwd<T>(a, c.pz.d, tile_smem(c.pz, a.ty * a.nf, sizeof(cx_t<T>), a.sched), c.stream);
   return 0;
 }
 
@@ -1494,9 +1507,11 @@ int sam_gpu_measure_fp64_peak(double* tflops) {
   return check_launch();
 }
 
-// Tile autotuner: each pass is timed (CUDA events, best of `reps`) with each
-// candidate tiling on the resident state and the fastest is kept.  The z
-// forward pass updates u and r, so both are saved first and restored after.
+// Tile and FFT-schedule autotuner: each pass is timed (CUDA events, best of
+// `reps`) with each candidate on the resident state and the fastest is kept.
+// The z forward pass updates u and r, so both are saved first and restored
+// after; stages 1 and 2 recompute dt and the statistics from that state and
+// leave the time alone.
 int sam_gpu_autotune(int reps) {
   NEED_CTX();
   if (reps < 1) reps = 1;
@@ -1510,11 +1525,11 @@ int sam_gpu_autotune(int reps) {
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  auto time_pass = [&](int p) {
+  auto time_pass = [&](int p, int nrk = 2) {
     float best = 1e30f;
     for (int r = 0; r < reps + 1; ++r) {
       cudaEventRecord(e0, c.stream);
-      if (stage_any(c, 2, nullptr, p)) return 1e30f;
+      if (stage_any(c, nrk, nullptr, p)) return 1e30f;
       cudaEventRecord(e1, c.stream);
       cudaEventSynchronize(e1);
       float ms = 0.0f;
@@ -1523,15 +1538,19 @@ int sam_gpu_autotune(int reps) {
     }
     return best;
   };
-  auto tune = [&](int p, int* field, std::initializer_list<int> cands) {
+  // a candidate replaces the current choice when it is faster by more than
+  // `margin`; `both` times stages 1 and 2 together (stage 1 adds vel_max's
+  // work to the x pass; stage 3 would advance the time)
+  auto tune = [&](int p, int* field, std::initializer_list<int> cands, float margin = 0.0f, bool both = false) {
+    auto timed = [&]() { return both ? time_pass(p, 1) + time_pass(p, 2) : time_pass(p); };
     int best_v = *field;
-    float best_t = time_pass(p);
+    float best_t = timed();
     for (int v : cands) {
       if (v == best_v) continue;
       const int keep = *field;
       *field = v;
-      const float t = time_pass(p);
-      if (t < best_t) { best_t = t; best_v = v; }
+      const float t = timed();
+      if (t < best_t * (1.0f - margin)) { best_t = t; best_v = v; }
       else *field = keep;
     }
     *field = best_v;
@@ -1542,6 +1561,12 @@ int sam_gpu_autotune(int reps) {
   tune(2, &c.grp_x, {1, 2, 3, 5, 9});
   tune(3, &c.tz_yf, {4, 8, 16, 32});
   tune(4, &c.ty_zf, {1, 2, 4, 8});
+  // then the FFT schedule of each pass with length-256 lines (16 x 16
+  // registers or compile-time Stockham) with those tiles: the register path
+  // stays unless the other is more than 2 % faster over stages 1 and 2
+  const int plen[5] = {c.g.nz, c.g.ny, c.g.nx, c.g.ny, c.g.nz};
+  for (int p = 0; p < 5; ++p)
+    if (plen[p] == 256) tune(p, &c.sched[p], {0, 1}, 0.02f, true);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   CK(cudaMemcpyAsync(c.U, su, bytes, cudaMemcpyDeviceToDevice, c.stream));
@@ -1552,6 +1577,24 @@ int sam_gpu_autotune(int reps) {
   if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
   c.graph_stale = 1;  // recapture with the new tiles
   return check_launch();
+}
+
+int sam_gpu_set_fft_schedule(const int* sched5) {
+  NEED_CTX();
+  if (!sched5) return fail(SAM_GPU_EINVAL, "set_fft_schedule: null array");
+  for (int p = 0; p < 5; ++p)
+    if (sched5[p] != 0 && sched5[p] != 1) return fail(SAM_GPU_EINVAL, "FFT schedule %d of pass %d", sched5[p], p);
+  for (int p = 0; p < 5; ++p) c.sched[p] = sched5[p];
+  if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+  c.graph_stale = 1;
+  return 0;
+}
+
+int sam_gpu_fft_schedule(int* out5) {
+  NEED_CTX();
+  if (!out5) return fail(SAM_GPU_EINVAL, "fft_schedule: null array");
+  for (int p = 0; p < 5; ++p) out5[p] = c.sched[p];
+  return 0;
 }
 
 int sam_gpu_tiles(int* out6) {

@@ -29,7 +29,7 @@ EXPORTS = [
     "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
     "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
     "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
-    "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_planes",
+    "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_set_fft_schedule", "sam_gpu_fft_schedule", "sam_gpu_planes",
     "sam_gpu_set_forcing", "sam_gpu_set_les", "sam_gpu_les_coef",
     "sam_gpu_mlp_set", "sam_gpu_mlp_get", "sam_gpu_mlp_forward", "sam_gpu_mlp_grad", "sam_gpu_mlp_train",
     "sam_gpu_mma_selftest", "sam_gpu_box_filter", "sam_gpu_closure_inputs",
@@ -114,6 +114,8 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_get_mean.argtypes = [P, C.c_int, C.c_int, P, P, P]
     lib.sam_gpu_autotune.argtypes = [C.c_int]
     lib.sam_gpu_tiles.argtypes = [P]
+    lib.sam_gpu_set_fft_schedule.argtypes = [P]
+    lib.sam_gpu_fft_schedule.argtypes = [P]
     lib.sam_gpu_set_forcing.argtypes = [C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int)]
     lib.sam_gpu_set_les.argtypes = [C.c_int, C.c_double, C.c_double]
     lib.sam_gpu_mlp_set.argtypes = [P, C.c_int]
@@ -324,12 +326,29 @@ class SamGpu:
         return dict(zip(("z_inv", "y_inv", "x_pass", "y_fwd", "z_fwd"), [float(x) for x in ms]))
 
     def autotune(self, reps=3):
-        """Pick the fastest tiling of each pass on the resident state."""
+        """Pick the fastest tiling and FFT schedule of each pass on the
+        resident state; returns the choice."""
         self._check(load_library().sam_gpu_autotune(reps), "autotune")
         t = np.zeros(6, dtype=np.int32)
         self._check(load_library().sam_gpu_tiles(t.ctypes.data_as(C.c_void_p)), "tiles")
-        return dict(zip(("z_inv_rows", "y_inv_cols", "x_rows", "x_group", "y_fwd_planes", "z_fwd_rows"),
-                        [int(x) for x in t]))
+        out = dict(zip(("z_inv_rows", "y_inv_cols", "x_rows", "x_group", "y_fwd_planes", "z_fwd_rows"),
+                       [int(x) for x in t]))
+        out["fft_schedule"] = self.fft_schedule()
+        return out
+
+    def set_fft_schedule(self, sched):
+        """FFT schedule of the five passes (z inverse, y inverse, x, y forward,
+        z forward) for length-256 lines: 0 the 16 x 16 register path, 1
+        compile-time Stockham stages (8, 8, 4)."""
+        a = np.ascontiguousarray(sched, dtype=np.int32)
+        if a.shape != (5,):
+            raise ValueError("set_fft_schedule: five values")
+        self._check(load_library().sam_gpu_set_fft_schedule(a.ctypes.data_as(C.c_void_p)), "set_fft_schedule")
+
+    def fft_schedule(self):
+        a = np.zeros(5, dtype=np.int32)
+        self._check(load_library().sam_gpu_fft_schedule(a.ctypes.data_as(C.c_void_p)), "fft_schedule")
+        return [int(x) for x in a]
 
     def fp64_peak_tflops(self):
         t = C.c_double(0.0)

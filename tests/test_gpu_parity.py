@@ -128,6 +128,47 @@ def test_resident_stages(gpu_lib, grid):
         assert relerr(rg[: d.nz_min, ..., d.lu], r[: d.nz_min, ..., d.lu]) < TOL_ROUTINE
 
 
+# the grids with length-256 lines, run with the other FFT schedule of every
+# pass (compile-time Stockham 8, 8, 4 instead of the 16 x 16 register path)
+@pytest.mark.parametrize("grid", [g for g in GRIDS if 256 in (g["nx"], g["ny"], g["nz"])])
+def test_resident_stages_stockham_schedule(gpu_lib, grid):
+    g, o = pair(**grid)
+    d = o.d
+    g.set_fft_schedule([1, 1, 1, 1, 1])
+    assert g.fft_schedule() == [1, 1, 1, 1, 1]
+    u = o.init_random(43)
+    g.upload(u)
+    r = o.wave(d.lr)
+    for nrk in (1, 2, 3):
+        o.stage(u, r, nrk)
+        g.stage(nrk)
+        ug, rg = g.download(with_r=True)
+        for n in range(d.lu):
+            assert relerr(ug[: d.nz_min, ..., n], u[: d.nz_min, ..., n]) < TOL_ROUTINE, (nrk, n)
+            assert relerr(rg[: d.nz_min, ..., n], r[: d.nz_min, ..., n]) < TOL_ROUTINE, (nrk, n)
+
+
+def test_fft_schedules_agree_in_fp32(gpu_lib):
+    """FP32 bulk form, 256 x 256 x 12: one step with each schedule (FP32
+    round-off apart) and the rejection of an unknown schedule."""
+    cfg = dict(nx=256, ny=256, nz=12, i_strat=1, vis=1e-2, dt0=0.01, buoy_fac_z=1.0, lapse=1.0)
+    o = O.Oracle(**cfg)
+    u = o.init_random(5)
+    out = []
+    for sched in ([0, 0, 0, 0, 0], [1, 1, 1, 1, 1]):
+        g = SamGpu(precision=32, **cfg)
+        g.set_fft_schedule(sched)
+        g.upload(u)
+        g.step(1)
+        out.append(g.download())
+        if sched[0] == 1:
+            with pytest.raises(Exception):
+                g.set_fft_schedule([2, 0, 0, 0, 0])
+            assert g.fft_schedule() == [1, 1, 1, 1, 1]
+        g.close()
+    assert relerr(out[1], out[0]) < 1e-5
+
+
 def test_taylor_green_64_200_steps(gpu_lib):
     """Config 1: Taylor-Green 64^3, nu = 1/400, dt = 0.01, 200 RK3 steps."""
     cfg = dict(nx=64, ny=64, nz=64, vis=1.0 / 400, dt0=0.01)
