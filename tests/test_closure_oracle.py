@@ -73,3 +73,37 @@ def test_zero_network_is_smagorinsky():
         o.steps(u, r, 2)
         us.append(u)
     assert np.array_equal(us[0], us[1])
+
+
+def test_training_targets_recover_a_known_eddy_viscosity_and_diffusivity():
+    """closure_data.targets: filtered fields whose subgrid stress is exactly
+    -2 nu0 S (S traceless) and whose subgrid flux is exactly -kappa0 grad T
+    give C_nu* = nu0 / (delta^2 |S|) and C_kappa* = kappa0 / (delta^2 |S|)
+    (clipped to [0, C_MAX] in the first output, unclipped in the second)."""
+    from sam_gb300 import closure_data as CD
+
+    rng = np.random.default_rng(4)
+    shp = (6, 5, 4)
+    lu, dsq, nu0, kap0 = 4, 0.02, 3e-4, 5e-4
+    ub = rng.standard_normal(shp + (3,))
+    tb = rng.standard_normal(shp)
+    S = rng.standard_normal(shp + (6,))  # product order S11 S12 S22 S13 S23 S33
+    S[..., 5] = -(S[..., 0] + S[..., 2])
+    gT = rng.standard_normal(shp + (3,))
+    pairs = [(0, 0), (0, 1), (1, 1), (0, 2), (1, 2), (2, 2)]
+    filt = np.zeros(shp + (lu + 9,))
+    filt[..., :3] = ub
+    filt[..., 3] = tb
+    for m, (a, b) in enumerate(pairs):
+        filt[..., lu + m] = ub[..., a] * ub[..., b] - 2 * nu0 * S[..., m]
+    for a in range(3):
+        filt[..., lu + 6 + a] = ub[..., a] * tb - kap0 * gT[..., a]
+    grads = np.concatenate([S, gT], axis=-1)
+    clipped, raw, smag = CD.targets(np.asfortranarray(filt), np.asfortranarray(grads), lu, dsq)
+    ss = sum(w * S[..., m] ** 2 for m, w in enumerate([1, 2, 1, 2, 2, 1]))
+    smag_ref = np.sqrt(2 * ss).ravel(order="F")
+    np.testing.assert_allclose(smag, smag_ref, rtol=1e-12)
+    np.testing.assert_allclose(raw[:, 0], nu0 / (dsq * smag_ref), rtol=1e-9)
+    np.testing.assert_allclose(raw[:, 1], kap0 / (dsq * smag_ref), rtol=1e-9)
+    assert clipped.dtype == np.float32 and clipped.min() >= 0 and clipped.max() <= CD.C_MAX
+    np.testing.assert_allclose(clipped, np.clip(raw, 0, CD.C_MAX), rtol=1e-6)
