@@ -186,23 +186,58 @@ def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
 
 
-def cpu_oracle_rate(n, steps, threads, warm_stages=1):
-    """Steps/s of the oracle (C restatement of the reference path, OpenMP)."""
+def cpu_oracle_rate(n, steps, threads, warm_stages=1, u_start=None):
+    """Steps/s of the oracle (C restatement of the reference path, OpenMP)
+    over `steps` steps from the workload's start (or u_start); also returns
+    the state after them.  The warm-up stages run on a copy."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     O.build()
     cfg = workload_cfg(n)
     cfg.pop("precision")
     o = O.Oracle(nthreads=threads, **cfg)
-    u = o.init_packet(PACKET["seed"], PACKET["k0"], PACKET["sigma"], PACKET["amplitude"], PACKET["noise"])
-    r = o.wave(o.d.lr)
+    if u_start is None:
+        u = o.init_packet(PACKET["seed"], PACKET["k0"], PACKET["sigma"], PACKET["amplitude"], PACKET["noise"])
+    else:
+        u = u_start.copy(order="F")
+    uw, rw = u.copy(order="F"), o.wave(o.d.lr)
     for s in range(warm_stages):
-        o.stage(u, r, 1)
+        o.stage(uw, rw, 1)
+    o.close()
+    o = O.Oracle(nthreads=threads, **cfg)
+    r = o.wave(o.d.lr)
     t0 = time.perf_counter()
     o.steps(u, r, steps)
     dt = time.perf_counter() - t0
+    st = o.stats()
+    nz_min = o.d.nz_min
     o.close()
-    return steps / dt, dt
+    return steps / dt, dt, u, st, nz_min
+
+
+def parity_vs_oracle(u_start, u_oracle, st_oracle, nz_min, steps, stream):
+    """The same `steps` steps on the GPU from u_start (FP64 drop-in and FP32
+    bulk, fresh contexts) against the oracle's state: the largest error per
+    field relative to the field's largest coefficient, the CFL dt and the
+    divergence of the result."""
+    import numpy as np
+    from sam_gb300 import SamGpu
+    out = {"steps": steps, "bar_fp64": 1e-12,
+           "measure": "max |u_gpu - u_oracle| / max |u_oracle| per field (Nz_min rows)"}
+    for name, prec in (("fp64", 64), ("fp32_bulk", 32)):
+        g = SamGpu(**workload_cfg(precision=prec))
+        g.set_stream(stream.cuda_stream)
+        g.upload(u_start)
+        g.step(steps)
+        ug = g.download()
+        err = [float(np.abs(ug[:nz_min, ..., n] - u_oracle[:nz_min, ..., n]).max()
+                     / np.abs(u_oracle[:nz_min, ..., n]).max()) for n in range(u_oracle.shape[-1])]
+        st = g.stats()
+        out[name] = {"max_rel_err_per_field": err, "dt_rel_diff": abs(st["dt"] - st_oracle["dt"]) / st_oracle["dt"],
+                     "div_max": g.div_check()["div_max"]}
+        g.close()
+    out["fp64_within_bar"] = max(out["fp64"]["max_rel_err_per_field"]) <= 1e-12
+    return out
 
 
 def band_errors(u, ref):
@@ -397,13 +432,60 @@ def run_probe(args):
     return 0
 
 
+def run_parity_curve(args):
+    """Error of the GPU forms against the oracle versus step count on the
+    128^3 stratified decaying-turbulence configuration (N = 1, Pr = 1,
+    nu = 1/800, k^4 exp(-2 (k/4)^2) start at rms 1 with theta at 0.1, CFL
+    0.5), seeds 0, 1, 2: max over fields of max |u_gpu - u_oracle| / max
+    |u_oracle| every `every` steps up to args.parity_curve steps; one JSON
+    line.  Diagnostic mode (no timing)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    from sam_gb300 import SamGpu, build as B
+    B.build()
+    O.build()
+    cfg = dict(nx=128, ny=128, nz=128, i_strat=1, i_cfl=1, cfl0=0.5, vis=1.0 / 800, pr=1.0, buoy_fac_z=1.0,
+               lapse=1.0)
+    every = 25
+    out = {"parity_curve": "128^3 stratified decaying turbulence, config of the 500-step run", "every": every,
+           "measure": "max over fields of max|u_gpu - u_oracle| / max|u_oracle| (Nz_min rows)", "seeds": {}}
+    for seed in (0, 1, 2):
+        o = O.Oracle(**cfg)
+        u = o.init_random(seed, 6, 1.0, 6, 0.1)
+        r = o.wave(o.d.lr)
+        gs = {}
+        for prec in (64, 32):
+            g = SamGpu(precision=prec, **cfg)
+            g.upload(u)
+            gs[prec] = g
+        rows = []
+        done = 0
+        while done < args.parity_curve:
+            o.steps(u, r, every)
+            done += every
+            row = {"step": done, "time": o.stats()["time"]}
+            for prec, g in gs.items():
+                g.step(every)
+                ug = g.download()
+                row[f"fp{prec}"] = max(float(np.abs(ug[:o.d.nz_min, ..., n] - u[:o.d.nz_min, ..., n]).max()
+                                             / np.abs(u[:o.d.nz_min, ..., n]).max()) for n in range(o.d.lu))
+            rows.append(row)
+        for g in gs.values():
+            g.close()
+        o.close()
+        out["seeds"][str(seed)] = rows
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_reference(args):
     rank, _, ws = dist_env()
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
     steps = max(1, min(args.steps, 20))
-    rate, secs = cpu_oracle_rate(N, steps, threads, warm_stages=min(args.warmup, 3))
+    rate, secs, _, _, _ = cpu_oracle_rate(N, steps, threads, warm_stages=min(args.warmup, 3))
     sample = f"{steps} full RK3 steps of the 256^3 workload after {min(args.warmup, 3)} warm-up stage(s)"
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "steps/s", "n_gpus": args.gpus,
             "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 / rate, "higher_is_better": True,
@@ -434,6 +516,8 @@ def main():
                     help="profiling case: the workload's start state and 3 steps only (no timing, autotune or "
                          "baselines); with --les 3 the learned-closure LES start")
     ap.add_argument("--les", type=int, default=0, help="closure model of the --probe run")
+    ap.add_argument("--parity-curve", type=int, default=0,
+                    help="diagnostic: GPU-vs-oracle error every 25 steps up to this many steps at 128^3")
     args = ap.parse_args()
     global N, WORKLOAD
     if args.grid != N:
@@ -443,6 +527,8 @@ def main():
         return run_reference(args)
     if args.probe:
         return run_probe(args)
+    if args.parity_curve:
+        return run_parity_curve(args)
 
     rank, local_rank, ws = dist_env()
     if ws > 1:
@@ -559,13 +645,16 @@ def main():
     if not args.no_ensemble:
         ens = ensemble_form(max(4, K // 2), W)
 
-    # ---- CPU baseline: the oracle on the host cores, bounded sample
+    # ---- CPU baseline: the oracle on the host cores, bounded sample; its
+    # final state is the parity reference of the same steps on the GPU
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
-        rate, secs = cpu_oracle_rate(N, 2, threads)
+        rate, secs, u_or, st_or, nz_min = cpu_oracle_rate(N, 2, threads, u_start=u_init)
         cpu = {"value": rate, "unit": "steps/s", "cores": threads, "kind": "port",
                "sample": f"2 full RK3 steps of the same 256^3 workload ({secs:.1f} s), oracle C restatement"}
+        parity = parity_vs_oracle(u_init, u_or, st_or, nz_min, 2, stream)
 
     if rank != 0:
         return 0
@@ -575,14 +664,16 @@ def main():
     x_ms = passes["x_pass"]
     achieved = xb / (x_ms / 1e3) / 1e9
     tr = profile_traffic()
-    roofline = {"bound": "hbm", "kernel": "k_x_pass<double> (C2R, vel_max, 9 products, R2C)",
-                "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-                "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks else "fallback",
+    alu = x_pass_flops() / (x_ms / 1e3) / 1e12
+    roofline = {"bound": "fp64_alu", "kernel": "k_x_pass<double> (C2R, vel_max, 9 products, R2C)",
+                "achieved": alu, "peak": fp64_peak, "unit": "TFLOP/s", "frac": alu / fp64_peak,
+                "peak_source": "FP64 FMA peak measured live in this run (DFMA loop); not in MEASURED_PEAKS.json",
+                "flops_per_launch": x_pass_flops(),
                 "traffic": tr.get("bytes_per_launch") if tr else None,
-                "algorithmic_bytes_per_launch": xb,
-                "fp64_alu": {"achieved_tflops": x_pass_flops() / (x_ms / 1e3) / 1e12, "peak_tflops": fp64_peak,
-                             "frac": x_pass_flops() / (x_ms / 1e3) / 1e12 / fp64_peak,
-                             "note": "the FP64 drop-in is bound by GB300's FP64 ALU rate, measured live here"},
+                "hbm": {"achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
+                        "algorithmic_bytes_per_launch": xb,
+                        "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)" if "hbm_gbs" in peaks
+                        else "fallback"},
                 "passes_ms": passes}
     if fp32 is not None:
         # the FP32 form's dominant kernel against the same HBM peak
@@ -594,7 +685,7 @@ def main():
                             "achieved": a32, "peak": hbm_peak, "unit": "GB/s", "frac": a32 / hbm_peak,
                             "traffic": tr32.get("bytes_per_launch") if tr32 else None,
                             "algorithmic_bytes_per_launch": xb32, "ms": x32_ms,
-                            "note": "instruction- and latency-bound (ncu: issue 62-64 %, FP32 pipes 29-33 %)"}
+                            "note": "instruction- and latency-bound: counters in profiles/x_pass_256_ncu.md"}
     ms_step = ms / K
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -605,7 +696,8 @@ def main():
                        "grid_point_updates_per_s": value * N ** 3,
                        "hbm_gbs_step": algorithmic_bytes_per_step() / (ms_step / 1e3) / 1e9,
                        "dt_final": st["dt"], "tiles": tiles},
-            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches_per_step * K,
+            "roofline": roofline, "cpu_baseline": cpu, "parity_vs_oracle": parity, "e2e": e2e,
+            "gpu_launches": launches_per_step * K,
             "clocks": clk.summary(), "fp32_bulk": fp32, "les": les, "ensemble": ens}
     print(json.dumps(line), flush=True)
     return 0

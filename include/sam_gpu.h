@@ -35,7 +35,7 @@ typedef struct sam_gpu_config {
   int nx, ny, nz;     /* Nx, Ny, Nz; Nx even */
   int n_dealias;      /* 0, 1 (2/3 rule), 2 (init.f:49-62) */
   int i_strat;        /* 0: Lu=3, Lr=6;  1: Lu=4, Lr=9 (init.f:35-41) */
-  int i_cfl;          /* 1: dt from the CFL number (vel_max.f:187-192) */
+  int i_cfl;          /* 1: dt from the CFL number (vel_max.f:40-45) */
   int nrk_max;        /* 1, 2 or 3 (init.f:117-145) */
   int rot_sav;        /* 1 for the tilted-box wave, i_prob = 4 (sam.f:176-185) */
   int i_les;          /* Chollet-Lesieur spectra (spectra.f:21) */
@@ -74,7 +74,7 @@ const char* sam_gpu_error_string(void);
 /* ---- per-routine drop-ins (host arrays, reference layouts) ---- */
 /* z_trans_b.f:1  u1(Nze,Ny_min,nxp,n_var) -> u2 blocks (Ny_min,nxp,Nze,n_var);
  * isymm(n_var) must be 0 (the sine/cosine branches of the reference use
- * undefined variables, z_trans_b.f:256,260). u_c, u_r, u_i are workspace and
+ * undefined variables, z_trans_b.f:58,62,80,84). u_c, u_r, u_i are workspace and
  * may be NULL. */
 int sam_gpu_z_trans_b(const double* u1, double* u2, int n_var, const int* isymm, double* u_c, double* u_r,
                       double* u_i);
@@ -169,7 +169,7 @@ int sam_gpu_measure_fp64_peak(double* tflops);
 /* ---- vel_max for callers that cannot allocate device memory ----
  * No counterpart in the reference.  For callers that own all device memory
  * through another allocator, or must not stall a step loop on cudaMalloc:
- * same sums as vel_max.f:156-181, but u_dev (real (Nx,Ny,nzp,Lu)) and
+ * same sums as vel_max.f:11-34, but u_dev (real (Nx,Ny,nzp,Lu)) and
  * stats_dev (16 doubles: u_avg[4], u_var[4], u_max[4], energy, count of
  * non-finite values, 2 unused) are DEVICE pointers, and the per-plane
  * partial sums live in a 512 KB array compiled into the library (held on

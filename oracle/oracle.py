@@ -7,7 +7,7 @@ CUDA library never calls it.
 
 Arrays follow the reference layouts in Fortran order:
   wave space   complex128 (Nze, Ny_min, Nx_min, n)   sam.f:93
-  z_trans_b    complex128 (Ny_min, Nx_min, Nze, n)   z_trans_b.f:203
+  z_trans_b    complex128 (Ny_min, Nx_min, Nze, n)   z_trans_b.f:10-13
   x2z output   complex128 (Ny, Nx/2, Nz, n)          x2z_decomp.f:17
   physical     float64    (Nx, Ny, Nz, n)            sam.f:94
 """

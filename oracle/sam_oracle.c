@@ -8,7 +8,7 @@
  *
  * Layout helpers (0-based, Fortran column-major, nxp = Nx_min, nzp = Nze):
  *   W(k,j,i,n)  wave space  (Nze, Ny_min, Nx_min, n)     sam.f:93
- *   ZB(j,i,k,n) z_trans_b   (Ny_min, Nx_min, Nze, n)     z_trans_b.f:203
+ *   ZB(j,i,k,n) z_trans_b   (Ny_min, Nx_min, Nze, n)     z_trans_b.f:10-13
  *   XY(j,i,k,n) x2z output  (Ny, Nx/2, Nz, n) complex    x2z_decomp.f:17
  *   P(i,j,k,n)  physical    (Nx, Ny, Nz, n) real         sam.f:94
  */
@@ -84,7 +84,7 @@ static void set_threads(const so_ctx *c) {
 /* ------------------------------------------------------------------ setup */
 
 /* init.f:49-73 (kmax, minimal dims), init.f:117-145 (RK coefficients),
- * fft_init.f:324-359 (scales, integer wave numbers), sam.f:68-69 (Lm). */
+ * fft_init.f:41-78 (scales, integer wave numbers), sam.f:68-69 (Lm). */
 so_ctx *so_create(const so_config *cfg) {
   if (cfg->nx < 2 || cfg->nx % 2 || cfg->ny < 1 || cfg->nz < 1) return NULL;
   so_ctx *c = (so_ctx *)calloc(1, sizeof(so_ctx));
@@ -177,7 +177,7 @@ void so_stats(const so_ctx *c, double *o) {
 
 /* ------------------------------------------------------------- transforms */
 
-/* z_trans_b.f:213-250 (isymm = 0): pad kz to Nz, cfftb, scatter into the
+/* z_trans_b.f:26-52 (isymm = 0): pad kz to Nz, cfftb, scatter into the
  * (Ny_min, nxp, Nze, n_var) block layout. */
 int so_z_trans_b(so_ctx *c, const double *u1d, double *u2d, int n_var) {
   const so_cplx *u1 = (const so_cplx *)u1d;
@@ -229,7 +229,7 @@ int so_x2z_decomp(so_ctx *c, const double *u1d, double *u2d, int n_var) {
   return 0;
 }
 
-/* xy_trans_b.f:71-123: per (z, var) plane, cfftb along y for kx <= kx_max
+/* xy_trans_b.f:11-63: per (z, var) plane, cfftb along y for kx <= kx_max
  * (in place in u1), pack into the rfft layout (real part only for kx = 0),
  * zero kx > kx_max, rfftb along x.  u1 and u2 may be the same array. */
 int so_xy_trans_b(so_ctx *c, double *u1d, double *u2, int n_var) {
@@ -314,7 +314,7 @@ int so_z2x_decomp(so_ctx *c, const double *u1, double *u2, int n_var) {
   return 0;
 }
 
-/* z_trans_f.f:138-157 (isymm = 0): cfftf along z, keep |kz| <= kz_max scaled
+/* z_trans_f.f:21-31 (isymm = 0): cfftf along z, keep |kz| <= kz_max scaled
  * by 1/Nz in the first Nz_min rows. */
 int so_z_trans_f(so_ctx *c, double *ud, int n_var) {
   so_cplx *u = (so_cplx *)ud;
@@ -340,7 +340,7 @@ int so_z_trans_f(so_ctx *c, double *ud, int n_var) {
 
 /* ---------------------------------------------------------------- physics */
 
-/* vel_max.f:156-196: FP64 sum, sum of squares and max |u| per field, then
+/* vel_max.f:11-49: FP64 sum, sum of squares and max |u| per field, then
  * averages, variances, energy, CFL numbers and (i_cfl = 1) the new dt. */
 int so_vel_max(so_ctx *c, const double *u) {
   const size_t np = (size_t)c->nx * c->ny * c->nz;
@@ -587,7 +587,7 @@ int so_spectra(so_ctx *c, const double *ud, const double *rd, double *out) {
   return 0;
 }
 
-/* div_check.f:123-150 */
+/* div_check.f:11-36 */
 int so_div_check(so_ctx *c, const double *ud, double *o) {
   const so_cplx *u = (const so_cplx *)ud;
   double s[4] = {0, 0, 0, 0};
@@ -610,7 +610,7 @@ int so_div_check(so_ctx *c, const double *ud, double *o) {
   return 0;
 }
 
-/* cl_energy.f:161-195.  Rows beyond Nz_min of the padded z dimension are the
+/* cl_energy.f:8-43.  Rows beyond Nz_min of the padded z dimension are the
  * reference's padding; they are read as stored (zero after read_field). */
 double so_cl_energy(so_ctx *c, const double *ud) {
   const so_cplx *u = (const so_cplx *)ud;
@@ -641,7 +641,7 @@ double so_cl_energy(so_ctx *c, const double *ud) {
   return sum_e;
 }
 
-/* get_mean.f:207-255 (i_symm = 0): horizontal-mean profile through rfftb in z
+/* get_mean.f:8-56 (i_symm = 0): horizontal-mean profile through rfftb in z
  * and the linear-jump estimate; i_remove = 1 subtracts the jump's linear
  * profile from the kx = ky = 0 column. */
 double so_get_mean(so_ctx *c, double *ud, int i_remove, double *u_mean) {
@@ -732,7 +732,7 @@ int so_y_deriv(so_ctx *c, const double *u, double *du) {
  * filter.f, sm.f, dm.f include a header (speciso.h) that the reference does
  * not ship.  Its symbols are defined here from their use:
  *   Lx = Nx+2, Ly = Ny+2, Lz = Nz+2 (periodic halo planes 1 and N+2,
- *     periodicity.f:215-239);
+ *     periodicity.f:7-32);
  *   ifact = (1,1,1,2,2,2) for the symmetric tensor (S11,S22,S33,S12,S23,S13);
  *   ip = (1,2,3,1,2,1), jp = (1,2,3,2,3,3) the index pairs of that tensor;
  *   alpha_sq = 4 (test-to-grid filter width ratio 2 for the 1-4-1 filter);
@@ -747,7 +747,7 @@ static const int SO_IP[6] = {0, 1, 2, 0, 1, 0};
 static const int SO_JP[6] = {0, 1, 2, 1, 2, 2};
 static const double SO_ALPHA_SQ = 4.0;
 
-/* periodicity2.f:250-262 on a plane array f(Lx,Ly,n_var) */
+/* periodicity2.f:7-19 on a plane array f(Lx,Ly,n_var) */
 static void periodicity2(const so_ctx *c, double *f, int n_var) {
   const int nx = c->nx, ny = c->ny;
   const size_t pl = (size_t)(nx + 2) * (ny + 2);
@@ -758,7 +758,7 @@ static void periodicity2(const so_ctx *c, double *f, int n_var) {
   }
 }
 
-/* periodicity.f:215-239 on a volume f(Lx,Ly,Lz) */
+/* periodicity.f:7-32 on a volume f(Lx,Ly,Lz) */
 static void periodicity3(const so_ctx *c, double *f) {
   const int nx = c->nx, ny = c->ny, nz = c->nz;
   for (int j = 1; j <= ny; ++j)
@@ -798,7 +798,7 @@ int so_filter(so_ctx *c, const double *f_bar, double *f_hat, int n_var) {
   return 0;
 }
 
-/* the staggered-to-centre velocity of one haloed plane kk (sm.f:147-157) */
+/* the staggered-to-centre velocity of one haloed plane kk (sm.f:45-51) */
 static void centre_plane(const so_ctx *c, const double *u, int kk, double *ub) {
   const int nx = c->nx, ny = c->ny;
   const size_t pl = (size_t)(nx + 2) * (ny + 2), vol = pl * (c->nz + 2);
@@ -811,7 +811,7 @@ static void centre_plane(const so_ctx *c, const double *u, int kk, double *ub) {
   periodicity2(c, ub, 3);
 }
 
-/* strain of the centre plane from three u_bar planes lo/mid/hi (sm.f:161-178) */
+/* strain of the centre plane from three u_bar planes lo/mid/hi (sm.f:57-75) */
 static void strain_plane(const so_ctx *c, const double *lo, const double *mid, const double *hi, double *sb) {
   const int nx = c->nx, ny = c->ny;
   const size_t pl = (size_t)(nx + 2) * (ny + 2);
@@ -837,7 +837,7 @@ static double delta_sq_of(const so_ctx *c) {
   return pow(dx * dy * dz, 2.0 / 3.0);
 }
 
-/* sm.f:134-205: conventional Smagorinsky nu_t = c_smag delta^2 |S| */
+/* sm.f:41-101: conventional Smagorinsky nu_t = c_smag delta^2 |S| */
 int so_sm(so_ctx *c, const double *u, double *vt) {
   const int nx = c->nx, ny = c->ny, nz = c->nz;
   const size_t pl = (size_t)(nx + 2) * (ny + 2);
@@ -1228,7 +1228,7 @@ int so_write_field(so_ctx *c, const char *fname, const double *ud) {
   return 0;
 }
 
-/* read_field.f:61-100: size check, then the records; rows above Nz_min zeroed */
+/* read_field.f:37-52: size check, then the records; rows above Nz_min zeroed */
 int so_read_field(so_ctx *c, const char *fname, double *ud) {
   so_cplx *u = (so_cplx *)ud;
   FILE *f = fopen(fname, "rb");

@@ -32,7 +32,7 @@ typedef struct so_config {
   int nx, ny, nz;
   int n_dealias; /* init.f:49-62 (0, 1, 2) */
   int i_strat;   /* 0: Lu=3/Lr=6, 1: Lu=4/Lr=9 (init.f:35-41) */
-  int i_cfl;     /* vel_max.f:187-192 */
+  int i_cfl;     /* vel_max.f:40-45 */
   int nrk_max;   /* 1, 2, 3 (init.f:117-145) */
   int rot_sav;   /* 1 for the tilted-box gravity wave (sam.f:176-185) */
   int i_les;     /* Chollet-Lesieur spectra (init.f:88-93, spectra.f:21) */
@@ -122,7 +122,7 @@ int so_mlp_set(so_ctx *c, const float *params);
 void so_closure_invariants(const double *S, const double *g, const double *w, double bz, double n2, double dsq,
                            double nu, float *f);
 int so_write_field(so_ctx *c, const char *fname, const double *u);
-/* 0 ok, -1 open, -2 wrong size (read_field.f:74-80), -3 short read */
+/* 0 ok, -1 open, -2 wrong size (read_field.f:26-32), -3 short read */
 int so_read_field(so_ctx *c, const char *fname, double *u);
 
 /* ---- planes output (sam.f:145-166, write_planes.f): u and p = r(Lu+1) in

@@ -11,8 +11,9 @@
 // ReLU epilogue writes the next layer's BF16 operand into shared memory (the
 // biases are in the MMAs, against constant-1 input columns).  Three MMA
 // groups per tile (K = 16, then 5 x K = 16 twice).  Every wait is bounded:
-// on timeout the kernel sets *err, waits for its loads in flight, frees its
-// TMEM and returns.
+// on timeout the kernel sets *err, waits (bounded again) for its TMA load and
+// its MMA group still in flight, frees its TMEM and returns; the outputs of a
+// launch that timed out are undefined.
 //
 // Training: the backward pass of the loss mean (C - y)^2 and Adam run on the
 // CUDA cores in FP32 (the network is small; the weight gradients are
@@ -25,6 +26,7 @@
 #include <stdint.h>
 
 #include "closure.cuh"
+#include "common.cuh"
 #include "tc05.cuh"
 
 namespace samgpu {
@@ -183,12 +185,16 @@ __global__ void __launch_bounds__(128 * kMlpWG, kMlpFwdCtas)
   uint32_t mph = 0, tph = 0;
   int bad = 0;
   bool pend = first < ntiles;  // a TMA load not yet waited for (the same in every thread of the warpgroup)
+  bool mpend = false;          // an MMA group committed and not yet waited for
   // one thread polls each barrier; the warpgroup's named barrier releases
   // the others and makes bad the same in all of them
   auto wait_mma = [&]() {
     int b = r == 0 ? mbar_wait(&S.mbar[g], mph) : 0;
-    mph ^= 1u;
     b = bar_named_or(bid, 128, b);
+    if (!b) {
+      mph ^= 1u;
+      mpend = false;
+    }
     tc_fence_after();
     return b;
   };
@@ -212,6 +218,7 @@ __global__ void __launch_bounds__(128 * kMlpWG, kMlpFwdCtas)
       mma_bf16(tm, sdesc(sa1, 2048, 128), sdesc(w1, 128, 256), id64, 0);
       mma_commit(&S.mbar[g]);
     }
+    mpend = true;
     if ((bad = wait_mma())) break;
     // the input tile has been read: the next one loads during this tile's chain
     const long long tn = t + nslots;
@@ -227,6 +234,7 @@ __global__ void __launch_bounds__(128 * kMlpWG, kMlpFwdCtas)
         mma_bf16(tm, sdesc(sa2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w2 + 256 * kk, 128, kMlpK2 * 16), id64, kk > 0);
       mma_commit(&S.mbar[g]);
     }
+    mpend = true;
     if ((bad = wait_mma())) break;
     epilogue(tl, a2, r, h2g, row, live);
     to_mma();
@@ -237,6 +245,7 @@ __global__ void __launch_bounds__(128 * kMlpWG, kMlpFwdCtas)
         mma_bf16(tm, sdesc(sa2 + 256 * kk, 128, kMlpK2 * 16), sdesc(w3 + 256 * kk, 128, kMlpK2 * 16), id16, kk > 0);
       mma_commit(&S.mbar[g]);
     }
+    mpend = true;
     if ((bad = wait_mma())) break;
     float o[2];
     tmem_ld2(tl, o);
@@ -253,8 +262,10 @@ __global__ void __launch_bounds__(128 * kMlpWG, kMlpFwdCtas)
     tc_fence_after();
   }
   if (bad && r == 0) atomicExch(err, 1);
-  // a load still in flight (the loop left early) completes before exit
+  // a load or an MMA group still in flight (the loop left early) completes
+  // before the shared memory and the TMEM it uses are released
   if (pend && r == 0) mbar_wait(&S.tbar[g], tph);
+  if (mpend && r == 0) mbar_wait(&S.mbar[g], mph);
   tc_fence_before();
   __syncthreads();
   if (tid < 32) {
@@ -292,7 +303,7 @@ static bool x16_map(const __nv_bfloat16* x16, long long n, CUtensorMap* m) {
 int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2* coef, const MlpBatch* batch,
                 int* err, cudaStream_t s) {
   const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
-  long long grid = 152 * kMlpFwdCtas;  // persistent: one wave
+  long long grid = (long long)sm_count() * kMlpFwdCtas;  // persistent: one wave
   if (grid > (ntiles + kMlpWG - 1) / kMlpWG) grid = (ntiles + kMlpWG - 1) / kMlpWG;
   if (grid < 1) return 0;
   CUtensorMap m;
@@ -358,7 +369,7 @@ __global__ void k_features_bf16(const float* __restrict__ f, __nv_bfloat16* __re
 
 void mlp_features_bf16(const float* f, __nv_bfloat16* x16, long long n, cudaStream_t s) {
   long long g = (n * kMlpK1 + 255) / 256;
-  if (g > 152 * 32) g = 152 * 32;
+  if (g > sm_count() * 32) g = sm_count() * 32;
   if (g < 1) g = 1;
   k_features_bf16<<<(int)g, 256, 0, s>>>(f, x16, n);
 }

@@ -10,7 +10,7 @@ namespace samgpu {
 
 // Geometry of one run.  Wave space keeps kx in [0, kx_max] (Nx_min modes),
 // ky and kz in [-k_max, k_max] stored non-negative first (Ny_min, Nz_min
-// modes), as fft_init.f:333-353 orders them.
+// modes), as fft_init.f:52-72 orders them.
 struct Grid {
   int nx, ny, nz, nze;
   int mx, my, mz;
@@ -39,13 +39,27 @@ struct StageConsts {
 };
 
 // Signed wave number of stored index j along a direction with k_max = km and
-// m = 2 km + 1 stored modes (fft_init.f:339-353).
+// m = 2 km + 1 stored modes (fft_init.f:57-72).
 __device__ __forceinline__ int kwave(int j, int km, int m) { return j <= km ? j : j - m; }
 
 // Position in an FFT line of length n of stored index j (zero band removed).
 __device__ __forceinline__ int kpos(int j, int km, int m, int n) { return j <= km ? j : j + (n - m); }
 
 constexpr int kThreads = 256;
+
+// Streaming multiprocessors of the current device (looked up once per
+// device): persistent and grid-stride launches are sized in multiples of it.
+inline int sm_count() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (!cache[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n < 1) n = 1;
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
 
 // Records the message returned by sam_gpu_error_string(); returns code.
 int set_error(int code, const char* msg);

@@ -1,6 +1,6 @@
 // Diagnostics on the resident wave-space state, in FP64 whatever the working
-// precision: shell spectra (spectra.f:13-90), divergence (div_check.f:123-150),
-// cut-off shell energy (cl_energy.f:161-195); and the plane derivatives of the
+// precision: shell spectra (spectra.f:13-90), divergence (div_check.f:11-36),
+// cut-off shell energy (cl_energy.f:8-43); and the plane derivatives of the
 // output path (x_deriv.f:7-25, y_deriv.f:7-28).
 #include <cuda_runtime.h>
 #include <math.h>
@@ -337,9 +337,7 @@ __global__ void k_dfma(double* out, int iters, double a, double b) {
 }
 
 double diag_fp64_peak(cudaStream_t s) {
-  int sms = 0;
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, 0);
-  const int blocks = sms * 2, threads = 256, iters = 20000;
+  const int blocks = sm_count() * 2, threads = 256, iters = 20000;
   double* out = nullptr;
   if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return 0.0;
   cudaEvent_t e0, e1;

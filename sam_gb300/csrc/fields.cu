@@ -206,7 +206,7 @@ __global__ void k_convert_out(const cx_t<T>* __restrict__ src, double2* __restri
 
 static int grid_for(long long n) {
   long long g = (n + kThreads - 1) / kThreads;
-  if (g > 152 * 32) g = 152 * 32;
+  if (g > sm_count() * 32) g = sm_count() * 32;
   if (g < 1) g = 1;
   return (int)g;
 }

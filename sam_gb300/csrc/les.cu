@@ -4,7 +4,7 @@
 // filter.f, sm.f and dm.f include a header the reference does not ship
 // (speciso.h).  Its symbols are defined from their use:
 //   Lx = Nx+2, Ly = Ny+2, Lz = Nz+2: planes 1 and N+2 are periodic halos
-//     (periodicity.f:215-239);
+//     (periodicity.f:7-32);
 //   ifact = (1,1,1,2,2,2) over the symmetric tensor (S11,S22,S33,S12,S23,S13);
 //   ip = (1,2,3,1,2,1), jp = (1,2,3,2,3,3): index pairs of that tensor;
 //   alpha_sq = 4: (test/grid filter width)^2 for the 1-4-1 test filter;
@@ -68,7 +68,7 @@ __global__ void k_filter(const double* __restrict__ f_bar, double* __restrict__ 
   }
 }
 
-// ---- staggered-to-centre velocity u_bar on the interior (sm.f:149-155)
+// ---- staggered-to-centre velocity u_bar on the interior (sm.f:47-49)
 __global__ void k_ubar(const double* __restrict__ u, double* __restrict__ ub, Halo H) {
   const long long n = H.ninterior(), vol = H.vol();
   for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n; e += (long long)gridDim.x * blockDim.x) {
@@ -79,7 +79,7 @@ __global__ void k_ubar(const double* __restrict__ u, double* __restrict__ ub, Ha
   }
 }
 
-// strain (sm.f:161-178) at interior point (x, y, z) from periodic u_bar
+// strain (sm.f:57-75) at interior point (x, y, z) from periodic u_bar
 __device__ __forceinline__ void strain(const double* __restrict__ ub, const Halo& H, int x, int y, int z, double dxi,
                                        double dyi, double dzi, double* s) {
   const long long n = H.ninterior();
@@ -98,7 +98,7 @@ __device__ __forceinline__ double smag(const double* s) {
   return sqrt(2.0 * sum);
 }
 
-// sm.f:181-190: vt = c_smag delta^2 |S| on the interior of the haloed output
+// sm.f:77-86: vt = c_smag delta^2 |S| on the interior of the haloed output
 __global__ void k_sm(const double* __restrict__ ub, double* __restrict__ vt, Halo H, double c_delta_sq, double dxi,
                      double dyi, double dzi) {
   const long long n = H.ninterior();
@@ -110,7 +110,7 @@ __global__ void k_sm(const double* __restrict__ ub, double* __restrict__ vt, Hal
   }
 }
 
-// periodicity.f:215-239 on a haloed volume (every halo point from its image)
+// periodicity.f:7-32 on a haloed volume (every halo point from its image)
 __global__ void k_periodic3(double* __restrict__ f, Halo H) {
   const long long tot = H.vol();
   const int lx = H.nx + 2, ly = H.ny + 2;
@@ -211,7 +211,7 @@ __global__ void k_dm_vt(const double* __restrict__ q, const double* __restrict__
   }
 }
 
-// ---- get_mean.f:207-255 (i_symm = 0) on the kx = ky = 0 column.  One CTA;
+// ---- get_mean.f:8-56 (i_symm = 0) on the kx = ky = 0 column.  One CTA;
 // line 0 of the shared tile holds the synthesis, line 1 the linear profile.
 __global__ void k_get_mean(double2* __restrict__ col, int mz, int kz, int nz, int i_remove,
                            const FftPlan* __restrict__ gpl, const double2* __restrict__ gtw,
@@ -252,7 +252,7 @@ __global__ void k_get_mean(double2* __restrict__ col, int mz, int kz, int nz, in
     __syncthreads();
     if (pass == 1 || i_remove != 1) break;
     // the linear profile jump (k/Nz - 1/2), rfftf, and its first kz_max+1
-    // packed entries scaled by 1/Nz (get_mean.f:224-231)
+    // packed entries scaled by 1/Nz (get_mean.f:24-32)
     const double jump = s_jump;
     __syncthreads();
     for (int p = threadIdx.x; p < nz; p += blockDim.x) ln[sidx(p)] = make_double2(jump * ((double)p * nz_inv - 0.5), 0.0);
@@ -284,7 +284,7 @@ __global__ void k_get_mean(double2* __restrict__ col, int mz, int kz, int nz, in
 
 static int grid_of(long long n) {
   long long g = (n + kThreads - 1) / kThreads;
-  if (g > 152 * 16) g = 152 * 16;
+  if (g > sm_count() * 16) g = sm_count() * 16;
   return (int)(g < 1 ? 1 : g);
 }
 
@@ -324,7 +324,7 @@ void les_dm(const double* u, double* ub, double* q, double* part, double* cds, d
 
 // ---- coupled dynamic closure: the physical velocity P(n, z, y, x) of the
 // x pass (working precision) into dm.f's haloed FP64 layout u(Lx,Ly,Lz,3),
-// halo planes filled with the periodic images (periodicity.f:215-239)
+// halo planes filled with the periodic images (periodicity.f:7-32)
 template <typename T>
 __global__ void k_pack_halo(const T* __restrict__ phys, double* __restrict__ uh, Halo H) {
   const long long vol = H.vol(), tot = 3 * vol;

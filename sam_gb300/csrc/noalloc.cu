@@ -34,7 +34,7 @@ namespace samgpu {
 // four partials (sum, sum of squares, max |u|, non-finite count).
 static __device__ __align__(256) double g_noalloc_partials[SAM_GPU_NOALLOC_MAX_PLANES * 4 * 4];
 
-// vel_max.f:158-168 for one z plane per CTA.
+// vel_max.f:11-21 for one z plane per CTA.
 __global__ void k_noalloc_plane_sums(const double* __restrict__ u, long long plane, long long field, int nzp, int lu,
                                      double* __restrict__ part) {
   __shared__ double red[4][kThreads];
@@ -65,7 +65,7 @@ __global__ void k_noalloc_plane_sums(const double* __restrict__ u, long long pla
   }
 }
 
-// vel_max.f:175-181: averages, variances, maxima and energy, summed over the
+// vel_max.f:28-34: averages, variances, maxima and energy, summed over the
 // planes in a fixed order.
 __global__ void k_noalloc_finish(const double* __restrict__ part, int nzp, int lu, double inv_n,
                                  double* __restrict__ out) {

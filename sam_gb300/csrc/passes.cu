@@ -4,13 +4,13 @@
 // for the next pass, so the reference's MPI slab transposes (x2z_decomp.f,
 // z2x_decomp.f) become the store patterns of these kernels.
 //
-//   z_inv  : z_trans_b.f:224-250     wave (kx,ky,kz)  -> (z, kx, ky)
-//   y_inv  : xy_trans_b.f:74-98      (z, kx, ky)      -> (z, y, kx)
-//   x_pass : xy_trans_b.f:99-120 + rhs.f:26-61 + xy_trans_f.f:26-37
+//   z_inv  : z_trans_b.f:30-52     wave (kx,ky,kz)  -> (z, kx, ky)
+//   y_inv  : xy_trans_b.f:14-38      (z, kx, ky)      -> (z, y, kx)
+//   x_pass : xy_trans_b.f:39-60 + rhs.f:26-61 + xy_trans_f.f:26-37
 //            (z, y, kx) -> physical line -> vel_max partials, products ->
 //            (m, z, kx, y)
 //   y_fwd  : xy_trans_f.f:39-54      (m, z, kx, y)    -> (m, kx, ky, z)
-//   z_fwd  : z_trans_f.f:144-157 + rhs.f:108-142 + sam.f:210-221,293-314
+//   z_fwd  : z_trans_f.f:21-31 + rhs.f:108-142 + sam.f:210-221,293-314
 //            (m, kx, ky, z) -> projected rhs, RK3 update of u
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
             for (int u = 0; u < kBatch; ++u) {
               const int L = L0 + u * lanes;
               if (L < nl) {
-                if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
+                if (kx == 0) {  // xy_trans_b.f:28-31 keeps only the real part of kx = 0
                   X[u].y = (T)0;
                   Yv[u].y = (T)0;
                 }
@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
           [&](int e, Pair q) {
             const int L = (int)fdiv(e, a.fd_mx), kx = e - L * mx;
             C X = q.x, Yv = q.y;
-            if (kx == 0) {  // xy_trans_b.f:88-91 keeps only the real part of kx = 0
+            if (kx == 0) {  // xy_trans_b.f:28-31 keeps only the real part of kx = 0
               X.y = (T)0;
               Yv.y = (T)0;
             }
@@ -553,7 +553,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
   }
   __syncthreads();
 
-  // ---- vel_max partial sums (vel_max.f:158-168), FP64-accurate,
+  // ---- vel_max partial sums (vel_max.f:11-21), FP64-accurate,
   // deterministic order (FP64 arithmetic in the FP64 form; error-free FP32
   // pairs in the FP32 form, turned into FP64 per warp)
   if (a.partials && a.max_only) {
@@ -754,7 +754,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
   // ---- outputs
   if (a.out_mode == 3) return;  // statistics only (vel_max.f)
   if (a.out_mode == 0) {
-    // physical rows (xy_trans_b.f:117-119)
+    // physical rows (xy_trans_b.f:57-59)
     for (int e = threadIdx.x; e < nin * Y * nx; e += blockDim.x) {
       const int r = (int)fdiv(e, a.fd_nx), x = e - r * nx;
       const int f = (int)fdiv(r, a.fd_y), yy = r - f * Y;
@@ -1001,7 +1001,7 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
 
 // --------------------------------------------------------------- z forward
 // Tile: kx column i, ky rows j0 .. j0+TY-1, all nf fields.  Forward z
-// transform, truncation to Nz_min and 1/Nz (z_trans_f.f:150-156), then one of
+// transform, truncation to Nz_min and 1/Nz (z_trans_f.f:25-30), then one of
 //   mode 0: write the truncated modes back in place (z_trans_f),
 //   mode 1: rhs epilogue (rhs.f:108-142) into r with u_sav from memory,
 //   mode 2: full stage epilogue: rhs, then sam.f:210-221 and 293-314.
@@ -1083,7 +1083,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
 }
 
 // ----------------------------------------------------- vel_max completion
-// vel_max.f:170-196 on the per-CTA partials written by k_x_pass.
+// vel_max.f:28-49 on the per-CTA partials written by k_x_pass.
 // Parseval sums of vel_max (see launch_parseval): sums of the stored modes'
 // squares, FP64-accurate, per-thread strided order, block tree, fixed launch
 // shape.  The FP32 form (the only user) accumulates the exact squares of its
@@ -1377,7 +1377,7 @@ void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevS
 void launch_x2z(const double2* in, double2* out, const Grid& g, int nvar, int nx2, cudaStream_t s) {
   long long total = (long long)g.ny * g.mx * g.nz * nvar;
   int grid = (int)((total + kThreads - 1) / kThreads);
-  if (grid > 152 * 16) grid = 152 * 16;
+  if (grid > sm_count() * 16) grid = sm_count() * 16;
   if (grid < 1) grid = 1;
   k_x2z<<<grid, kThreads, 0, s>>>(in, out, g, nvar, nx2);
 }

@@ -6,7 +6,7 @@ namespace samgpu {
 
 static int blocks_for(long long n) {
   long long b = (n + kThreads - 1) / kThreads;
-  if (b > 152 * 32) b = 152 * 32;
+  if (b > sm_count() * 32) b = sm_count() * 32;
   return (int)(b < 1 ? 1 : b);
 }
 

@@ -1509,19 +1509,27 @@ int sam_gpu_measure_fp64_peak(double* tflops) {
 
 // Tile and FFT-schedule autotuner: each pass is timed (CUDA events, best of
 // `reps`) with each candidate on the resident state and the fastest is kept.
-// The z forward pass updates u and r, so both are saved first and restored
-// after; stages 1 and 2 recompute dt and the statistics from that state and
-// leave the time alone.
+// The z forward pass updates u and r, and stage 1 recomputes dt, the
+// statistics and (dynamic closure) the model coefficient from the state it
+// sees, so u, r, p, the scalar state and the coefficient are saved first and
+// restored after: the state after the call is the state before it.
 int sam_gpu_autotune(int reps) {
   NEED_CTX();
   if (reps < 1) reps = 1;
   const size_t nm = (size_t)c.g.mx * c.g.my * c.g.mz * c.g.lu;
   const size_t bytes = nm * csize(c);
-  void *su = nullptr, *sr = nullptr;
+  const size_t pbytes = (size_t)c.g.mx * c.g.my * c.g.mz * csize(c);
+  void *su = nullptr, *sr = nullptr, *sp = nullptr, *ss = nullptr;
   CK(cudaMalloc(&su, bytes));
   CK(cudaMalloc(&sr, bytes));
+  CK(cudaMalloc(&sp, pbytes));
+  CK(cudaMalloc(&ss, sizeof(DevState) + sizeof(double)));
+  double* scds = reinterpret_cast<double*>(static_cast<char*>(ss) + sizeof(DevState));
   CK(cudaMemcpyAsync(su, c.U, bytes, cudaMemcpyDeviceToDevice, c.stream));
   CK(cudaMemcpyAsync(sr, c.R, bytes, cudaMemcpyDeviceToDevice, c.stream));
+  CK(cudaMemcpyAsync(sp, c.P, pbytes, cudaMemcpyDeviceToDevice, c.stream));
+  CK(cudaMemcpyAsync(ss, c.state, sizeof(DevState), cudaMemcpyDeviceToDevice, c.stream));
+  if (c.les_cds) CK(cudaMemcpyAsync(scds, c.les_cds, sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
@@ -1571,9 +1579,14 @@ int sam_gpu_autotune(int reps) {
   cudaEventDestroy(e1);
   CK(cudaMemcpyAsync(c.U, su, bytes, cudaMemcpyDeviceToDevice, c.stream));
   CK(cudaMemcpyAsync(c.R, sr, bytes, cudaMemcpyDeviceToDevice, c.stream));
+  CK(cudaMemcpyAsync(c.P, sp, pbytes, cudaMemcpyDeviceToDevice, c.stream));
+  CK(cudaMemcpyAsync(c.state, ss, sizeof(DevState), cudaMemcpyDeviceToDevice, c.stream));
+  if (c.les_cds) CK(cudaMemcpyAsync(c.les_cds, scds, sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
   CK(cudaStreamSynchronize(c.stream));
   cudaFree(su);
   cudaFree(sr);
+  cudaFree(sp);
+  cudaFree(ss);
   if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
   c.graph_stale = 1;  // recapture with the new tiles
   return check_launch();
@@ -1769,7 +1782,7 @@ int sam_gpu_read_field(const char* fname) {
   fseek(f, 0, SEEK_END);
   const long found = ftell(f);
   fseek(f, 0, SEEK_SET);
-  if (found < 0 || (size_t)found != expect) {  // read_field.f:74-80
+  if (found < 0 || (size_t)found != expect) {  // read_field.f:26-32
     fclose(f);
     return fail(SAM_GPU_EINVAL, "read_field: vel file is not of correct size (expect %zu, found %ld)", expect, found);
   }

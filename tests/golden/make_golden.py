@@ -1,7 +1,7 @@
 """Generate tests/golden/kats.json from the reference's own known-answer tests.
 
-Run in a checkout where the reference tree is available:
-    python tests/golden/make_golden.py /root/reference
+Run where the reference tree is available, naming its root directory:
+    python tests/golden/make_golden.py <reference-root>
 
 The reference ships no data files beyond input.dat, so the fixtures are:
   * tfftpk: FFTPACK's self test (fft.f:2838-3011): rfftf of N=36 ones is
@@ -73,4 +73,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <reference-root>")
+    main(sys.argv[1])

@@ -62,7 +62,7 @@ def test_restart_failure_paths(gpu_lib, tmp_path):
     g.init_taylor_green()
     f = str(tmp_path / "vel.000000")
     g.write_field(f)
-    # truncated file: read_field.f:74-80 rejects the size
+    # truncated file: read_field.f:26-32 rejects the size
     with open(f, "r+b") as fh:
         fh.truncate(os.path.getsize(f) - 16)
     with pytest.raises(SamGpuError, match="not of correct size"):

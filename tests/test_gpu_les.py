@@ -10,7 +10,7 @@ pytestmark = pytest.mark.gpu
 
 
 def periodic_fill(a):
-    """periodicity.f:215-239: halo planes 0 and n+1 from the periodic images,
+    """periodicity.f:7-32: halo planes 0 and n+1 from the periodic images,
     x first, then y, then z."""
     a[0], a[-1] = a[-2], a[1]
     a[:, 0], a[:, -1] = a[:, -2], a[:, 1]

@@ -361,3 +361,24 @@ def test_unsupported_lengths_are_rejected(gpu_lib):
     for nx, ny, nz in ((14, 16, 16), (16, 22, 16), (16, 16, 2048)):
         with pytest.raises(SamGpuError, match="EINVAL"):
             SamGpu(nx=nx, ny=ny, nz=nz)
+
+
+@pytest.mark.parametrize("prec", [64, 32])
+def test_autotune_leaves_the_state(gpu_lib, prec):
+    """The autotuner times the passes on the resident state and puts u, r, p,
+    the scalar state (time, dt, statistics) back as they were."""
+    cfg = dict(nx=32, ny=32, nz=32, i_strat=1, i_cfl=1, cfl0=0.5, vis=1e-3, buoy_fac_z=1.0, lapse=1.0,
+               precision=prec)
+    g = SamGpu(**cfg)
+    g.init_random(3, 6, 1.0, 6, 0.1)
+    g.step(2)
+    u0, r0 = g.download(with_r=True)
+    s0 = g.stats()
+    g.autotune(1)
+    u1, r1 = g.download(with_r=True)
+    s1 = g.stats()
+    assert np.array_equal(u0, u1)
+    assert np.array_equal(r0, r1)
+    for key, v in s0.items():
+        assert np.array_equal(np.asarray(v), np.asarray(s1[key])), key
+    g.close()

@@ -56,7 +56,7 @@ def test_fft_conventions_against_numpy(n):
 
 @pytest.mark.parametrize("dims,strat", [((16, 16, 16), 0), ((12, 8, 24), 1), ((72, 1, 24), 1), ((32, 48, 20), 1)])
 def test_tst_transpose_round_trip(dims, strat):
-    """tst_transpose.f:294-332: z_trans_b -> x2z -> xy_trans_b -> xy_trans_f ->
+    """tst_transpose.f:98-146: z_trans_b -> x2z -> xy_trans_b -> xy_trans_f ->
     z2x -> z_trans_f reproduces every mode to 1e-15."""
     nx, ny, nz = dims
     o = O.Oracle(nx=nx, ny=ny, nz=nz, i_strat=strat)

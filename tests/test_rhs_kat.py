@@ -1,0 +1,249 @@
+"""Known-answer tests of the nonlinear term, the buoyancy terms and the
+pressure projection of rhs.f:74-142, from closed-form Boussinesq solutions.
+
+The right-hand side of the stratified equations in divergence form is
+    R_i = -d_j(u_i u_j) + (b_x, 0, b_z)_i theta - d_i p,   d_i R_i = 0
+    R_theta = -d_j(u_j theta) - lapse * w'
+with w' = w, or cos(t) w - sin(t) u in the tilted box (sam.f:175-185), and p
+the pressure that makes R solenoidal (rhs.f:134-139).  For the two velocity
+fields below these are written out by hand (2 pi periodic box):
+
+A. the ABC (Beltrami) flow u = (A sin z + C cos y, B sin x + A cos z,
+   C sin y + B cos x): (u.grad)u = grad(|u|^2/2), so the projected nonlinear
+   term vanishes and p = -(AC sin z cos y + AB sin x cos z + BC sin y cos x);
+B. u = (b cos z, a cos x, d cos y): (u.grad)u = -(bd cos y sin z,
+   ab sin x cos z, ad cos x sin y) is already solenoidal, so the nonlinear
+   term passes the projection unchanged (p = 0 from it).
+
+with theta = E cos x: the buoyancy b_z theta is solenoidal, b_x theta is not
+and adds b_x E sin x to p.  Both cases together exercise every product
+pairing, the sign of -i k_j T_ij, the divergence of the buoyancy flux, the
+projection and the pressure.  The expected wave coefficients are taken from
+the closed-form physical fields with numpy's FFT (independent of the
+oracle's and the CUDA transforms).  Bar: 1e-14 of the field scale.
+
+The same closed form checks one full RK3 stage (sam.f:175-195, 210-221,
+293-314): u_new = (u + gamma_1 dt R) exp(-nu k^2 gamma_1 dt), theta with
+nu / Pr, with and without the tilted-box rotation of u_sav.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+TOL = 1e-14
+N = 16
+CONSTS = dict(A=0.7, B=-0.45, C=0.3, a=0.6, b=-0.8, d=0.5, E=0.35)
+PHYS = dict(buoy_fac_x=0.3, buoy_fac_z=1.7, lapse=0.9, vis=0.02, pr=0.7, dt0=0.01)
+
+
+def grid(n=N):
+    x = 2 * np.pi * np.arange(n) / n
+    return np.meshgrid(x, x, x, indexing="ij")
+
+
+def closed_form(case, bx, bz, lapse, cth=1.0, sth=0.0, n=N):
+    """Physical u, v, w, theta and the expected R_1..R_3, R_theta, p."""
+    X, Y, Z = grid(n)
+    k = CONSTS
+    th = k["E"] * np.cos(X)
+    if case == "A":
+        u = k["A"] * np.sin(Z) + k["C"] * np.cos(Y)
+        v = k["B"] * np.sin(X) + k["A"] * np.cos(Z)
+        w = k["C"] * np.sin(Y) + k["B"] * np.cos(X)
+        r1 = np.zeros_like(X)
+        r2 = np.zeros_like(X)
+        r3 = bz * th
+        p = -(k["A"] * k["C"] * np.sin(Z) * np.cos(Y) + k["A"] * k["B"] * np.sin(X) * np.cos(Z)
+              + k["B"] * k["C"] * np.sin(Y) * np.cos(X)) + bx * k["E"] * np.sin(X)
+    else:
+        u = k["b"] * np.cos(Z)
+        v = k["a"] * np.cos(X)
+        w = k["d"] * np.cos(Y)
+        r1 = k["b"] * k["d"] * np.cos(Y) * np.sin(Z)
+        r2 = k["a"] * k["b"] * np.sin(X) * np.cos(Z)
+        r3 = k["a"] * k["d"] * np.cos(X) * np.sin(Y) + bz * th
+        p = bx * k["E"] * np.sin(X)
+    # -u.grad(theta) with grad(theta) = (-E sin x, 0, 0)
+    rth = u * k["E"] * np.sin(X) - lapse * (cth * w - sth * u)
+    return [u, v, w, th], [r1, r2, r3, rth], p
+
+
+def to_wave(f, d):
+    """Wave coefficients of a real physical field in the reference layout
+    (Nze, Ny_min, Nx_min): forward transform scaled by 1/(Nx Ny Nz)."""
+    F = np.fft.fftn(f) / f.size
+    K = d.kx_max
+    out = np.zeros((d.nze, d.ny_min, d.nx_min), dtype=np.complex128, order="F")
+    ky = [j if j <= d.ky_max else j - d.ny_min for j in range(d.ny_min)]
+    kz = [q if q <= d.kz_max else q - d.nz_min for q in range(d.nz_min)]
+    for i in range(K + 1):
+        for jj, kyv in enumerate(ky):
+            for qq, kzv in enumerate(kz):
+                out[qq, jj, i] = F[i, kyv % d.ny, kzv % d.nz]
+    return out
+
+
+def wave_fields(fields, d):
+    w = np.zeros((d.nze, d.ny_min, d.nx_min, len(fields)), dtype=np.complex128, order="F")
+    for n, f in enumerate(fields):
+        w[..., n] = to_wave(f, d)
+    return w
+
+
+def k_squared(d):
+    ky = np.array([j if j <= d.ky_max else j - d.ny_min for j in range(d.ny_min)], dtype=float)
+    kz = np.array([q if q <= d.kz_max else q - d.nz_min for q in range(d.nz_min)], dtype=float)
+    kx = np.arange(d.nx_min, dtype=float)
+    KZ, KY, KX = np.meshgrid(kz, ky, kx, indexing="ij")
+    return KX ** 2 + KY ** 2 + KZ ** 2
+
+
+def cfg_for(rot=False):
+    c = dict(nx=N, ny=N, nz=N, i_strat=1, **PHYS)
+    if rot:
+        t = 0.4
+        c.update(rot_sav=1, cos_theta=np.cos(t), sin_theta=np.sin(t))
+    return c
+
+
+def expected_rhs(case, d, rot=False):
+    c = cfg_for(rot)
+    cth, sth = c.get("cos_theta", 1.0), c.get("sin_theta", 0.0)
+    phys, rr, p = closed_form(case, c["buoy_fac_x"], c["buoy_fac_z"], c["lapse"], cth, sth)
+    return phys, wave_fields(rr, d), to_wave(p, d)
+
+
+def rhs_inputs(o, phys):
+    d = o.d
+    uu = o.phys(d.lr)
+    for n in range(d.lu):
+        uu[..., n] = phys[n]
+    u_wave = wave_fields(phys, d)
+    usav = np.asfortranarray(u_wave[: d.nz_min, :, :, 2:4])
+    return uu, usav, u_wave
+
+
+def check(got, want, scale, what):
+    err = np.abs(got - want).max() / scale
+    assert err < TOL, (what, err)
+
+
+@pytest.mark.parametrize("case", ["A", "B"])
+def test_closed_form_fields_are_consistent(case):
+    """The hand-derived R is solenoidal and p is the potential that was
+    removed: div R = 0 and R = P[R_raw] for the spectral R_raw built here from
+    products of the physical fields (a check of the derivation itself)."""
+    cfg = cfg_for()
+    phys, rr, p = closed_form(case, cfg["buoy_fac_x"], cfg["buoy_fac_z"], cfg["lapse"])
+    kk = np.fft.fftfreq(N, 1.0 / N)
+    KX, KY, KZ = np.meshgrid(kk, kk, kk, indexing="ij")
+    kv = [KX, KY, KZ]
+    F = [np.fft.fftn(f) for f in rr[:3]]
+    div = sum(1j * kv[i] * F[i] for i in range(3))
+    assert np.abs(div).max() / N ** 3 < 1e-14
+    # raw divergence-form term from the products, plus buoyancy
+    u = phys
+    raw = []
+    for i in range(3):
+        s = 0
+        for j in range(3):
+            s = s - 1j * kv[j] * np.fft.fftn(u[i] * u[j])
+        raw.append(s)
+    raw[0] = raw[0] + cfg["buoy_fac_x"] * np.fft.fftn(u[3])
+    raw[2] = raw[2] + cfg["buoy_fac_z"] * np.fft.fftn(u[3])
+    ksq = np.maximum(KX ** 2 + KY ** 2 + KZ ** 2, 1e-10)
+    pw = -1j * (KX * raw[0] + KY * raw[1] + KZ * raw[2]) / ksq
+    for i in range(3):
+        assert np.abs(raw[i] - 1j * kv[i] * pw - F[i]).max() / N ** 3 < 1e-14
+    assert np.abs(pw - np.fft.fftn(p)).max() / N ** 3 < 1e-14
+
+
+@pytest.mark.parametrize("case", ["A", "B"])
+def test_oracle_rhs_matches_closed_form(case):
+    o = O.Oracle(**cfg_for())
+    d = o.d
+    phys, r_exp, p_exp = expected_rhs(case, d)
+    uu, usav, _ = rhs_inputs(o, phys)
+    o.set_time(0.0, 0.01)
+    r = o.rhs(uu, usav, 2)
+    scale = max(np.abs(r_exp).max(), np.abs(p_exp).max())
+    for n in range(d.lu):
+        check(r[: d.nz_min, ..., n], r_exp[: d.nz_min, ..., n], scale, ("R", case, n))
+    check(r[: d.nz_min, ..., d.lu], p_exp[: d.nz_min], scale, ("p", case))
+    o.close()
+
+
+def expected_stage(case, d, rot):
+    c = cfg_for(rot)
+    phys, r_exp, p_exp = expected_rhs(case, d, rot)
+    u0 = wave_fields(phys, d)
+    g1 = 8.0 / 15.0
+    dt = c["dt0"]
+    ksq = k_squared(d)
+    u1 = np.zeros_like(u0)
+    for n in range(d.lu):
+        vf = c["vis"] * g1 * dt * (1.0 / c["pr"] if n == 3 else 1.0)
+        u1[: d.nz_min, ..., n] = (u0[: d.nz_min, ..., n] + g1 * dt * r_exp[: d.nz_min, ..., n]) * np.exp(-vf * ksq)
+    return u0, u1, r_exp, p_exp
+
+
+@pytest.mark.parametrize("case", ["A", "B"])
+@pytest.mark.parametrize("rot", [False, True])
+def test_oracle_stage_matches_closed_form(case, rot):
+    o = O.Oracle(**cfg_for(rot))
+    d = o.d
+    u0, u1, r_exp, p_exp = expected_stage(case, d, rot)
+    u = u0.copy(order="F")
+    r = o.wave(d.lr)
+    o.stage(u, r, 1)
+    scale = max(np.abs(u1).max(), np.abs(r_exp).max())
+    for n in range(d.lu):
+        check(u[: d.nz_min, ..., n], u1[: d.nz_min, ..., n], scale, ("u", case, rot, n))
+        check(r[: d.nz_min, ..., n], r_exp[: d.nz_min, ..., n], scale, ("R", case, rot, n))
+    check(r[: d.nz_min, ..., d.lu], p_exp[: d.nz_min], scale, ("p", case, rot))
+    o.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["A", "B"])
+def test_gpu_rhs_matches_closed_form(gpu_lib, case):
+    from sam_gb300 import SamGpu
+    cfg = cfg_for()
+    o = O.Oracle(**cfg)
+    d = o.d
+    phys, r_exp, p_exp = expected_rhs(case, d)
+    uu, usav, _ = rhs_inputs(o, phys)
+    g = SamGpu(**cfg)
+    g.set_tstep(2, 0.01, 0.0)
+    r = g.rhs(uu, usav)
+    scale = max(np.abs(r_exp).max(), np.abs(p_exp).max())
+    for n in range(d.lu):
+        check(r[: d.nz_min, ..., n], r_exp[: d.nz_min, ..., n], scale, ("R", case, n))
+    check(r[: d.nz_min, ..., d.lu], p_exp[: d.nz_min], scale, ("p", case))
+    g.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["A", "B"])
+@pytest.mark.parametrize("rot", [False, True])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_gpu_stage_matches_closed_form(gpu_lib, case, rot, precision):
+    """The resident stage (z_inv ... z_fwd with the update epilogue) against
+    the closed form; the FP32 bulk form to its own rounding (2e-6)."""
+    from sam_gb300 import SamGpu
+    cfg = cfg_for(rot)
+    o = O.Oracle(**cfg)
+    d = o.d
+    u0, u1, r_exp, p_exp = expected_stage(case, d, rot)
+    g = SamGpu(precision=precision, **cfg)
+    g.upload(u0)
+    g.stage(1)
+    ug, rg = g.download(with_r=True)
+    scale = max(np.abs(u1).max(), np.abs(r_exp).max())
+    tol = TOL if precision == 64 else 2e-6
+    for n in range(d.lu):
+        assert np.abs(ug[: d.nz_min, ..., n] - u1[: d.nz_min, ..., n]).max() / scale < tol, ("u", n)
+        assert np.abs(rg[: d.nz_min, ..., n] - r_exp[: d.nz_min, ..., n]).max() / scale < tol, ("R", n)
+    assert np.abs(rg[: d.nz_min, ..., d.lu] - p_exp[: d.nz_min]).max() / scale < tol
+    g.close()
