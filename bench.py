@@ -224,7 +224,7 @@ def parity_vs_oracle(u_start, u_oracle, st_oracle, nz_min, steps, stream):
     from sam_gb300 import SamGpu
     out = {"steps": steps, "bar_fp64": 1e-12,
            "measure": "max |u_gpu - u_oracle| / max |u_oracle| per field (Nz_min rows)"}
-    for name, prec in (("fp64", 64), ("fp32_bulk", 32)):
+    for name, prec in (("fp64", 64), ("double_float", 48), ("fp32_bulk", 32)):
         g = SamGpu(**workload_cfg(precision=prec))
         g.set_stream(stream.cuda_stream)
         g.upload(u_start)
@@ -237,6 +237,7 @@ def parity_vs_oracle(u_start, u_oracle, st_oracle, nz_min, steps, stream):
                      "div_max": g.div_check()["div_max"]}
         g.close()
     out["fp64_within_bar"] = max(out["fp64"]["max_rel_err_per_field"]) <= 1e-12
+    out["double_float_within_bar"] = max(out["double_float"]["max_rel_err_per_field"]) <= 1e-12
     return out
 
 
@@ -433,8 +434,9 @@ def run_probe(args):
 
 
 def run_parity_curve(args):
-    """Error of the GPU forms against the oracle versus step count on the
-    128^3 stratified decaying-turbulence configuration (N = 1, Pr = 1,
+    """Error of the GPU forms (FP64, double-float, FP32 bulk) against the
+    oracle versus step count on the 128^3 stratified decaying-turbulence
+    configuration (N = 1, Pr = 1,
     nu = 1/800, k^4 exp(-2 (k/4)^2) start at rms 1 with theta at 0.1, CFL
     0.5), seeds 0, 1, 2: max over fields of max |u_gpu - u_oracle| / max
     |u_oracle| every `every` steps up to args.parity_curve steps; one JSON
@@ -451,29 +453,31 @@ def run_parity_curve(args):
     out = {"parity_curve": "128^3 stratified decaying turbulence, config of the 500-step run", "every": every,
            "measure": "max over fields of max|u_gpu - u_oracle| / max|u_oracle| (Nz_min rows)", "seeds": {}}
     for seed in (0, 1, 2):
+        # the oracle's states every `every` steps, then each GPU form in turn
+        # from the same start (one library context at a time)
         o = O.Oracle(**cfg)
         u = o.init_random(seed, 6, 1.0, 6, 0.1)
+        u0 = u.copy(order="F")
         r = o.wave(o.d.lr)
-        gs = {}
-        for prec in (64, 32):
-            g = SamGpu(precision=prec, **cfg)
-            g.upload(u)
-            gs[prec] = g
-        rows = []
+        snaps, times = [], []
         done = 0
         while done < args.parity_curve:
             o.steps(u, r, every)
             done += every
-            row = {"step": done, "time": o.stats()["time"]}
-            for prec, g in gs.items():
+            snaps.append(u.copy(order="F"))
+            times.append(o.stats()["time"])
+        nz_min, lu = o.d.nz_min, o.d.lu
+        o.close()
+        rows = [{"step": every * (i + 1), "time": times[i]} for i in range(len(snaps))]
+        for prec in (64, 48, 32):
+            g = SamGpu(precision=prec, **cfg)
+            g.upload(u0)
+            for i, ref in enumerate(snaps):
                 g.step(every)
                 ug = g.download()
-                row[f"fp{prec}"] = max(float(np.abs(ug[:o.d.nz_min, ..., n] - u[:o.d.nz_min, ..., n]).max()
-                                             / np.abs(u[:o.d.nz_min, ..., n]).max()) for n in range(o.d.lu))
-            rows.append(row)
-        for g in gs.values():
+                rows[i][f"prec{prec}"] = max(float(np.abs(ug[:nz_min, ..., n] - ref[:nz_min, ..., n]).max()
+                                                  / np.abs(ref[:nz_min, ..., n]).max()) for n in range(lu))
             g.close()
-        o.close()
         out["seeds"][str(seed)] = rows
     print(json.dumps(out), flush=True)
     return 0
@@ -507,10 +511,11 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32", action="store_true")
+    ap.add_argument("--no-dd", action="store_true", help="skip the double-float form")
     ap.add_argument("--no-les", action="store_true")
     ap.add_argument("--no-ensemble", action="store_true")
     ap.add_argument("--grid", type=int, default=256, help="N of the N^3 box (profiling of smaller cases)")
-    ap.add_argument("--precision", type=int, default=64, choices=[64, 32],
+    ap.add_argument("--precision", type=int, default=64, choices=[64, 48, 32],
                     help="precision of the timed run (32 for profiling the FP32 bulk form)")
     ap.add_argument("--probe", action="store_true",
                     help="profiling case: the workload's start state and 3 steps only (no timing, autotune or "
@@ -636,6 +641,36 @@ def main():
                 # stages 2 and 3: the x pass alone (vel_max's kernels run at stage 1)
                 "_x_ms": (prof32[1]["x_pass"] + prof32[2]["x_pass"]) / 2}
 
+    # ---- the double-float form (FP32 pairs on the FP32 pipe, FP64-accurate)
+    # on the same workload and start state
+    ddf = None
+    if not args.no_dd:
+        gd = SamGpu(**workload_cfg(precision=48))
+        gd.set_stream(stream.cuda_stream)
+        gd.upload(u_init)
+        tilesd = gd.autotune(3)
+        gd.step(W)
+        torch.cuda.synchronize()
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            gd.step(K)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        msd = e0.elapsed_time(e1)
+        ud = gd.download()
+        profd = [gd.profile_stage(nrk, max(2, K // 4)) for nrk in (1, 2, 3)]
+        passesd = {k: sum(p[k] for p in profd) / 3 for k in profd[0]}
+        errd = [float(np.abs(ud[..., n] - u_fp64[..., n]).max() / np.abs(u_fp64[..., n]).max()) for n in range(4)]
+        gd.close()
+        bd = algorithmic_bytes_per_step(w=8)
+        ddf = {"value": ws * K / (msd / 1e3), "unit": "steps/s", "ms_per_step": msd / K,
+               "speedup_over_fp64": (ws * K / (msd / 1e3)) / value,
+               "rel_err_vs_fp64_per_field": errd, "after_steps": W + K,
+               "hbm_gbs": bd / (msd / K / 1e3) / 1e9, "passes_ms": passesd, "tiles": tilesd,
+               "arithmetic": "FP32 pairs (hi + lo, about 48 significand bits) on the FP32 pipe; vel_max sums, "
+                             "dt and the integrating factor's exponentials in FP64",
+               "_x_ms": (profd[1]["x_pass"] + profd[2]["x_pass"]) / 2}
+
     # ---- the LES forms of the same workload: FP64 drop-in with dm.f's
     # dynamic Smagorinsky coupled in, and FP32 bulk with the learned closure
     les = None
@@ -686,6 +721,14 @@ def main():
                             "traffic": tr32.get("bytes_per_launch") if tr32 else None,
                             "algorithmic_bytes_per_launch": xb32, "ms": x32_ms,
                             "note": "instruction- and latency-bound: counters in profiles/x_pass_256_ncu.md"}
+    if ddf is not None:
+        xd_ms = ddf.pop("_x_ms")
+        ad = x_pass_bytes(w=8) / (xd_ms / 1e3) / 1e9
+        ddf["roofline"] = {"bound": "fp32_issue", "kernel": "k_x_pass<dd> (C2R, 9 products, R2C; stages 2 and 3)",
+                           "achieved_hbm_gbs": ad, "peak_hbm_gbs": hbm_peak, "hbm_frac": ad / hbm_peak,
+                           "algorithmic_bytes_per_launch": x_pass_bytes(w=8), "ms": xd_ms,
+                           "fp64_equivalent_tflops": x_pass_flops() / (xd_ms / 1e3) / 1e12,
+                           "fp64_peak_tflops": fp64_peak}
     ms_step = ms / K
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -698,7 +741,7 @@ def main():
                        "dt_final": st["dt"], "tiles": tiles},
             "roofline": roofline, "cpu_baseline": cpu, "parity_vs_oracle": parity, "e2e": e2e,
             "gpu_launches": launches_per_step * K,
-            "clocks": clk.summary(), "fp32_bulk": fp32, "les": les, "ensemble": ens}
+            "clocks": clk.summary(), "double_float": ddf, "fp32_bulk": fp32, "les": les, "ensemble": ens}
     print(json.dumps(line), flush=True)
     return 0
 

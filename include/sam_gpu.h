@@ -28,6 +28,11 @@ extern "C" {
 #define SAM_GPU_ECUDA -4        /* CUDA runtime failure */
 #define SAM_GPU_ENONFINITE -5   /* vel_max met NaN/Inf in the physical field */
 
+/* sam_gpu_config.precision values */
+#define SAM_GPU_PREC_FP64 64
+#define SAM_GPU_PREC_DD 48
+#define SAM_GPU_PREC_FP32 32
+
 /* The input.dat values the hot path reads (set_labels.f:29-102) and the
  * derived values of init.f / initial_field.f.  Mirrors /static/, /strat/,
  * /gravity_wave/ and the RK choice of /tstep/ (sam.h:14-62). */
@@ -39,7 +44,11 @@ typedef struct sam_gpu_config {
   int nrk_max;        /* 1, 2 or 3 (init.f:117-145) */
   int rot_sav;        /* 1 for the tilted-box wave, i_prob = 4 (sam.f:176-185) */
   int i_les;          /* Chollet-Lesieur spectra (spectra.f:21) */
-  int precision;      /* 64: FP64 drop-in; 32: FP32 bulk with FP64 reductions */
+  int precision;      /* 64: FP64 drop-in; 48 (SAM_GPU_PREC_DD): the resident step
+                         in double-float pairs on the FP32 pipe (about 48
+                         significand bits; plain step only: no LES, forcing,
+                         planes); 32: FP32 bulk with FP64 reductions.  The
+                         per-routine drop-ins always compute in FP64. */
   double xl, yl, zl;  /* box */
   double vis, pr;     /* viscosity, Prandtl number */
   double dt0, cfl0;

@@ -57,32 +57,38 @@ def advance_to(g, t_end, chunk=20):
             raise FloatingPointError("DNS blew up (non-finite velocity)")
 
 
-def dns_snapshots(n=512, f=4, n_snap=10, t_spinup=1.0, t_every=0.1, seed=0, vis=1e-3, precision=32,
-                  forcing=(2.5, 0.5, 0.5), t_eval=0.2, log=print):
-    """Filtered snapshots (X, Y, Z, Lu+Lr) of a forced stratified DNS, and an
-    evaluation pair: after the training snapshots the forcing stops, one
-    more snapshot is taken and another t_eval later (decaying, so a coarse
-    LES can follow it without the DNS's random forcing)."""
+def dns_snapshots(n=512, filters=(4,), n_snap=10, t_spinup=1.0, t_every=0.1, seed=0, vis=1e-3, precision=32,
+                  forcing=(2.5, 0.5, 0.5), t_eval=0.2, n_eval=1, log=print):
+    """Filtered snapshots (X, Y, Z, Lu+Lr) of a forced stratified DNS for
+    every filter ratio f in `filters` ({f: [snapshots]}), and an evaluation
+    sequence: after the training snapshots the forcing stops and the
+    filtered field is taken at t0 and at n_eval later times spaced
+    t_eval / n_eval apart (decaying, so a coarse LES can follow it without
+    the DNS's random forcing): {f: [fields]} and the times after t0."""
     g = SamGpu(**dns_config(n, precision, vis))
     try:
         g.init_random(seed, 6, 1.0, 6, 0.1)
         if forcing:
             g.set_forcing(seed + 1, *forcing)
         advance_to(g, t_spinup)
-        snaps = []
+        snaps = {f: [] for f in filters}
         for s in range(n_snap):
-            snaps.append(g.box_filter(f))
+            for f in filters:
+                snaps[f].append(g.box_filter(f))
             st = g.stats()
             log(f"snapshot {s}: t = {st['time']:.3f}, energy {st['energy']:.4f}, u_max {st['u_max'][:3]}")
             advance_to(g, st["time"] + t_every)
         g.set_forcing(0, 0.0)
-        ev0 = g.box_filter(f)
+        ev = {f: [g.box_filter(f)] for f in filters}
         t0 = g.stats()["time"]
-        advance_to(g, t0 + t_eval, chunk=1)
-        t1 = g.stats()["time"]
-        ev1 = g.box_filter(f)
-        log(f"evaluation pair: t = {t0:.3f} .. {t1:.3f}")
-        return snaps, (ev0, ev1, t1 - t0)
+        times = []
+        for e in range(n_eval):
+            advance_to(g, t0 + t_eval * (e + 1) / n_eval, chunk=1)
+            times.append(g.stats()["time"] - t0)
+            for f in filters:
+                ev[f].append(g.box_filter(f))
+        log(f"evaluation sequence: t = {t0:.3f} + {times}")
+        return snaps, (ev, times)
     finally:
         g.close()
 
@@ -243,74 +249,102 @@ def shell_spectrum(g):
     return g.spectra()["ek"]
 
 
-def evaluate_a_posteriori(params, filt0, filt1, t_span, n_coarse, vis=1e-3, kmax_frac=0.5):
-    """Coarse LES from the filtered snapshot filt0 over t_span with no model,
-    dm.f's dynamic closure and the learned closure; the relative spectrum
-    error against the filtered DNS snapshot filt1 (taken t_span later) over
-    shells k <= kmax_frac * k_max."""
+def evaluate_a_posteriori(params, fields, times, n_coarse, vis=1e-3, kmax_frac=0.5):
+    """Coarse LES from the filtered snapshot fields[0] with no model, dm.f's
+    dynamic closure and the learned closure, compared with the filtered DNS
+    fields[1:] at the elapsed times `times`: per closure the relative
+    spectrum error over shells k <= kmax_frac * k_max (the largest over the
+    shells, averaged over the comparison times), the same over all shells
+    k <= k_max, and the spectra at the last time."""
     g = SamGpu(**coarse_config(n_coarse, vis))
     try:
-        ref = None
-        g.upload(to_wave(g, filt1[..., :g.lu]))
-        ref = shell_spectrum(g)
-        u0 = to_wave(g, filt0[..., :g.lu])
+        refs = []
+        for fld in fields[1:]:
+            g.upload(to_wave(g, fld[..., :g.lu]))
+            refs.append(shell_spectrum(g))
+        u0 = to_wave(g, fields[0][..., :g.lu])
         kmax = int((n_coarse - 0.1) / 3)
         ks = np.arange(1, int(kmax_frac * kmax) + 1)
-        out = {}
+        ka = np.arange(1, kmax + 1)
+        out = {"times": list(times)}
         for name, model in (("none", 0), ("dm", 2), ("net", 3)):
             g.upload(u0)
             g.set_tstep(1, 1e-3, 0.0)
             if model == 3:
                 g.mlp_set(params)
             g.set_les(model)
-            advance_to(g, t_span, chunk=5)
-            ek = shell_spectrum(g)
+            e_half, e_all = [], []
+            for t, ref in zip(times, refs):
+                advance_to(g, t, chunk=5)
+                ek = shell_spectrum(g)
+                e_half.append(float(np.abs(ek[ks] / ref[ks] - 1).max()))
+                e_all.append(float(np.abs(ek[ka] / ref[ka] - 1).max()))
             g.set_les(0)
-            out[name] = float(np.abs(ek[ks] / ref[ks] - 1).max())
+            out[name] = float(np.mean(e_half))
+            out[f"{name}_all_shells"] = float(np.mean(e_all))
             out[f"spectrum_{name}"] = ek[: kmax + 1].tolist()
-        out["spectrum_dns"] = ref[: kmax + 1].tolist()
+        out["spectrum_dns"] = refs[-1][: kmax + 1].tolist()
         return out
     finally:
         g.close()
 
 
-def run(n=512, f=4, n_snap=10, steps=None, batch=8192, lr=1e-3, vis=1e-3, t_spinup=1.0, t_every=0.1, t_eval=0.2,
-        seed=0, out=WEIGHTS, log=print, forcing=(2.5, 0.5, 0.5)):
-    """The whole pipeline: DNS snapshots, samples, training on all but the
-    last training snapshot, a priori evaluation on that one, a posteriori
-    evaluation on the decaying pair; saves the parameters and the report."""
+def run(n=512, filters=(4,), n_snap=10, steps=None, batch=8192, lr=1e-3, vis=1e-3, t_spinup=1.0, t_every=0.1,
+        t_eval=0.2, n_eval=1, seed=0, out=WEIGHTS, log=print, forcing=(2.5, 0.5, 0.5)):
+    """The whole pipeline: DNS snapshots filtered at every ratio in
+    `filters`, samples, one network trained on all of them but the last
+    snapshot, a priori evaluation on that one and a posteriori evaluation on
+    the decaying sequence, per filter ratio; saves the parameters and the
+    report."""
     import json
     import time
 
     t0 = time.time()
-    snaps, (ev0, ev1, t_span) = dns_snapshots(n, f, n_snap, t_spinup, t_every, seed, vis, forcing=forcing,
-                                              t_eval=t_eval, log=log)
-    nc = n // f
+    snaps, (ev, times) = dns_snapshots(n, filters, n_snap, t_spinup, t_every, seed, vis, forcing=forcing,
+                                       t_eval=t_eval, n_eval=n_eval, log=log)
     t1 = time.time()
-    feat, y, raw, smag, dsq = coarse_samples(snaps, nc, vis)
-    npt = nc ** 3
-    tr = slice(0, npt * (n_snap - 1))
-    te = slice(npt * (n_snap - 1), npt * n_snap)
+    data = {}
+    for f in filters:
+        nc = n // f
+        feat, y, raw, smag, dsq = coarse_samples(snaps[f], nc, vis)
+        npt = nc ** 3
+        data[f] = dict(nc=nc, feat=feat, y=y, raw=raw, smag=smag, dsq=dsq, tr=slice(0, npt * (n_snap - 1)),
+                       te=slice(npt * (n_snap - 1), npt * n_snap))
+    x_tr = np.concatenate([d["feat"][d["tr"]] for d in data.values()])
+    y_tr = np.concatenate([d["y"][d["tr"]] for d in data.values()])
     t2 = time.time()
-    params, hist = train(feat[tr], y[tr], steps, batch, lr, seed)
+    params, hist = train(x_tr, y_tr, steps, batch, lr, seed)
     t3 = time.time()
-    c_dm = dm_coefficient(snaps[-1], nc, vis)
-    prior = evaluate_a_priori(params, feat[te], raw[te], smag[te], dsq, c_dm)
-    c_test = predict(params, feat[te])
-    prior["mse_net"] = float(((c_test - y[te]) ** 2).mean())
-    prior["mse_mean"] = float(((y[tr].mean(0) - y[te]) ** 2).mean())
-    post = evaluate_a_posteriori(params, ev0, ev1, t_span, nc, vis)
-    report = {"dns": n, "filter": f, "coarse": nc, "snapshots": n_snap, "samples_train": int(tr.stop),
-              "forcing": list(forcing), "vis": vis,
-              "steps": int(len(hist)), "batch": batch, "lr": lr, "loss_first": float(hist[:10].mean()),
-              "loss_last": float(hist[-10:].mean()), "a_priori": prior,
-              "a_posteriori_max_rel_err_k_le_kmax_half": {k: post[k] for k in ("none", "dm", "net")},
+    per_filter = {}
+    for f, d in data.items():
+        te, tr = d["te"], d["tr"]
+        c_dm = dm_coefficient(snaps[f][-1], d["nc"], vis)
+        prior = evaluate_a_priori(params, d["feat"][te], d["raw"][te], d["smag"][te], d["dsq"], c_dm)
+        c_test = predict(params, d["feat"][te])
+        prior["mse_net"] = float(((c_test - d["y"][te]) ** 2).mean())
+        prior["mse_mean"] = float(((d["y"][tr].mean(0) - d["y"][te]) ** 2).mean())
+        post = evaluate_a_posteriori(params, ev[f], times, d["nc"], vis)
+        per_filter[str(f)] = {
+            "coarse": d["nc"], "a_priori": prior,
+            "a_posteriori_max_rel_err_k_le_kmax_half": {k: post[k] for k in ("none", "dm", "net")},
+            "a_posteriori_max_rel_err_all_shells": {k: post[f"{k}_all_shells"] for k in ("none", "dm", "net")},
+            "a_posteriori_times": post["times"],
+            "spectra": {k: post[k] for k in post if k.startswith("spectrum")}}
+    report = {"dns": n, "filters": list(filters), "snapshots": n_snap, "samples_train": int(len(x_tr)),
+              "forcing": list(forcing), "vis": vis, "steps": int(len(hist)), "batch": batch, "lr": lr,
+              "loss_first": float(hist[:10].mean()), "loss_last": float(hist[-10:].mean()),
+              "per_filter": {f: {k: v for k, v in r.items() if k != "spectra"} for f, r in per_filter.items()},
               "seconds": {"dns": t1 - t0, "samples": t2 - t1, "train": t3 - t2}}
+    # the first filter's figures at the top level as well (the layout the
+    # single-filter report had)
+    first = per_filter[str(filters[0])]
+    report.update({"filter": filters[0], "coarse": first["coarse"], "a_priori": first["a_priori"],
+                   "a_posteriori_max_rel_err_k_le_kmax_half": first["a_posteriori_max_rel_err_k_le_kmax_half"]})
     log(json.dumps(report))
     if out:
         os.makedirs(os.path.dirname(out), exist_ok=True)
-        np.savez(out, params=params, loss=hist, report=json.dumps(report), spectra=json.dumps(
-            {k: post[k] for k in post if k.startswith("spectrum")}))
+        np.savez(out, params=params, loss=hist, report=json.dumps(report),
+                 spectra=json.dumps({f: r["spectra"] for f, r in per_filter.items()}))
     return params, report
 
 
@@ -319,18 +353,19 @@ if __name__ == "__main__":
 
     ap = argparse.ArgumentParser(description="train the learned closure on filtered DNS")
     ap.add_argument("--n", type=int, default=512)
-    ap.add_argument("--f", type=int, default=4)
+    ap.add_argument("--filters", type=int, nargs="+", default=[4, 8], help="box-filter ratios of the samples")
     ap.add_argument("--snaps", type=int, default=10)
     ap.add_argument("--steps", type=int, default=0, help="Adam steps (default: one pass over the data)")
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=1e-3)
-    ap.add_argument("--vis", type=float, default=1e-3)
+    ap.add_argument("--vis", type=float, default=5e-4)
     ap.add_argument("--spinup", type=float, default=1.0)
     ap.add_argument("--every", type=float, default=0.1)
-    ap.add_argument("--eval", type=float, default=0.2)
+    ap.add_argument("--eval", type=float, default=1.0, help="a posteriori comparison window")
+    ap.add_argument("--neval", type=int, default=4, help="comparison times in the window")
     ap.add_argument("--sigma", type=float, default=0.5, help="OU forcing rms amplitude")
     ap.add_argument("--tl", type=float, default=0.5, help="OU forcing correlation time")
     ap.add_argument("--out", default=WEIGHTS)
     a = ap.parse_args()
-    run(a.n, a.f, a.snaps, a.steps or None, a.batch, a.lr, a.vis, a.spinup, a.every, a.eval, out=a.out,
-        forcing=(2.5, a.sigma, a.tl))
+    run(a.n, tuple(a.filters), a.snaps, a.steps or None, a.batch, a.lr, a.vis, a.spinup, a.every, a.eval, a.neval,
+        out=a.out, forcing=(2.5, a.sigma, a.tl))

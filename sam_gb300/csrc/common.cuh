@@ -47,6 +47,10 @@ __device__ __forceinline__ int kpos(int j, int km, int m, int n) { return j <= k
 
 constexpr int kThreads = 256;
 
+// sam_gpu_config.precision of the double-float form (FP32 pairs, about 48
+// significand bits; SAM_GPU_PREC_DD in sam_gpu.h)
+constexpr int kPrecDD = 48;
+
 // Streaming multiprocessors of the current device (looked up once per
 // device): persistent and grid-stride launches are sized in multiples of it.
 inline int sm_count() {

@@ -14,11 +14,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "ddfloat.cuh"
+
 namespace samgpu {
 
 template <typename T> struct Cx;
 template <> struct Cx<double> { using type = double2; };
 template <> struct Cx<float> { using type = float2; };
+template <> struct Cx<dd> { using type = ddc; };
 template <typename T> using cx_t = typename Cx<T>::type;
 
 template <typename C> __device__ __forceinline__ C mk(decltype(C::x) a, decltype(C::x) b) { C r; r.x = a; r.y = b; return r; }

@@ -366,5 +366,7 @@ template void convert_in<float>(const double2*, float2*, long long, cudaStream_t
 template void convert_out<float>(const float2*, double2*, long long, cudaStream_t);
 template void convert_in<double>(const double2*, double2*, long long, cudaStream_t);
 template void convert_out<double>(const double2*, double2*, long long, cudaStream_t);
+template void convert_in<dd>(const double2*, ddc*, long long, cudaStream_t);
+template void convert_out<dd>(const ddc*, double2*, long long, cudaStream_t);
 
 }  // namespace samgpu

@@ -1,4 +1,5 @@
-// Argument blocks and launchers of the transform passes (passes.cu).
+// Argument blocks and launchers of the transform passes (passes_impl.cuh,
+// instantiated in passes.cu, passes_f32.cu and passes_dd_*.cu).
 // Strides are in complex (or real, for physical arrays) elements.
 #pragma once
 #include "common.cuh"
@@ -121,6 +122,10 @@ struct ZFwdArgs {
   long long u_ky, u_kx, u_n;
   DevState* state;
   StageConsts sc;
+  // double-float form, mode 2: the integrating factor exp(-nu k^2 dt_fac)
+  // as products of per-direction tables [2][Mx + My + Mz] (velocity, then
+  // temperature with nu / Pr), written by launch_if_tables for this stage
+  const dd* ift;
   T nz_inv;                  // filled by the launcher: 1/Nz
   FastDiv fd_t, fd_m;  // filled by the launcher: ty, Nz_min
 };
@@ -131,10 +136,34 @@ template <typename T> void launch_x_pass(const XPassArgs<T>& a, const FftPlan* p
 template <typename T> int x_pass_blocks(const XPassArgs<T>& a);
 template <typename T> void launch_y_fwd(const YFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
 template <typename T> void launch_z_fwd(const ZFwdArgs<T>& a, const FftPlan* pl, size_t smem, cudaStream_t s);
-template <typename T> void set_smem_limits();
+template <typename T> void smem_limits_zinv(int optin);
+template <typename T> void smem_limits_yinv(int optin);
+template <typename T> void smem_limits_x(int optin);
+template <typename T> void smem_limits_yfwd(int optin);
+template <typename T> void smem_limits_zfwd(int optin);
+// every pass of precision T opted into the device's largest dynamic shared memory
+template <typename T> inline void set_smem_limits() {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  smem_limits_zinv<T>(optin);
+  smem_limits_yinv<T>(optin);
+  smem_limits_x<T>(optin);
+  smem_limits_yfwd<T>(optin);
+  smem_limits_zfwd<T>(optin);
+}
+// vmax (max_only forms): ints 0..7 hold the per-field maxima (FP32 form: the
+// float bit patterns in ints 0..3; double-float form: 64-bit keys of
+// dd_abs_key in ints 0..7, vkind = 1), int 8 the non-finite flag
 void launch_vel_max_finish(const double* partials, int nblk, const Grid& g, DevState* st, int i_cfl, double cfl0,
                            double adv_cfl_limit, cudaStream_t s, const double* pv = nullptr, int npv = 0,
-                           int* vmax = nullptr);
+                           int* vmax = nullptr, int vkind = 0);
+// The double-float form's integrating-factor tables of one stage (mode-2
+// z forward): t[w * (Mx + My + Mz) + r] = exp(-nu_w dt_fac k_r^2) for the
+// wave numbers of kx (r < Mx), ky, then kz, with nu_0 = vis and nu_1 =
+// vis / Pr, dt_fac = (gamma + zeta) dt (sam.f:293-297), dt read on the device.
+void launch_if_tables(const DevState* st, const StageConsts& sc, const Grid& g, dd* t, cudaStream_t s);
+constexpr int kVmaxInts = 16;  // the vmax block at the end of pv
 // vel_max's sums from wave space (Parseval), FP64 arithmetic on the state U
 // (Lu fields (kx, ky, kz)): pv[b * Lu + f] = block b's share of
 // sum w |u|^2 (w = 1 for kx = 0, 2 otherwise), pv[npv * Lu + f] = u(0,0,0).

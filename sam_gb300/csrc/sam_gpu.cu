@@ -49,7 +49,14 @@ struct Plan {
   FftPlan* d = nullptr;
   double2* tw64 = nullptr;
   float2* tw32 = nullptr;
+  ddc* twdd = nullptr;
 };
+
+// the nearest double-float pair to an extended-precision value
+static dd dd_of(long double v) {
+  const float h = (float)v;
+  return dd(h, (float)(v - (long double)h));
+}
 
 // Radices 8, 4, 2, 3, 5 in that order; twiddles w_{l p}^{f q} = exp(-2 pi i
 // f q / (l p)) in long double, rounded once to each working precision.
@@ -85,6 +92,7 @@ static int build_plan(int n, Plan& P) {
   if (pl.team > kThreads) return fail(SAM_GPU_EINVAL, "FFT length %d needs too wide a team", n);
   std::vector<double2> t64;
   std::vector<float2> t32;
+  std::vector<ddc> tdd;
   int l = 1, off = 0;
   const long double two_pi = 6.283185307179586476925286766559005768L;
   pl.tw16_off = -1;
@@ -99,6 +107,7 @@ static int build_plan(int n, Plan& P) {
         const long double c = cosl(a), sn = -sinl(a);
         t64.push_back(make_double2((double)c, (double)sn));
         t32.push_back(make_float2((float)c, (float)sn));
+        tdd.push_back(ddc{dd_of(c), dd_of(sn)});
       }
     off = 256;
   }
@@ -117,30 +126,38 @@ static int build_plan(int n, Plan& P) {
         const long double c = cosl(a), sn = -sinl(a);
         t64.push_back(make_double2((double)c, (double)sn));
         t32.push_back(make_float2((float)c, (float)sn));
+        tdd.push_back(ddc{dd_of(c), dd_of(sn)});
       }
     off += l * (p - 1);
     l *= p;
   }
   pl.tw_total = off;
   pl.tw_pass = n == 256 ? 256 : off;
-  if (t64.empty()) { t64.push_back(make_double2(1, 0)); t32.push_back(make_float2(1, 0)); }
+  if (t64.empty()) {
+    t64.push_back(make_double2(1, 0));
+    t32.push_back(make_float2(1, 0));
+    tdd.push_back(ddc{dd(1), dd(0)});
+  }
   CK(cudaMalloc(&P.d, sizeof(FftPlan)));
   CK(cudaMemcpy(P.d, &pl, sizeof(FftPlan), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&P.tw64, sizeof(double2) * t64.size()));
   CK(cudaMemcpy(P.tw64, t64.data(), sizeof(double2) * t64.size(), cudaMemcpyHostToDevice));
   CK(cudaMalloc(&P.tw32, sizeof(float2) * t32.size()));
   CK(cudaMemcpy(P.tw32, t32.data(), sizeof(float2) * t32.size(), cudaMemcpyHostToDevice));
+  CK(cudaMalloc(&P.twdd, sizeof(ddc) * tdd.size()));
+  CK(cudaMemcpy(P.twdd, tdd.data(), sizeof(ddc) * tdd.size(), cudaMemcpyHostToDevice));
   return 0;
 }
 
 static void free_plan(Plan& P) {
-  cudaFree(P.d); cudaFree(P.tw64); cudaFree(P.tw32);
-  P.d = nullptr; P.tw64 = nullptr; P.tw32 = nullptr;
+  cudaFree(P.d); cudaFree(P.tw64); cudaFree(P.tw32); cudaFree(P.twdd);
+  P.d = nullptr; P.tw64 = nullptr; P.tw32 = nullptr; P.twdd = nullptr;
 }
 
 template <typename T> const cx_t<T>* tw_of(const Plan& P);
 template <> const double2* tw_of<double>(const Plan& P) { return P.tw64; }
 template <> const float2* tw_of<float>(const Plan& P) { return P.tw32; }
+template <> const ddc* tw_of<dd>(const Plan& P) { return P.twdd; }
 
 // -------------------------------------------------------------- the context
 struct Scratch {
@@ -161,7 +178,8 @@ struct Ctx {
   void *U = nullptr, *R = nullptr, *P = nullptr, *S1 = nullptr, *S2 = nullptr, *S3 = nullptr;
   double* partials = nullptr;
   int partial_blocks = 0;
-  double* pv = nullptr;  // vel_max's wave-space sums (FP32 form)
+  double* pv = nullptr;  // vel_max's wave-space sums (FP32 and double-float forms)
+  dd* ift = nullptr;     // double-float form: integrating-factor tables of the stage
   DevState* state = nullptr;
   Scratch sc[4];
   // tile choices
@@ -219,6 +237,17 @@ static int ensure(Scratch& s, size_t bytes) {
 }
 
 static size_t csize(const Ctx& c) { return c.cfg.precision == 32 ? sizeof(float2) : sizeof(double2); }
+
+// The resident state's working precision from / to an FP64 copy of n complex
+// values (no-ops in the FP64 form, whose state is the copy).
+static void state_from_fp64(Ctx& c, const double2* src, void* dst, long long n) {
+  if (c.cfg.precision == 32) convert_in<float>(src, (float2*)dst, n, c.stream);
+  else if (c.cfg.precision == kPrecDD) convert_in<dd>(src, (ddc*)dst, n, c.stream);
+}
+static void state_to_fp64(Ctx& c, const void* src, double2* dst, long long n) {
+  if (c.cfg.precision == 32) convert_out<float>((const float2*)src, dst, n, c.stream);
+  else if (c.cfg.precision == kPrecDD) convert_out<dd>((const ddc*)src, dst, n, c.stream);
+}
 
 static int line_ld(int n) { return line_stride(n); }
 
@@ -375,16 +404,17 @@ static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in
       c.partial_blocks = nblk;
     }
     a.partials = c.partials;
-    // the FP32 form takes vel_max's sums from wave space (Parseval, FP64
-    // arithmetic): the x pass then only forms max |u| and the NaN check
-    a.max_only = sizeof(T) == 4 && in_mode == 0 && in == c.S2;
+    // the FP32 and double-float forms take vel_max's sums from wave space
+    // (Parseval, FP64 arithmetic): the x pass then only forms max |u| and
+    // the NaN check
+    a.max_only = (sizeof(T) == 4 || kIsDD<T>) && in_mode == 0 && in == c.S2;
     a.vmax = reinterpret_cast<int*>(c.pv + 4 * ((size_t)kParsevalBlocks + 1));
   }
   launch_x_pass<T>(a, c.px.d, x_smem<T>(c, nin, a.yt, a.group), c.stream);
   if (stats) {
     if (a.max_only) launch_parseval<T>((const cx_t<T>*)c.U, c.g, c.pv, c.stream);
     launch_vel_max_finish(c.partials, nblk, c.g, c.state, c.cfg.i_cfl, c.cfg.cfl0, c.adv_cfl_limit, c.stream,
-                          a.max_only ? c.pv : nullptr, kParsevalBlocks, a.vmax);
+                          a.max_only ? c.pv : nullptr, kParsevalBlocks, a.vmax, kIsDD<T> ? 1 : 0);
   }
   return 0;
 }
@@ -436,6 +466,10 @@ static int run_z_fwd(Ctx& c, ZFwdArgs<T>& a) {
   a.ld = line_ld(c.g.nz);
   a.sched = c.sched[4];
   a.ty = pick_tile(c.pz, c.ty_zf, a.nf, sizeof(cx_t<T>), a.sched);
+  if (kIsDD<T> && a.mode == 2) {
+    launch_if_tables(c.state, a.sc, c.g, c.ift, c.stream);
+    a.ift = c.ift;
+  }
   launch_z_fwd<T>(a, c.pz.d, tile_smem(c.pz, a.ty * a.nf, sizeof(cx_t<T>), a.sched), c.stream);
   return 0;
 }
@@ -469,13 +503,15 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
   if (ev) cudaEventRecord(ev[2], c.stream);
   // dynamic closure at nrk = 1 (once per step, like vel_max): the physical
   // velocity, then dm.f's coefficient on it
-  if (run(2) && c.les_model == 2 && nrk == 1) {
-    rc = run_x_pass<T>(c, 0, 0, 3, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
-                       nullptr, c.les_phys, 0, 0, 0, g.nx, (long long)g.nx * g.ny, (long long)g.nx * g.ny * g.nz,
-                       false);
-    if (rc) return rc;
-    les_dynamic<T>((const T*)c.les_phys, c.les_work, c.les_cds, g.nx, g.ny, g.nz, c.les_dxi, c.les_dyi, c.les_dzi,
-                   c.stream);
+  if constexpr (!kIsDD<T>) {  // (the double-float form has no closure)
+    if (run(2) && c.les_model == 2 && nrk == 1) {
+      rc = run_x_pass<T>(c, 0, 0, 3, c.S2, nullptr, g.mx, (long long)g.ny * g.mx, (long long)g.nz * g.ny * g.mx,
+                         nullptr, c.les_phys, 0, 0, 0, g.nx, (long long)g.nx * g.ny, (long long)g.nx * g.ny * g.nz,
+                         false);
+      if (rc) return rc;
+      les_dynamic<T>((const T*)c.les_phys, c.les_work, c.les_cds, g.nx, g.ny, g.nz, c.les_dxi, c.les_dyi, c.les_dzi,
+                     c.stream);
+    }
   }
   // learned closure: the invariants of every point, then the network
   if (run(2) && c.les_model == 3) {
@@ -522,7 +558,9 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
 }
 
 static int stage_any(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = -1) {
-  return c.cfg.precision == 32 ? enqueue_stage<float>(c, nrk, ev, only) : enqueue_stage<double>(c, nrk, ev, only);
+  if (c.cfg.precision == 32) return enqueue_stage<float>(c, nrk, ev, only);
+  if (c.cfg.precision == kPrecDD) return enqueue_stage<dd>(c, nrk, ev, only);
+  return enqueue_stage<double>(c, nrk, ev, only);
 }
 
 static int check_launch() {
@@ -542,7 +580,7 @@ static void free_ctx(Ctx* c) {
   free_plan(c->px); free_plan(c->py); free_plan(c->pz);
   cudaFree(c->U); cudaFree(c->R); cudaFree(c->P);
   cudaFree(c->S1); cudaFree(c->S2); cudaFree(c->S3);
-  cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou); cudaFree(c->pv);
+  cudaFree(c->partials); cudaFree(c->state); cudaFree(c->ou); cudaFree(c->pv); cudaFree(c->ift);
   cudaFree(c->les_cds); cudaFree(c->les_phys); cudaFree(c->les_work);
   cudaFree(c->les_feat); cudaFree(c->les_coef);
   cudaFree(c->mlp_p); cudaFree(c->mlp_m); cudaFree(c->mlp_v); cudaFree(c->mlp_g); cudaFree(c->mlp_loss);
@@ -660,7 +698,8 @@ static int init_ctx(const sam_gpu_config* cfg) {
   if (!cfg) return fail(SAM_GPU_EINVAL, "null config");
   if (cfg->nx < 2 || cfg->nx % 2 || cfg->ny < 1 || cfg->nz < 1)
     return fail(SAM_GPU_EINVAL, "grid %d x %d x %d: Nx must be even and >= 2", cfg->nx, cfg->ny, cfg->nz);
-  if (cfg->precision != 64 && cfg->precision != 32) return fail(SAM_GPU_EINVAL, "precision must be 64 or 32");
+  if (cfg->precision != 64 && cfg->precision != 32 && cfg->precision != kPrecDD)
+    return fail(SAM_GPU_EINVAL, "precision must be 64, 48 (double-float pairs) or 32");
   if (cfg->nrk_max < 1 || cfg->nrk_max > 3) return fail(SAM_GPU_EINVAL, "nrk_max must be 1, 2 or 3");
   Ctx* c = new Ctx();
   c->cfg = *cfg;
@@ -718,6 +757,7 @@ static int init_ctx(const sam_gpu_config* cfg) {
   }
   set_smem_limits<double>();
   set_smem_limits<float>();
+  set_smem_limits<dd>();
   diag_set_smem_limits();
   const size_t es = csize(*c);
   const size_t nzmm = (size_t)g.mx * g.my * g.mz;
@@ -734,8 +774,11 @@ static int init_ctx(const sam_gpu_config* cfg) {
   // allocation ever happens inside a captured step
   c->partial_blocks = g.nz * g.ny;
   ok = ok && cudaMalloc(&c->partials, sizeof(double) * 4 * 4 * (size_t)c->partial_blocks) == cudaSuccess;
-  ok = ok && cudaMalloc(&c->pv, sizeof(double) * (4 * ((size_t)kParsevalBlocks + 1) + 4)) == cudaSuccess;
-  if (ok) cudaMemset(c->pv, 0, sizeof(double) * (4 * ((size_t)kParsevalBlocks + 1) + 4));
+  const size_t pv_bytes = sizeof(double) * 4 * ((size_t)kParsevalBlocks + 1) + sizeof(int) * kVmaxInts;
+  ok = ok && cudaMalloc(&c->pv, pv_bytes) == cudaSuccess;
+  if (ok) cudaMemset(c->pv, 0, pv_bytes);
+  if (ok && cfg->precision == kPrecDD)
+    ok = cudaMalloc(&c->ift, sizeof(dd) * 2 * ((size_t)g.mx + g.my + g.mz)) == cudaSuccess;
   if (!ok) { free_ctx(c); g_ctx = nullptr; return fail(SAM_GPU_ECUDA, "device allocation failed"); }
   cudaMemset(c->U, 0, es * g.lu * nzmm);
   cudaMemset(c->R, 0, es * g.lu * nzmm);
@@ -1074,14 +1117,14 @@ int sam_gpu_upload(const double* u) {
   const size_t nm = (size_t)g.mx * g.my * g.mz * g.lu;
   int rc;
   void* dst = c.U;
-  if (c.cfg.precision == 32) {
+  if (c.cfg.precision != 64) {
     if ((rc = ensure(c.sc[0], nm * 16))) return rc;
     dst = c.sc[0].p;
   }
   // rows 1..Nz_min of each (ky, kx, var) column of u(Nze,Ny_min,nxp,Lu)
   CK(cudaMemcpy2DAsync(dst, (size_t)g.mz * 16, u, (size_t)g.nze * 16, (size_t)g.mz * 16, (size_t)g.my * g.mx * g.lu,
                        cudaMemcpyHostToDevice, c.stream));
-  if (c.cfg.precision == 32) convert_in<float>((const double2*)dst, (float2*)c.U, (long long)nm, c.stream);
+  if (c.cfg.precision != 64) state_from_fp64(c, (const double2*)dst, c.U, (long long)nm);
   CK(cudaMemsetAsync(c.R, 0, csize(c) * nm, c.stream));
   return sync_stream(c);
 }
@@ -1091,9 +1134,9 @@ static int download_field(Ctx& c, const void* src, double* host, int nf, int hos
   const size_t nm = (size_t)g.mx * g.my * g.mz * nf;
   const void* s = src;
   int rc;
-  if (c.cfg.precision == 32) {
+  if (c.cfg.precision != 64) {
     if ((rc = ensure(c.sc[1], nm * 16))) return rc;
-    convert_out<float>((const float2*)src, (double2*)c.sc[1].p, (long long)nm, c.stream);
+    state_to_fp64(c, src, (double2*)c.sc[1].p, (long long)nm);
     s = c.sc[1].p;
   }
   double* h = host + (size_t)2 * g.nze * g.my * g.mx * host_field0;
@@ -1151,6 +1194,8 @@ int sam_gpu_step(int nsteps) {
 int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, double t_l, int* n_modes) {
   NEED_CTX();
   if (n_modes) *n_modes = 0;
+  if (c.cfg.precision == kPrecDD && k_f > 0.0 && sigma != 0.0)
+    return fail(SAM_GPU_EUNSUPPORTED, "set_forcing: the double-float form runs the plain step only");
   if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
   c.graph_stale = 1;
   if (k_f <= 0.0 || sigma == 0.0) {
@@ -1178,6 +1223,8 @@ static int mlp_ensure(Ctx& c);
 
 int sam_gpu_set_les(int model, double c_smag, double pr_t) {
   NEED_CTX();
+  if (model != 0 && c.cfg.precision == kPrecDD)
+    return fail(SAM_GPU_EUNSUPPORTED, "set_les: the double-float form runs the plain step only");
   if (model < 0 || model > 3)
     return fail(SAM_GPU_EINVAL, "set_les: model %d (0 off, 1 Smagorinsky, 2 dynamic, 3 learned)", model);
   if (!(pr_t > 0.0)) return fail(SAM_GPU_EINVAL, "set_les: turbulent Prandtl number must be > 0");
@@ -1436,6 +1483,7 @@ int sam_gpu_box_filter(int f, double* out) {
   const Grid& g = c.g;
   if (!out || f < 1 || g.nx % f || g.ny % f || g.nz % f)
     return fail(SAM_GPU_EINVAL, "box_filter: the grid must divide into blocks of %d", f);
+  if (c.cfg.precision == kPrecDD) return fail(SAM_GPU_EUNSUPPORTED, "box_filter: not in the double-float form");
   return c.cfg.precision == 32 ? box_filter_impl<float>(c, f, out) : box_filter_impl<double>(c, f, out);
 }
 
@@ -1479,6 +1527,7 @@ int sam_gpu_closure_inputs(unsigned short* feat, double* grads) {
   double dsq, dxi, dyi, dzi;
   grid_spacing(c, dxi, dyi, dzi, dsq);
   c.les_dsq = dsq;
+  if (c.cfg.precision == kPrecDD) return fail(SAM_GPU_EUNSUPPORTED, "closure_inputs: not in the double-float form");
   return c.cfg.precision == 32 ? closure_inputs_impl<float>(c, feat, grads)
                                : closure_inputs_impl<double>(c, feat, grads);
 }
@@ -1643,7 +1692,7 @@ int sam_gpu_profile_stage(int nrk, int reps, float* ms5) {
 static int init_finish(Ctx& c, double2* tmp) {
   const Grid& g = c.g;
   const size_t nm = (size_t)g.mx * g.my * g.mz * g.lu;
-  if (c.cfg.precision == 32) convert_in<float>(tmp, (float2*)c.U, (long long)nm, c.stream);
+  if (c.cfg.precision != 64) state_from_fp64(c, tmp, c.U, (long long)nm);
   CK(cudaMemsetAsync(c.R, 0, csize(c) * nm, c.stream));
   return sync_stream(c);
 }
@@ -1651,7 +1700,7 @@ static int init_finish(Ctx& c, double2* tmp) {
 static int init_target(Ctx& c, double2** out) {
   const Grid& g = c.g;
   const size_t nm = (size_t)g.mx * g.my * g.mz * g.lu;
-  if (c.cfg.precision == 32) {
+  if (c.cfg.precision != 64) {
     int rc = ensure(c.sc[0], nm * 16);
     if (rc) return rc;
     *out = (double2*)c.sc[0].p;
@@ -1693,6 +1742,28 @@ int sam_gpu_init_packet(unsigned long long seed, int kx0, int ky0, int kz0, doub
 
 // ------------------------------------------------------------- diagnostics
 
+// The state the diagnostics read: U and R themselves in the FP64 and FP32
+// forms; FP64 copies (scratch 1 and 2) in the double-float form, whose
+// diagnostics then run the FP64 kernels (prec).
+static int diag_state(Ctx& c, bool with_r, void** u, const void** r, int* prec) {
+  *u = c.U;
+  if (r) *r = c.R;
+  *prec = c.cfg.precision;
+  if (c.cfg.precision != kPrecDD) return 0;
+  const long long nm = (long long)c.g.mx * c.g.my * c.g.mz * c.g.lu;
+  int rc;
+  if ((rc = ensure(c.sc[1], (size_t)nm * 16))) return rc;
+  state_to_fp64(c, c.U, (double2*)c.sc[1].p, nm);
+  *u = c.sc[1].p;
+  if (with_r) {
+    if ((rc = ensure(c.sc[2], (size_t)nm * 16))) return rc;
+    state_to_fp64(c, c.R, (double2*)c.sc[2].p, nm);
+    *r = c.sc[2].p;
+  }
+  *prec = 64;
+  return 0;
+}
+
 int sam_gpu_spectra(double* out) {
   NEED_CTX();
   int rc = ensure(c.sc[3], sizeof(double) * ((size_t)5 * c.lm + 8) * 1024);
@@ -1701,8 +1772,12 @@ int sam_gpu_spectra(double* out) {
   if (c.cfg.i_les) {
     if ((rc = sam_gpu_cl_energy(&e_cl))) return rc;
   }
-  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, e_cl, c.cfg.precision);
-  diag_spectra(d, c.U, c.R, (double*)c.sc[3].p, out, c.stream);
+  void* u;
+  const void* r;
+  int prec;
+  if ((rc = diag_state(c, true, &u, &r, &prec))) return rc;
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, e_cl, prec);
+  diag_spectra(d, u, r, (double*)c.sc[3].p, out, c.stream);
   return sync_stream(c);
 }
 
@@ -1710,8 +1785,11 @@ int sam_gpu_div_check(double* out4) {
   NEED_CTX();
   int rc = ensure(c.sc[3], sizeof(double) * 8 * 1024);
   if (rc) return rc;
-  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, c.cfg.precision);
-  diag_div_check(d, c.U, (double*)c.sc[3].p, out4, c.stream);
+  void* u;
+  int prec;
+  if ((rc = diag_state(c, false, &u, nullptr, &prec))) return rc;
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, prec);
+  diag_div_check(d, u, (double*)c.sc[3].p, out4, c.stream);
   return sync_stream(c);
 }
 
@@ -1719,8 +1797,11 @@ int sam_gpu_cl_energy(double* e_cl) {
   NEED_CTX();
   int rc = ensure(c.sc[3], sizeof(double) * 8 * 1024);
   if (rc) return rc;
-  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, c.cfg.precision);
-  diag_cl_energy(d, c.U, (double*)c.sc[3].p, e_cl, c.stream);
+  void* u;
+  int prec;
+  if ((rc = diag_state(c, false, &u, nullptr, &prec))) return rc;
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, prec);
+  diag_cl_energy(d, u, (double*)c.sc[3].p, e_cl, c.stream);
   return sync_stream(c);
 }
 
@@ -1731,8 +1812,13 @@ int sam_gpu_force(const double* ek_0, int k_force) {
   int rc = ensure(c.sc[3], sizeof(double) * 64);
   if (rc) return rc;
   CK(cudaMemcpyAsync(c.sc[3].p, ek_0, sizeof(double) * (k_force + 1), cudaMemcpyHostToDevice, c.stream));
-  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, c.cfg.precision);
-  diag_force(d, c.U, (const double*)c.sc[3].p, k_force, c.stream);
+  void* u;
+  int prec;
+  if ((rc = diag_state(c, false, &u, nullptr, &prec))) return rc;
+  DiagArgs d = diag_args(c.g, c.lm, c.nx2, c.k_cl, c.cfg.vis, c.cfg.i_les, 0.0, prec);
+  diag_force(d, u, (const double*)c.sc[3].p, k_force, c.stream);
+  // the double-float form rescaled an FP64 copy: back into the state
+  if (u != c.U) state_from_fp64(c, (const double2*)u, c.U, (long long)c.g.mx * c.g.my * c.g.mz * c.g.lu);
   return sync_stream(c);
 }
 
@@ -1749,7 +1835,7 @@ static int resident_fp64(Ctx& c, const double2** out) {
   }
   int rc = ensure(c.sc[1], nm * 16);
   if (rc) return rc;
-  convert_out<float>((const float2*)c.U, (double2*)c.sc[1].p, (long long)nm, c.stream);
+  state_to_fp64(c, c.U, (double2*)c.sc[1].p, (long long)nm);
   *out = (const double2*)c.sc[1].p;
   return 0;
 }
@@ -1792,12 +1878,12 @@ int sam_gpu_read_field(const char* fname) {
   if (r != expect) return fail(SAM_GPU_EINVAL, "read_field: short read from %s", fname);
   int rc;
   void* dst = c.U;
-  if (c.cfg.precision == 32) {
+  if (c.cfg.precision != 64) {
     if ((rc = ensure(c.sc[0], expect))) return rc;
     dst = c.sc[0].p;
   }
   CK(cudaMemcpyAsync(dst, host.data(), expect, cudaMemcpyHostToDevice, c.stream));
-  if (c.cfg.precision == 32) convert_in<float>((const double2*)dst, (float2*)c.U, (long long)nm, c.stream);
+  if (c.cfg.precision != 64) state_from_fp64(c, (const double2*)dst, c.U, (long long)nm);
   CK(cudaMemsetAsync(c.R, 0, csize(c) * nm, c.stream));
   return sync_stream(c);
 }
@@ -1974,6 +2060,7 @@ int sam_gpu_planes(const int* k_xy, int n_xy, const int* j_xz, int n_xz, const i
     if (i_yz[m] < 1 || i_yz[m] > g.nx) return fail(SAM_GPU_EINVAL, "planes: i_yz(%d) = %d outside 1..%d", m + 1, i_yz[m], g.nx);
     sel.i_yz[m] = i_yz[m] - 1;
   }
+  if (c.cfg.precision == kPrecDD) return fail(SAM_GPU_EUNSUPPORTED, "planes: not in the double-float form");
   const int rc = c.cfg.precision == 32 ? planes_impl<float>(c, sel, xy, xz, yz, mean)
                                        : planes_impl<double>(c, sel, xy, xz, yz, mean);
   if (rc) return rc;

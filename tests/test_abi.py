@@ -41,3 +41,19 @@ def test_calls_before_init_fail_cleanly():
     assert lib.sam_gpu_dims(None) == -2
     lib.sam_gpu_error_string.restype = ctypes.c_char_p
     assert b"sam_gpu_init" in lib.sam_gpu_error_string()
+
+
+def test_fortran_module_binds_every_symbol():
+    """include/sam_gpu.f90 (the ISO_C_BINDING module sam.f uses) has one
+    bind(C) interface per routine the header declares, with the same number
+    of arguments."""
+    f90 = open(os.path.join(ROOT, "include", "sam_gpu.f90")).read().replace("&\n", " ")
+    bound = dict((m.group(2), m.group(1)) for m in
+                 re.finditer(r"function\s+\w+\(([^)]*)\)\s*bind\(C,\s*name=\"(sam_gpu_\w+)\"\)", f90))
+    header = open(os.path.join(ROOT, "include", "sam_gpu.h")).read()
+    for sym in declared_symbols():
+        assert sym in bound, sym
+        m = re.search(r"^\s*(?:int|const char\*)\s+" + sym + r"\s*\(([^)]*)\)", header, re.M)
+        c_args = [a for a in m.group(1).replace("\n", " ").split(",") if a.strip() not in ("", "void")]
+        f_args = [a for a in bound[sym].split(",") if a.strip()]
+        assert len(c_args) == len(f_args), (sym, c_args, f_args)

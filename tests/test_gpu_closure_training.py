@@ -13,8 +13,8 @@ pytestmark = pytest.mark.gpu
 
 @pytest.fixture(scope="module")
 def trained(gpu_lib):
-    params, report = CD.run(n=128, f=4, n_snap=4, steps=300, batch=4096, lr=2e-3, vis=5e-3, t_spinup=0.5,
-                            t_every=0.1, t_eval=0.2, out=None, log=lambda *a: None)
+    params, report = CD.run(n=128, filters=(4,), n_snap=4, steps=300, batch=4096, lr=2e-3, vis=5e-3,
+                            t_spinup=0.5, t_every=0.1, t_eval=0.2, out=None, log=lambda *a: None)
     return params, report
 
 
