@@ -50,10 +50,69 @@ __device__ __forceinline__ float2 csub(float2 a, float2 b) {
   asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(f2_pack(a)), "l"(f2_pack(b)));
   return f2_unpack(r);
 }
+// Double-float complex sums with the real and imaginary parts in one packed
+// pair per instruction: the high parts' TwoSum, the low parts' sum and the
+// renormalisation of ddfloat.cuh's operator+, each step on (re, im) at once
+// (the same IEEE operations and results as two scalar pair sums).
+__device__ __forceinline__ unsigned long long f2p(float a, float b) {
+  unsigned long long r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2u(unsigned long long r, float& a, float& b) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long f2add(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ unsigned long long f2sub(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+// s + e = H +- K exactly (TwoSum; for the difference with -K folded in), then
+// the low parts' sum L added and the pair renormalised
+template <bool SUB>
+__device__ __forceinline__ ddc dd_cplx_sum(unsigned long long H, unsigned long long K, unsigned long long L) {
+  const unsigned long long s = SUB ? f2sub(H, K) : f2add(H, K);
+  const unsigned long long bb = f2sub(s, H);
+  const unsigned long long t = f2sub(H, f2sub(s, bb));
+  unsigned long long e = SUB ? f2sub(t, f2add(K, bb)) : f2add(t, f2sub(K, bb));
+  e = f2add(e, L);
+  const unsigned long long h = f2add(s, e);
+  const unsigned long long l = f2sub(e, f2sub(h, s));
+  ddc r;
+  f2u(h, r.x.hi, r.y.hi);
+  f2u(l, r.x.lo, r.y.lo);
+  return r;
+}
+__device__ __forceinline__ ddc cadd(ddc a, ddc b) {
+  return dd_cplx_sum<false>(f2p(a.x.hi, a.y.hi), f2p(b.x.hi, b.y.hi),
+                            f2add(f2p(a.x.lo, a.y.lo), f2p(b.x.lo, b.y.lo)));
+}
+__device__ __forceinline__ ddc csub(ddc a, ddc b) {
+  return dd_cplx_sum<true>(f2p(a.x.hi, a.y.hi), f2p(b.x.hi, b.y.hi),
+                           f2sub(f2p(a.x.lo, a.y.lo), f2p(b.x.lo, b.y.lo)));
+}
 // a * w (SIGN=-1) or a * conj(w) (SIGN=+1)
 template <int SIGN, typename C> __device__ __forceinline__ C ctw(C a, C w) {
   if (SIGN < 0) return mk<C>(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
   return mk<C>(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
+}
+// double-float pairs: each part as one fused product difference (one
+// renormalisation instead of three)
+template <int SIGN> __device__ __forceinline__ ddc ctw(ddc a, ddc w) {
+  ddc r;
+  if (SIGN < 0) {
+    r.x = dd_mul_sub(a.x, w.x, a.y, w.y);
+    r.y = dd_mul_add(a.x, w.y, a.y, w.x);
+  } else {
+    r.x = dd_mul_add(a.x, w.x, a.y, w.y);
+    r.y = dd_mul_sub(a.y, w.x, a.x, w.y);
+  }
+  return r;
 }
 // multiply by SIGN * i  (exp(SIGN i pi/2))
 template <int SIGN, typename C> __device__ __forceinline__ C cmul_si(C a) {
@@ -198,6 +257,17 @@ template <int SIGN, typename C> __device__ __forceinline__ void dft5(C* a) {
   a[3] = csub(m2, n2);
 }
 
+// v * (cr + i si) for real constants cr, si
+template <typename C, typename T> __device__ __forceinline__ C crot(C v, T cr, T si) {
+  return mk<C>(v.x * cr - v.y * si, v.x * si + v.y * cr);
+}
+__device__ __forceinline__ ddc crot(ddc v, dd cr, dd si) {
+  ddc r;
+  r.x = dd_mul_sub(v.x, cr, v.y, si);
+  r.y = dd_mul_add(v.x, si, v.y, cr);
+  return r;
+}
+
 // 16-point DFT in registers as 4 x 4: DFT4 over n1 of x[4 n1 + n2], the
 // twiddles w16^{n2 k1}, DFT4 over n2; output k1 + 4 k2 in place.
 template <int SIGN, typename C> __device__ __forceinline__ void dft16(C* a) {
@@ -214,7 +284,7 @@ template <int SIGN, typename C> __device__ __forceinline__ void dft16(C* a) {
     for (int k1 = 0; k1 < 4; ++k1) b[n2][k1] = t[k1];
   }
   // w16^j = (cos(2 pi j/16), SIGN sin(2 pi j/16)) for j = n2 k1
-  auto rot = [&](C v, T cr, T si) { return mk<C>(v.x * cr - v.y * si, v.x * si + v.y * cr); };
+  auto rot = [&](C v, T cr, T si) { return crot(v, cr, si); };
   const T sg = (T)SIGN;
   b[1][1] = rot(b[1][1], c1, sg * s1);   // j = 1
   b[1][2] = rot(b[1][2], h, sg * h);     // j = 2

@@ -52,8 +52,10 @@ template <int K, int PATH> struct MinBlocks<double, K, PATH> {
 };
 // double-float pairs: the 16 x 16 register path holds 16 complex pairs (64
 // registers) per thread, as in FP64
+// (the z-forward epilogue keeps one CTA: its tiles fill the shared memory of
+// an SM anyway, and two modes' inputs in flight need the registers)
 template <int K, int PATH> struct MinBlocks<dd, K, PATH> {
-  static constexpr int value = PATH == kFftGeneric ? 1 : 2;
+  static constexpr int value = PATH == kFftGeneric || K == kPassZFwd ? 1 : 2;
 };
 template <typename V, typename Get, typename Put>
 __device__ __forceinline__ void batched(int count, Get get, Put put) {
@@ -71,6 +73,15 @@ __device__ __forceinline__ void batched(int count, Get get, Put put) {
     }
   }
 }
+
+// v * s for a constant s of the launch: in the double-float form, when s is
+// a power of two (1/Nz, 1/(2 Nx Ny) on power-of-two grids), two exact FP32
+// products instead of a pair product
+template <typename W> __device__ __forceinline__ W scale_by(W v, W s, bool pow2) { return v * s; }
+template <> __device__ __forceinline__ dd scale_by<dd>(dd v, dd s, bool pow2) {
+  return pow2 ? dd(__fmul_rn(v.hi, s.hi), __fmul_rn(v.lo, s.hi)) : v * s;
+}
+__host__ __device__ inline bool is_pow2_inv(int n) { return n > 0 && (n & (n - 1)) == 0; }
 
 // First-stage loader reading element idx of a row in global memory.
 // Store phase of the transposes: line t (t < nl) of a tile of `tile` lines
@@ -836,6 +847,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
     return;
   }
   const T fn = a.fn;  // 1/(Nx Ny) (xy_trans_f.f:20) and the 1/2 of the split
+  const bool fn_pow2 = is_pow2_inv(nx) && is_pow2_inv(ny);
   // output line q = m * Y/2 + c: pair c of output field m.  out_mode 1
   // transforms the input lines in place, all at once; out_mode 2 forms the
   // products `group` lines at a time (group >= 1 by construction)
@@ -875,8 +887,8 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
           for (int kx = lane; kx < mx; kx += lanes, o += ostep) {
             const C z1 = ln[sidx(kx)];
             const C z2 = ln[sidx(kx == 0 ? 0 : nx - kx)];
-            const C ve = mk<C>((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
-            const C vo = mk<C>((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
+            const C ve = mk<C>(scale_by(z1.x + z2.x, fn, fn_pow2), scale_by(z1.y - z2.y, fn, fn_pow2));
+            const C vo = mk<C>(scale_by(z1.y + z2.y, fn, fn_pow2), scale_by(z2.x - z1.x, fn, fn_pow2));
             if (two) {
               if ((reinterpret_cast<uintptr_t>(o) & (2 * sizeof(C) - 1)) == 0) {
                 store_pair(o, ve, vo);
@@ -934,7 +946,7 @@ __device__ __forceinline__ float wexp(float x) { return expf(x); }
 // thread: the FP32 form then touches no FP64 arithmetic per mode.
 template <typename W> struct EpiConst {
   W wave_x, wave_y, wave_z, nz_inv, dt_fac1, dt_fac2, mvis_f, mvis_t, bx, bz, lapse, cth, sth;
-  bool same_t;
+  bool same_t, nz_pow2;
 };
 
 template <typename W, typename T>
@@ -943,6 +955,7 @@ __device__ __forceinline__ EpiConst<W> epi_const(const ZFwdArgs<T>& a, double dt
   EpiConst<W> e;
   e.wave_x = (W)a.g.wave_x; e.wave_y = (W)a.g.wave_y; e.wave_z = (W)a.g.wave_z;
   e.nz_inv = (W)a.nz_inv;
+  e.nz_pow2 = is_pow2_inv(a.g.nz);
   e.dt_fac1 = (W)(sc.gamma * dt);
   e.dt_fac2 = (W)(sc.zeta * dt);
   const double vis_f = sc.vis * (sc.gamma * dt + sc.zeta * dt);  // sam.f:293-295
@@ -1007,8 +1020,8 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
   for (int f = 0; f < 9; ++f) {
     if (f < nf) {
       const C v = ln[f * fstride];
-      tr[f] = (W)v.x * c.nz_inv;
-      ti[f] = (W)v.y * c.nz_inv;
+      tr[f] = scale_by((W)v.x, c.nz_inv, c.nz_pow2);
+      ti[f] = scale_by((W)v.y, c.nz_inv, c.nz_pow2);
     } else {
       tr[f] = (W)0; ti[f] = (W)0;
     }
