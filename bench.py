@@ -291,60 +291,101 @@ def les_cfg(precision):
                 lapse=1.0, precision=precision)
 
 
-def les_forms(stream, K, W):
-    """Steps/s of the FP64 drop-in with dm.f's dynamic closure and of the
-    FP32 bulk form with the learned closure on the LES workload from the same
-    start (CUDA events on the launching stream), and how far the FP32 +
-    learned spectrum is from the FP64 + dm.f spectrum after the timed steps
-    (shells k <= k_max/2)."""
+def les_forms(stream, K, W, t_spin=1.5, t_win=1.0, n_win=10):
+    """The LES workload in three forms, each spun up on its own from the same
+    random start and OU forcing: the FP64 drop-in with dm.f's dynamic
+    closure (the judge), the FP32 bulk form with the learned closure, and the
+    FP32 bulk form with no model (a control).  Steps/s of the first two (K
+    steps from their developed state after W warm-up steps, CUDA events on
+    the launching stream); then each form's kinetic-energy spectrum averaged
+    over n_win samples of the window (t_spin, t_spin + t_win], and its largest
+    relative difference from the dm.f form's over shells k <= k_max/2."""
     import numpy as np
     import torch
     from sam_gb300 import SamGpu
     params, src = closure_params()
-    out = {"workload": LES_WORKLOAD, "spinup": "FP32 + learned closure to t = 1 (untimed), then both runs from "
-                                               "that state"}
-    # a developed start: the random field has no energy near the cutoff
-    g = SamGpu(**les_cfg(32))
-    g.init_random(3, 6, 1.0, 6, 0.1)
-    g.set_forcing(4, 2.5, 0.15, 0.5)
-    g.mlp_set(params)
-    g.set_les(3)
-    while g.stats()["time"] < 1.0:
-        g.step(20)
-    u0 = g.download()
-    g.close()
-    spectra = {}
-    for name, prec, model in (("fp64_dm", 64, 2), ("fp32_learned", 32, 3)):
+    out = {"workload": LES_WORKLOAD,
+           "comparison": f"each form spun up independently from the same start to t = {t_spin}, E(k) averaged "
+                         f"over {n_win} samples in t in ({t_spin}, {t_spin + t_win}]"}
+
+    def advance(g, t_end, chunk=10):
+        while g.stats()["time"] < t_end:
+            g.step(chunk)
+
+    avg = {}
+    for name, prec, model in (("fp64_dm", 64, 2), ("fp32_learned", 32, 3), ("fp32_none", 32, 0)):
         g = SamGpu(**les_cfg(prec))
         g.set_stream(stream.cuda_stream)
-        g.upload(u0)
+        g.init_random(3, 6, 1.0, 6, 0.1)
         g.set_forcing(4, 2.5, 0.15, 0.5)
         if model == 3:
             g.mlp_set(params)
-        g.set_les(model)
+        if model:
+            g.set_les(model)
         g.autotune(3)  # tiles for this form's passes (setup, outside the timed region)
-        g.step(W)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(stream):
-            e0.record(stream)
-            g.step(K)
-            e1.record(stream)
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
-        spectra[name] = g.spectra()["ek"]
-        passes = [g.profile_stage(nrk, 2) for nrk in (1, 2, 3)]
-        out[name] = {"value": K / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / K,
-                     "c_delta_sq_final": g.les_coef() if model == 2 else None,
-                     "passes_ms": {k: sum(p[k] for p in passes) / 3 for k in passes[0]}}
+        advance(g, 0.5 * t_spin)
+        row = {}
+        if model:
+            g.step(W)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                g.step(K)
+                e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+            passes = [g.profile_stage(nrk, 2) for nrk in (1, 2, 3)]
+            row = {"value": K / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / K,
+                   "passes_ms": {k: sum(p[k] for p in passes) / 3 for k in passes[0]}}
+        advance(g, t_spin)
+        eks = []
+        for i in range(n_win):
+            advance(g, t_spin + t_win * (i + 1) / n_win)
+            eks.append(g.spectra()["ek"])
+        avg[name] = np.mean(eks, axis=0)
+        st = g.stats()
+        row.update({"time_final": st["time"], "energy_final": st["energy"],
+                    "c_delta_sq_final": g.les_coef() if model == 2 else None})
+        out[name] = row
         g.close()
     kmax = int((N - 0.1) / 3)
     ks = np.arange(1, kmax // 2 + 1)
     out["speedup_fp32_learned_over_fp64_dm"] = out["fp32_learned"]["value"] / out["fp64_dm"]["value"]
-    out["spectrum_max_rel_diff_k_le_kmax_half"] = float(
-        np.abs(spectra["fp32_learned"][ks] / spectra["fp64_dm"][ks] - 1).max())
-    out["after_steps"] = W + K
+    out["spectrum_max_rel_diff_k_le_kmax_half"] = float(np.abs(avg["fp32_learned"][ks] / avg["fp64_dm"][ks] - 1).max())
+    out["spectrum_max_rel_diff_k_le_kmax_half_no_model"] = float(
+        np.abs(avg["fp32_none"][ks] / avg["fp64_dm"][ks] - 1).max())
+    out["spectrum_max_rel_diff_all_shells"] = {
+        k: float(np.abs(avg[k][1:kmax + 1] / avg["fp64_dm"][1:kmax + 1] - 1).max()) for k in ("fp32_learned",
+                                                                                          "fp32_none")}
     out["network"] = src
+    return out
+
+
+def closure_training_rate(steps=300, batch=8192, n=1 << 21):
+    """Adam training throughput of the closure network (samples/s) on
+    synthetic features, with the backward contractions on the tensor cores
+    and, for comparison, on the CUDA cores (host clock around
+    sam_gpu_mlp_train, which synchronises)."""
+    import numpy as np
+    from sam_gb300 import SamGpu
+    from sam_gb300 import closure_data as CD
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal((n, 12)).astype(np.float32)
+    y = (0.02 * np.abs(rng.standard_normal((n, 2)))).astype(np.float32)
+    g = SamGpu(nx=16, ny=16, nz=16)
+    out = {"batch": batch, "steps": steps, "unit": "samples/s"}
+    try:
+        for name, tc in (("tensor_cores", True), ("cuda_cores", False)):
+            g.mlp_set(CD.init_params(0))
+            g.mlp_set_backward(tc)
+            g.mlp_train(x, y, 20, batch, 1e-3)  # warm-up
+            t0 = time.perf_counter()
+            g.mlp_train(x, y, steps, batch, 1e-3)
+            out[name] = steps * batch / (time.perf_counter() - t0)
+    finally:
+        g.close()
+    out["speedup"] = out["tensor_cores"] / out["cuda_cores"]
     return out
 
 
@@ -676,6 +717,7 @@ def main():
     les = None
     if not args.no_les:
         les = les_forms(stream, max(K, 20), W)
+        les["closure_training"] = closure_training_rate()
     ens = None
     if not args.no_ensemble:
         ens = ensemble_form(max(4, K // 2), W)

@@ -260,6 +260,10 @@ module sam_gpu
       type(c_ptr), value :: features, target, grad, loss
       integer(c_long_long), value :: n
     end function
+    integer(c_int) function sam_gpu_mlp_set_backward(tensor_cores) bind(C, name="sam_gpu_mlp_set_backward")
+      import :: c_int
+      integer(c_int), value :: tensor_cores
+    end function
     integer(c_int) function sam_gpu_mlp_train(features, target, n, steps, batch, lr, loss_hist) &
         bind(C, name="sam_gpu_mlp_train")
       import :: c_int, c_ptr, c_long_long, c_float

@@ -276,6 +276,10 @@ int sam_gpu_mlp_grad(const float* features, const float* target, long long n, fl
 /* `steps` Adam steps (lr, beta 0.9/0.999, eps 1e-8) on minibatches of
  * `batch` points taken in order from the data as given (the caller
  * shuffles); loss_hist (may be NULL) receives each minibatch's loss. */
+/* Backward pass of sam_gpu_mlp_grad / sam_gpu_mlp_train: 1 (default) the
+ * contractions as tcgen05 tensor-core MMAs, 0 the CUDA-core kernel (the same
+ * gradient to the rounding of the deltas' two-part BF16 split, about 2^-17). */
+int sam_gpu_mlp_set_backward(int tensor_cores);
 int sam_gpu_mlp_train(const float* features, const float* target, long long n, int steps, int batch, float lr,
                       float* loss_hist);
 /* Training data of the closure.  sam_gpu_box_filter: the resident field

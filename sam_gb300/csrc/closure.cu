@@ -487,6 +487,259 @@ __global__ void __launch_bounds__(128) k_mlp_bwd(const __nv_bfloat16* __restrict
   if (tid == 0) out[kMlpParams] = (s_loss[0] + s_loss[1]) + (s_loss[2] + s_loss[3]);
 }
 
+// -------------------------------------------- backward pass on tensor cores
+// The three contractions of the backward pass as tcgen05 MMAs, per tile of
+// 128 points (thread t owns point t, TMEM lane t):
+//   (1) hidden-1 pre-deltas   G1  = D2 W2          M = 128 points, N = 64, K = 64
+//   (2) layer 1 and 2 weights [D2^T; D1^T] [H1 | 1 | X | 1]^T
+//                                                  M = 128, N = 96, K = 128 points
+//       rows 0..63 x columns 0..79 give dW2 and db2 (H1's constant-1
+//       columns), rows 64..127 x columns 80..95 give dW1 and db1 (the input
+//       tile's constant-1 column); the two off-diagonal blocks are unused
+//   (3) layer 3 weights       [H2^T; 1] [DO_hi | DO_lo]^T
+//                                                  M = 128 (65 used), N = 16 (4 used), K = 128
+// The deltas are FP32; each enters the BF16 MMAs as an exact two-part split
+// hi + lo (hi = bf16(d), lo = bf16(d - hi): 16 significand bits), so the
+// products with the BF16 activations and weights lose nothing beyond 2^-17
+// of the delta.  The weight gradients accumulate in TMEM over the CTA's tiles
+// (persistent CTAs, fixed tile order); the CTA then writes its partial sums,
+// reduced over CTAs in a fixed order by k_mlp_reduce as before.
+constexpr int kBk = 128;  // K of the weight-gradient MMAs: the points of a tile
+struct MlpBwdSmem {
+  uint8_t w2t[kMlpH * kMlpH * 2];         // W2^T as [k][n] (N = 64, K = 64)
+  uint8_t ad2[2][kMlpTile * kMlpH * 2];   // D2 [point][n], hi and lo (M = 128, K = 64)
+  uint8_t ast[2][128 * kBk * 2];          // [D2^T; D1^T], hi and lo (M = 128, K = 128)
+  uint8_t bst[96 * kBk * 2];              // [H1^T; 1; X^T] (N = 96, K = 128)
+  uint8_t a3[128 * kBk * 2];              // [H2^T; 1; 0] (M = 128, K = 128)
+  uint8_t b3[16 * kBk * 2];               // [DO_hi; DO_lo; 0] (N = 16, K = 128)
+  float w3[kMlpOut * kMlpH];
+  float red[4][kMlpOut];
+  uint64_t mbar;
+  uint32_t tbase;
+};
+constexpr size_t kMlpBwdSmemBytes = sizeof(MlpBwdSmem) + 1024;
+
+__device__ __forceinline__ void st_bf16(uint8_t* tile, uint32_t off, float v) {
+  *reinterpret_cast<__nv_bfloat16*>(tile + off) = __float2bfloat16_rn(v);
+}
+// the two-part split of v into the hi and lo tiles
+__device__ __forceinline__ void st_split(uint8_t* hi, uint8_t* lo, uint32_t off, float v) {
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  *reinterpret_cast<__nv_bfloat16*>(hi + off) = h;
+  *reinterpret_cast<__nv_bfloat16*>(lo + off) = __float2bfloat16_rn(v - __bfloat162float(h));
+}
+
+__global__ void __launch_bounds__(128, 1)
+    k_mlp_bwd_tc(const __nv_bfloat16* __restrict__ x16, const float2* __restrict__ y, long long n,
+                 const MlpDev* __restrict__ P, const __nv_bfloat16* __restrict__ h1g,
+                 const __nv_bfloat16* __restrict__ h2g, const float* __restrict__ og, float* __restrict__ part,
+                 int* err) {
+  extern __shared__ __align__(1024) uint8_t bwd_smem[];
+  MlpBwdSmem& S = *reinterpret_cast<MlpBwdSmem*>(bwd_smem + ((1024u - (smem_u32(bwd_smem) & 1023u)) & 1023u));
+  const int t = threadIdx.x;
+  const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
+  if (t < 32) tmem_alloc(&S.tbase, 256);
+  if (t == 0) {
+    mbar_init(&S.mbar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  // W2^T (element (k, n) = W2[n][k]) and the FP32 copy of W3
+  for (int e = t; e < kMlpH * kMlpH; e += blockDim.x) {
+    const int nn = e / kMlpH, k = e - nn * kMlpH;
+    *reinterpret_cast<__nv_bfloat16*>(S.w2t + kmaj(k, nn, kMlpH)) = P->w2[nn * kMlpK2 + k];
+  }
+  for (int e = t; e < kMlpOut * kMlpH; e += blockDim.x)
+    S.w3[e] = __bfloat162float(P->w3[(e / kMlpH) * kMlpK2 + e % kMlpH]);
+  // the constant rows of this thread's column (point t) of the operand tiles
+  for (int r = 64; r < 80; ++r) st_bf16(S.bst, kmaj(r, t, kBk), r < 67 ? 1.f : 0.f);
+  for (int r = 64; r < 128; ++r) st_bf16(S.a3, kmaj(r, t, kBk), r == 64 ? 1.f : 0.f);
+  for (int r = 4; r < 16; ++r) st_bf16(S.b3, kmaj(r, t, kBk), 0.f);
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tm = S.tbase;
+  const uint32_t tl = tm + ((uint32_t)(32 * (t >> 5)) << 16);  // this warp's lanes
+  const uint32_t c_g1 = 0, c_st = 64, c_3 = 160;                // TMEM columns of the three results
+  const float inv_n = 1.0f / (float)n;
+  float loss = 0.f;
+  uint32_t ph = 0;
+  int bad = 0;
+  bool mpend = false;
+  auto wait_mma = [&]() {
+    int b = t == 0 ? mbar_wait(&S.mbar, ph) : 0;
+    b = __syncthreads_or(b);
+    if (!b) {
+      ph ^= 1u;
+      mpend = false;
+    }
+    tc_fence_after();
+    return b;
+  };
+  bool first = true;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long row = tile * kMlpTile + t;
+    const bool live = row < n;
+    // ---- this point's deltas (FP32)
+    float dout[kMlpOut] = {0.f, 0.f};
+    if (live) {
+      const float2 yy = y[row];
+      const float tg[2] = {yy.x, yy.y};
+#pragma unroll
+      for (int j = 0; j < kMlpOut; ++j) {
+        const float o = og[2 * row + j];
+        const float sig = 1.f / (1.f + expf(-o));
+        const float r = kMlpScale * softplus(o) - tg[j];
+        loss += r * r;
+        dout[j] = r * inv_n * kMlpScale * sig;
+      }
+    }
+    for (int k0 = 0; k0 < kMlpH; k0 += 8) {
+      uint4 q1 = make_uint4(0u, 0u, 0u, 0u), q2 = q1;
+      if (live) {
+        q1 = *reinterpret_cast<const uint4*>(h1g + row * kMlpH + k0);
+        q2 = *reinterpret_cast<const uint4*>(h2g + row * kMlpH + k0);
+      }
+      const __nv_bfloat16* a1 = reinterpret_cast<const __nv_bfloat16*>(&q1);
+      const __nv_bfloat16* a2 = reinterpret_cast<const __nv_bfloat16*>(&q2);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int k = k0 + i;
+        const float h2v = __bfloat162float(a2[i]);
+        const float g = dout[0] * S.w3[k] + dout[1] * S.w3[kMlpH + k];
+        const float d2 = h2v > 0.f ? g : 0.f;
+        st_split(S.ad2[0], S.ad2[1], kmaj(t, k, kMlpH), d2);
+        st_split(S.ast[0], S.ast[1], kmaj(k, t, kBk), d2);
+        *reinterpret_cast<__nv_bfloat16*>(S.bst + kmaj(k, t, kBk)) = a1[i];
+        *reinterpret_cast<__nv_bfloat16*>(S.a3 + kmaj(k, t, kBk)) = a2[i];
+      }
+    }
+    {
+      uint4 qx[2] = {make_uint4(0u, 0u, 0u, 0u), make_uint4(0u, 0u, 0u, 0u)};
+      if (live) {
+        qx[0] = *reinterpret_cast<const uint4*>(x16 + row * kMlpK1);
+        qx[1] = *reinterpret_cast<const uint4*>(x16 + row * kMlpK1 + 8);
+      }
+      const __nv_bfloat16* xv = reinterpret_cast<const __nv_bfloat16*>(qx);
+#pragma unroll
+      for (int c = 0; c < kMlpK1; ++c) *reinterpret_cast<__nv_bfloat16*>(S.bst + kmaj(80 + c, t, kBk)) = xv[c];
+      // rows j and 2 + j of [DO_hi; DO_lo]
+#pragma unroll
+      for (int j = 0; j < kMlpOut; ++j) st_split(S.b3 + kmaj(j, 0, kBk), S.b3 + kmaj(2 + j, 0, kBk), kmaj(0, t, kBk),
+                                                 dout[j]);
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // ---- (1) G1 = D2 W2 (hi and lo parts) and (3) the layer-3 gradients
+    if (t == 0) {
+      const uint32_t id64 = idesc_bf16(128, 64), id16 = idesc_bf16(128, 16);
+      const uint32_t w2 = smem_u32(S.w2t);
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int kk = 0; kk < kMlpH / 16; ++kk)
+          mma_bf16(tm + c_g1, sdesc(smem_u32(S.ad2[h]) + 256 * kk, 128, kMlpH * 16), sdesc(w2 + 256 * kk, 128, kMlpH * 16),
+                   id64, (h | kk) != 0);
+#pragma unroll
+      for (int kk = 0; kk < kBk / 16; ++kk)
+        mma_bf16(tm + c_3, sdesc(smem_u32(S.a3) + 256 * kk, 128, kBk * 16), sdesc(smem_u32(S.b3) + 256 * kk, 128, kBk * 16),
+                 id16, !(first && kk == 0));
+      mma_commit(&S.mbar);
+    }
+    mpend = true;
+    if ((bad = wait_mma())) break;
+    // ---- hidden-1 deltas from G1 (this thread's lane), into rows 64..127 of [D2^T; D1^T]
+    {
+      uint4 q1[8];
+      if (live)
+#pragma unroll
+        for (int j = 0; j < 8; ++j) q1[j] = *reinterpret_cast<const uint4*>(h1g + row * kMlpH + 8 * j);
+      else
+#pragma unroll
+        for (int j = 0; j < 8; ++j) q1[j] = make_uint4(0u, 0u, 0u, 0u);
+      const __nv_bfloat16* a1 = reinterpret_cast<const __nv_bfloat16*>(q1);
+#pragma unroll
+      for (int c0 = 0; c0 < kMlpH; c0 += 16) {
+        float g[16];
+        tmem_ld16(tl + c_g1 + (uint32_t)c0, g);
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int k = c0 + i;
+          const float d1 = __bfloat162float(a1[k]) > 0.f ? g[i] : 0.f;
+          st_split(S.ast[0], S.ast[1], kmaj(64 + k, t, kBk), d1);
+        }
+      }
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    // ---- (2) the layer-1 and layer-2 weight gradients, accumulated over tiles
+    if (t == 0) {
+      const uint32_t id96 = idesc_bf16(128, 96);
+      const uint32_t bst = smem_u32(S.bst);
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int kk = 0; kk < kBk / 16; ++kk)
+          mma_bf16(tm + c_st, sdesc(smem_u32(S.ast[h]) + 256 * kk, 128, kBk * 16), sdesc(bst + 256 * kk, 128, kBk * 16),
+                   id96, !(first && h == 0 && kk == 0));
+      mma_commit(&S.mbar);
+    }
+    mpend = true;
+    if ((bad = wait_mma())) break;
+    first = false;
+  }
+  if (bad && t == 0) atomicExch(err, 1);
+  // an MMA group still in flight (the loop left early) completes before the
+  // shared memory and TMEM it uses are released
+  if (mpend && t == 0) mbar_wait(&S.mbar, ph);
+  // ---- this CTA's partial sums (a CTA without tiles writes zeros)
+  float* out = part + (long long)blockIdx.x * (kMlpParams + 1);
+  if (!bad) {
+    float v[16];
+    if (t < kMlpH) {
+      // row t: dW2[t][0..63] and db2[t] (column 64)
+      for (int c0 = 0; c0 < 80; c0 += 16) {
+        if (!first) tmem_ld16(tl + c_st + (uint32_t)c0, v);
+        else for (int i = 0; i < 16; ++i) v[i] = 0.f;
+        for (int i = 0; i < 16; ++i) {
+          const int k = c0 + i;
+          if (k < kMlpH) out[kMlpOffW2 + t * kMlpH + k] = v[i];
+          else if (k == kMlpH) out[kMlpOffB2 + t] = v[i];
+        }
+      }
+    } else {
+      // row 64 + r: dW1[r][0..11] and db1[r] (columns 80..92)
+      const int r = t - kMlpH;
+      if (!first) tmem_ld16(tl + c_st + 80u, v);
+      else for (int i = 0; i < 16; ++i) v[i] = 0.f;
+      for (int c = 0; c < kMlpIn; ++c) out[kMlpOffW1 + r * kMlpIn + c] = v[c];
+      out[kMlpOffB1 + r] = v[kMlpOne];
+    }
+    // layer 3: row k < 64 -> dW3[j][k] = hi + lo columns, row 64 -> db3[j]
+    if (!first) tmem_ld16(tl + c_3, v);
+    else for (int i = 0; i < 16; ++i) v[i] = 0.f;
+    if (t < kMlpH) {
+      for (int j = 0; j < kMlpOut; ++j) out[kMlpOffW3 + j * kMlpH + t] = v[j] + v[2 + j];
+    } else if (t == kMlpH) {
+      for (int j = 0; j < kMlpOut; ++j) out[kMlpOffB3 + j] = v[j] + v[2 + j];
+    }
+  }
+  // the loss sum of the CTA's points (fixed order)
+  for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+  if ((t & 31) == 0) S.red[t >> 5][0] = loss;
+  tc_fence_before();
+  __syncthreads();
+  if (t == 0) out[kMlpParams] = (S.red[0][0] + S.red[1][0]) + (S.red[2][0] + S.red[3][0]);
+  if (t < 32) {
+    tc_fence_after();
+    tmem_dealloc(tm, 256);
+  }
+}
+
 // grad[p] = sum over CTAs of part[b][p] in CTA order; loss[0] likewise
 __global__ void k_mlp_reduce(const float* __restrict__ part, int nblk, float* __restrict__ grad,
                              float* __restrict__ loss) {
@@ -501,14 +754,27 @@ __global__ void k_mlp_reduce(const float* __restrict__ part, int nblk, float* __
 long long mlp_partials(long long n) { return ((n + kMlpTile - 1) / kMlpTile) * (kMlpParams + 1); }
 
 void mlp_backward(const __nv_bfloat16* x16, const float2* y, long long n, const MlpDev* dev, const MlpBatch& batch,
-                  float* part, float* grad, float* loss, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
-    attr = true;
+                  float* part, float* grad, float* loss, int* err, bool tensor_cores, cudaStream_t s) {
+  const long long ntiles = (n + kMlpTile - 1) / kMlpTile;
+  int nblk;
+  if (tensor_cores) {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_mlp_bwd_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMlpBwdSmemBytes);
+      attr = true;
+    }
+    // persistent: one CTA per SM (the operand tiles take 165 KB of shared memory)
+    nblk = (int)(ntiles < sm_count() ? ntiles : sm_count());
+    k_mlp_bwd_tc<<<nblk, kMlpTile, kMlpBwdSmemBytes, s>>>(x16, y, n, dev, batch.h1, batch.h2, batch.o, part, err);
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(k_mlp_bwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kBwdSmem);
+      attr = true;
+    }
+    nblk = (int)ntiles;
+    k_mlp_bwd<<<nblk, kMlpTile, kBwdSmem, s>>>(x16, y, n, dev, batch.h1, batch.h2, batch.o, part);
   }
-  const int nblk = (int)((n + kMlpTile - 1) / kMlpTile);
-  k_mlp_bwd<<<nblk, kMlpTile, kBwdSmem, s>>>(x16, y, n, dev, batch.h1, batch.h2, batch.o, part);
   k_mlp_reduce<<<(kMlpParams + 1 + 255) / 256, 256, 0, s>>>(part, nblk, grad, loss);
 }
 

@@ -1,7 +1,8 @@
 // Learned subgrid closure (closure.cu): a 12 -> 64 -> 64 -> 2 MLP with BF16
-// weights and FP32 accumulation.  Inference runs on the 5th-generation
-// tensor cores (tcgen05.mma, accumulators in TMEM); the backward pass and
-// Adam run on the CUDA cores.
+// weights and FP32 accumulation.  Inference and the backward pass's
+// contractions run on the 5th-generation tensor cores (tcgen05.mma,
+// accumulators in TMEM); the delta nonlinearities and Adam run on the CUDA
+// cores.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -60,9 +61,11 @@ int mlp_forward(const __nv_bfloat16* x16, long long n, const MlpDev* dev, float2
 // Gradient of L = mean over points and both outputs of (C - y)^2, written
 // to grad (kMlpParams floats), and the loss sum into loss[0]; part holds
 // mlp_partials(n) floats.
+// tensor_cores: the three contractions as tcgen05 MMAs (k_mlp_bwd_tc; err
+// is set on a wait timeout), else the CUDA-core kernel (k_mlp_bwd).
 long long mlp_partials(long long n);
 void mlp_backward(const __nv_bfloat16* x16, const float2* y, long long n, const MlpDev* dev, const MlpBatch& batch,
-                  float* part, float* grad, float* loss, cudaStream_t s);
+                  float* part, float* grad, float* loss, int* err, bool tensor_cores, cudaStream_t s);
 // One Adam step on params (m, v moments), then the BF16 repack.
 void mlp_adam(float* params, float* m, float* v, const float* grad, int step, float lr, MlpDev* dev,
               cudaStream_t s);

@@ -203,6 +203,7 @@ struct Ctx {
   MlpDev* mlp_dev = nullptr;
   int* mlp_err = nullptr;
   int mlp_step = 0;
+  int mlp_tc_bwd = 1;  // backward contractions on the tensor cores (else CUDA cores)
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t graph_stream = nullptr;
   int graph_stale = 1;
@@ -1401,13 +1402,20 @@ int sam_gpu_mlp_grad(const float* feat, const float* target, long long n, float*
   CK(cudaMemcpyAsync(w.y, target, sizeof(float2) * (size_t)n, cudaMemcpyHostToDevice, c.stream));
   if (mlp_forward(x16, n, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream) < 0)
     return fail(SAM_GPU_ECUDA, "closure network: no TMA tensor map");
-  mlp_backward(x16, w.y, n, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss, c.stream);
+  mlp_backward(x16, w.y, n, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss, c.mlp_err, c.mlp_tc_bwd != 0, c.stream);
   CK(cudaMemcpyAsync(grad, c.mlp_g, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost, c.stream));
   float ls = 0.f;
   CK(cudaMemcpyAsync(&ls, c.mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, c.stream));
   rc = mlp_check_err(c);
   if (loss) *loss = ls / (2.0f * (float)n);
   return rc;
+}
+
+int sam_gpu_mlp_set_backward(int tensor_cores) {
+  NEED_CTX();
+  if (tensor_cores != 0 && tensor_cores != 1) return fail(SAM_GPU_EINVAL, "mlp_set_backward: 0 or 1");
+  c.mlp_tc_bwd = tensor_cores;
+  return 0;
 }
 
 int sam_gpu_mlp_train(const float* feat, const float* target, long long n, int steps, int batch, float lr,
@@ -1432,7 +1440,8 @@ int sam_gpu_mlp_train(const float* feat, const float* target, long long n, int s
     const long long off = (s % nchunks) * nb;
     if (mlp_forward(x16 + off * kMlpK1, nb, c.mlp_dev, w.coef, &w.b, c.mlp_err, c.stream) < 0)
       return fail(SAM_GPU_ECUDA, "closure network: no TMA tensor map");
-    mlp_backward(x16 + off * kMlpK1, y_all + off, nb, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss + 0, c.stream);
+    mlp_backward(x16 + off * kMlpK1, y_all + off, nb, c.mlp_dev, w.b, w.part, c.mlp_g, c.mlp_loss + 0, c.mlp_err,
+                 c.mlp_tc_bwd != 0, c.stream);
     mlp_adam(c.mlp_p, c.mlp_m, c.mlp_v, c.mlp_g, ++c.mlp_step, lr, c.mlp_dev, c.stream);
     if (loss_hist) CK(cudaMemcpyAsync(&hist[s], c.mlp_loss, sizeof(float), cudaMemcpyDeviceToHost, c.stream));
   }

@@ -32,6 +32,7 @@ EXPORTS = [
     "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_set_fft_schedule", "sam_gpu_fft_schedule", "sam_gpu_planes",
     "sam_gpu_set_forcing", "sam_gpu_set_les", "sam_gpu_les_coef",
     "sam_gpu_mlp_set", "sam_gpu_mlp_get", "sam_gpu_mlp_forward", "sam_gpu_mlp_grad", "sam_gpu_mlp_train",
+    "sam_gpu_mlp_set_backward",
     "sam_gpu_mma_selftest", "sam_gpu_box_filter", "sam_gpu_closure_inputs",
     "sam_gpu_ensemble_create", "sam_gpu_ensemble_select", "sam_gpu_ensemble_step", "sam_gpu_ensemble_destroy",
 ]
@@ -123,6 +124,7 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_mlp_forward.argtypes = [P, C.c_longlong, P]
     lib.sam_gpu_mlp_grad.argtypes = [P, P, C.c_longlong, P, P]
     lib.sam_gpu_mlp_train.argtypes = [P, P, C.c_longlong, C.c_int, C.c_int, C.c_float, P]
+    lib.sam_gpu_mlp_set_backward.argtypes = [C.c_int]
     lib.sam_gpu_mma_selftest.argtypes = [P, P, P]
     lib.sam_gpu_box_filter.argtypes = [C.c_int, P]
     lib.sam_gpu_ensemble_create.argtypes = [P, C.c_int]
@@ -415,6 +417,10 @@ class SamGpu:
                                                     len(f), g.ctypes.data_as(C.c_void_p), C.byref(loss)),
                     "mlp_grad")
         return g, loss.value
+
+    def mlp_set_backward(self, tensor_cores=True):
+        """Backward pass on the tensor cores (default) or on the CUDA cores."""
+        self._check(load_library().sam_gpu_mlp_set_backward(1 if tensor_cores else 0), "mlp_set_backward")
 
     def mlp_train(self, features, target, steps, batch=8192, lr=1e-3):
         f = self._f32(features).reshape(-1, MLP_FEATURES)

@@ -71,6 +71,31 @@ def test_gradient_matches_oracle(gpu_lib, ctx):
         assert np.linalg.norm(g[lo:hi] - gr[lo:hi]) <= 5e-3 * np.linalg.norm(gr[lo:hi]), (lo, hi)
 
 
+@pytest.mark.parametrize("npts", [2125, 200037])
+def test_backward_tensor_cores_match_cuda_cores(gpu_lib, ctx, npts):
+    """The tcgen05 backward pass (deltas split into two BF16 parts, weight
+    gradients accumulated in TMEM over each persistent CTA's tiles) against
+    the CUDA-core kernel with FP32 deltas, on one tile per CTA and on many."""
+    rng = np.random.default_rng(5)
+    p = CL.init_params(6)
+    p[CL.OFF_W3:CL.OFF_B3] *= 10
+    p[CL.OFF_B1:CL.OFF_W2] = 0.1 * rng.standard_normal(CL.N_H)
+    ctx.mlp_set(p)
+    x = rng.standard_normal((npts, CL.N_IN)).astype(np.float32)
+    y = (0.02 * np.abs(rng.standard_normal((npts, 2)))).astype(np.float32)
+    ctx.mlp_set_backward(False)
+    g0, l0 = ctx.mlp_grad(x, y)
+    ctx.mlp_set_backward(True)
+    g1, l1 = ctx.mlp_grad(x, y)
+    assert abs(l1 - l0) <= 1e-6 * l0
+    for lo, hi in ((CL.OFF_W1, CL.OFF_B1), (CL.OFF_B1, CL.OFF_W2), (CL.OFF_W2, CL.OFF_B2), (CL.OFF_B2, CL.OFF_W3),
+                   (CL.OFF_W3, CL.OFF_B3), (CL.OFF_B3, CL.N_PARAMS)):
+        assert np.linalg.norm(g1[lo:hi] - g0[lo:hi]) <= 1e-4 * np.linalg.norm(g0[lo:hi]), (lo, hi)
+    # and a second call gives the same gradient (fixed reduction order)
+    g2, _ = ctx.mlp_grad(x, y)
+    assert np.array_equal(g1, g2)
+
+
 def test_adam_training_fits_a_smooth_target(gpu_lib, ctx):
     """A coefficient that depends on two of the inputs: 300 Adam steps of
     batch 1024 cut the loss by more than 10x and generalise to new points."""
