@@ -291,7 +291,7 @@ def les_cfg(precision):
                 lapse=1.0, precision=precision)
 
 
-def les_forms(stream, K, W, t_spin=1.5, t_win=1.0, n_win=10):
+def les_forms(stream, K, W, t_spin=1.5, t_win=2.0, n_win=20):
     """The LES workload in three forms, each spun up on its own from the same
     random start and OU forcing: the FP64 drop-in with dm.f's dynamic
     closure (the judge), the FP32 bulk form with the learned closure, and the
@@ -355,6 +355,8 @@ def les_forms(stream, K, W, t_spin=1.5, t_win=1.0, n_win=10):
     out["spectrum_max_rel_diff_k_le_kmax_half"] = float(np.abs(avg["fp32_learned"][ks] / avg["fp64_dm"][ks] - 1).max())
     out["spectrum_max_rel_diff_k_le_kmax_half_no_model"] = float(
         np.abs(avg["fp32_none"][ks] / avg["fp64_dm"][ks] - 1).max())
+    out["spectrum_rel_diff_per_shell_k_le_kmax_half"] = {
+        k: [round(float(v), 4) for v in (avg[k][ks] / avg["fp64_dm"][ks] - 1)] for k in ("fp32_learned", "fp32_none")}
     out["spectrum_max_rel_diff_all_shells"] = {
         k: float(np.abs(avg[k][1:kmax + 1] / avg["fp64_dm"][1:kmax + 1] - 1).max()) for k in ("fp32_learned",
                                                                                           "fp32_none")}
