@@ -303,6 +303,14 @@ module sam_gpu
     integer(c_int) function sam_gpu_ensemble_destroy() bind(C, name="sam_gpu_ensemble_destroy")
       import :: c_int
     end function
+    integer(c_int) function sam_gpu_ensemble_set_persistent(ctas_per_sm) bind(C, name="sam_gpu_ensemble_set_persistent")
+      import :: c_int
+      integer(c_int), value :: ctas_per_sm
+    end function
+    integer(c_int) function sam_gpu_ensemble_persistent_members(n) bind(C, name="sam_gpu_ensemble_persistent_members")
+      import :: c_int
+      integer(c_int), intent(out) :: n
+    end function
 
     ! ---- restart files: write_field.f:1, read_field.f:1, write_header.f:1, read_header.f:1
     integer(c_int) function sam_gpu_write_field(fname) bind(C, name="sam_gpu_write_field")

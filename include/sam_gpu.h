@@ -313,6 +313,16 @@ int sam_gpu_ensemble_create(const sam_gpu_config* cfgs, int n);
 int sam_gpu_ensemble_select(int m);
 int sam_gpu_ensemble_step(int nsteps);
 int sam_gpu_ensemble_destroy(void);
+/* Members in the FP32 bulk form without a subgrid closure whose transform
+ * lengths are 32, 64, 96 or 128 advance together in one persistent launch per
+ * RK3 stage (a ticket-ordered queue of (member, pass, tile) work items with
+ * bounded dependency waits; no counterpart in the reference, which has no
+ * ensembles), with at most ctas_per_sm (1 or 2, the default) CTAs per SM;
+ * 0 gives every member its own branch of the step graph instead.  The same
+ * results either way. */
+int sam_gpu_ensemble_set_persistent(int ctas_per_sm);
+/* number of members the persistent launch took at the last graph build */
+int sam_gpu_ensemble_persistent_members(int* n);
 
 /* ---- restart files of the resident state ---- */
 /* write_field.f:1 / read_field.f:1  vel.NNNNNN: Lu*Nx_min records of

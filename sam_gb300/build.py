@@ -16,7 +16,7 @@ OBJ_DIR = os.path.join(HERE, "_build")
 LIB_DIR = os.path.join(HERE, "_lib")
 LIB_PATH = os.path.join(LIB_DIR, "libsam_gpu.so")
 SOURCES = ["passes.cu", "passes_f32.cu", "passes_dd_zinv.cu", "passes_dd_yinv.cu", "passes_dd_x.cu", "passes_dd_yfwd.cu",
-           "passes_dd_zfwd.cu", "fields.cu", "diag.cu", "les.cu", "noalloc.cu", "planes.cu", "closure.cu", "sam_gpu.cu"]
+           "passes_dd_zfwd.cu", "passes_ens.cu", "fields.cu", "diag.cu", "les.cu", "noalloc.cu", "planes.cu", "closure.cu", "sam_gpu.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2"]
 

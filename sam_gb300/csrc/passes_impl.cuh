@@ -104,20 +104,28 @@ __device__ __forceinline__ void store_tile_rows(C* __restrict__ dst, long long o
   }
 }
 
-template <typename C> struct RowLoad {
+// Loads of data that another CTA of the same launch wrote (the persistent
+// ensemble stage kernel, COH = true) go to L2 (ld.global.cg), never to a
+// possibly stale L1 line; the per-pass kernels (COH = false) load as usual.
+template <bool COH, typename V> __device__ __forceinline__ V ldc(const V* p) {
+  if constexpr (COH) return __ldcg(p);
+  else return *p;
+}
+
+template <typename C, bool COH = false> struct RowLoad {
   const C* __restrict__ row;
-  __device__ __forceinline__ C operator()(int idx) const { return row[idx]; }
+  __device__ __forceinline__ C operator()(int idx) const { return ldc<COH>(row + idx); }
 };
 
 // First-stage loader of a row of stored modes 0..k, then -k..-1, padded to
 // the transform length: idx <= lo from row[idx], idx >= hi from
 // row[idx - gap], the band between as zero.
-template <typename C> struct BandRowLoad {
+template <typename C, bool COH = false> struct BandRowLoad {
   const C* __restrict__ row;
   int lo, hi, gap;
   __device__ __forceinline__ C operator()(int idx) const {
-    if (idx <= lo) return row[idx];
-    if (idx >= hi) return row[idx - gap];
+    if (idx <= lo) return ldc<COH>(row + idx);
+    if (idx >= hi) return ldc<COH>(row + idx - gap);
     return mk<C>((decltype(C::x))0, (decltype(C::x))0);
   }
 };
@@ -153,8 +161,8 @@ template <typename C> struct DeriveLoad {
 // --------------------------------------------------------------- z inverse
 // Tile: field n, kx index i, ky rows j0 .. j0+TY-1.  Input rows hold Nz_min
 // modes; output A(n, z, kx, ky) with ky fastest.
-template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value) k_z_inv(ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+template <typename T, int PATH, bool COH = false>
+__device__ __forceinline__ void z_inv_body(const ZInvArgs<T>& a, const FftPlan* __restrict__ gpl, int bid) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -165,7 +173,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   const int nz = a.g.nz, mz = a.g.mz, km = a.g.kz, my = a.g.my;
   const int ld = a.ld;
   const int nty = (my + a.ty - 1) / a.ty;
-  int b = blockIdx.x;
+  int b = bid;
   const int jt = b % nty; b /= nty;
   const int i = b % a.g.mx; b /= a.g.mx;
   const int n = b;
@@ -177,8 +185,9 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   if (!a.derive || n < a.g.lu) {
     // the first stage reads the stored modes straight from the row, the
     // truncated band as zero (no shared-memory staging)
-    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl,
-                             [&](int L) { return BandRowLoad<C>{src + (long long)L * a.in_ky, km, nz - km, nz - mz}; });
+    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl, [&](int L) {
+      return BandRowLoad<C, COH>{src + (long long)L * a.in_ky, km, nz - km, nz - mz};
+    });
   } else {
     // gradient field m of the subgrid stress: S_ab = (i/2)(k_b u_a + k_a u_b)
     // (i k_a u_a when a = b) for the six velocity products in rhs.f's order,
@@ -235,13 +244,18 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value
   C* dst = a.out + (long long)n * a.out_n + (long long)i * a.out_kx + j0;
   store_tile_rows(dst, a.out_z, s_ln, ld, a.ty, nl, nz, [](int z) { return z; });
 }
+template <typename T, int PATH>
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZInv, PATH>::value)
+    k_z_inv(const __grid_constant__ ZInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+  z_inv_body<T, PATH>(a, gpl, blockIdx.x);
+}
 
 // --------------------------------------------------------------- y inverse
 // Tile: field n, plane z, kx columns i0 .. i0+TX-1.  Input rows (one per kx)
 // hold either Ny_min compact modes (zero band inserted here, as
 // x2z_decomp.f:111-124 does) or Ny values with the band already present.
-template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value) k_y_inv(YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+template <typename T, int PATH, bool COH = false>
+__device__ __forceinline__ void y_inv_body(const YInvArgs<T>& a, const FftPlan* __restrict__ gpl, int bid) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -252,7 +266,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
   const int ny = a.g.ny, my = a.g.my, km = a.g.ky, mx = a.g.mx;
   const int ld = a.ld;
   const int ntx = (mx + a.tx - 1) / a.tx;
-  int b = blockIdx.x;
+  int b = bid;
   const int it = b % ntx; b /= ntx;
   const int z = b % a.g.nz; b /= a.g.nz;
   const int n = b;
@@ -264,13 +278,19 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value
   // the first stage reads the rows straight from memory: all Ny values
   // (in_full) or the stored modes with the truncated band as zero
   if (a.in_full)
-    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl, [&](int L) { return RowLoad<C>{src + (long long)L * a.in_kx}; });
+    fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl,
+                             [&](int L) { return RowLoad<C, COH>{src + (long long)L * a.in_kx}; });
   else
     fft_lines_from<+1, PATH>(s_ln, ld, nl, s_tw, pl,
-                             [&](int L) { return BandRowLoad<C>{src + (long long)L * a.in_kx, km, ny - km, ny - my}; });
+                             [&](int L) { return BandRowLoad<C, COH>{src + (long long)L * a.in_kx, km, ny - km, ny - my}; });
   __syncthreads();
   C* dst = a.out + (long long)n * a.out_n + (long long)z * a.out_z + i0;
   store_tile_rows(dst, a.out_y, s_ln, ld, a.tx, nl, ny, [](int y) { return y; });
+}
+template <typename T, int PATH>
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYInv, PATH>::value)
+    k_y_inv(const __grid_constant__ YInvArgs<T> a, const FftPlan* __restrict__ gpl) {
+  y_inv_body<T, PATH>(a, gpl, blockIdx.x);
 }
 
 // Two adjacent complex values in one store (one 16-byte store in FP32, two in
@@ -455,9 +475,8 @@ __device__ __forceinline__ void product_pair(int m, int& a, int& b) {
   }
 }
 
-template <typename T, int PATH>
-__global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBlocks<T, kPassX, PATH>::value)
-    k_x_pass(XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
+template <typename T, int PATH, bool COH = false>
+__device__ __forceinline__ void x_pass_body(const XPassArgs<T>& a, const FftPlan* __restrict__ gpl, int bid) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -473,8 +492,8 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
   // before the first product is formed)
   double* s_red = reinterpret_cast<double*>(s_pr);
   const int nyt = (ny + Y - 1) / Y;
-  const int yt = blockIdx.x % nyt;
-  const int z = blockIdx.x / nyt;
+  const int yt = bid % nyt;
+  const int z = bid / nyt;
   const int y0 = yt * Y;
   const int yv = min(Y, ny - y0);  // valid rows in the tile
   load_twiddles<T>(s_tw, a.tw, tw_load<PATH>(pl));
@@ -509,8 +528,8 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
                 const int f = (int)fdiv(L, a.fd_yp), c = L - f * yp;
                 const int ya = y0 + 2 * c;
                 const C* src = src0 + (long long)f * a.in_n + (long long)ya * a.in_y;
-                if (ya < ny) X[u] = src[0];
-                if (ya + 1 < ny) Yv[u] = src[a.in_y];
+                if (ya < ny) X[u] = ldc<COH>(src);
+                if (ya + 1 < ny) Yv[u] = ldc<COH>(src + a.in_y);
               }
             }
 #pragma unroll
@@ -538,8 +557,8 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
             const int ya = y0 + 2 * c, yb = ya + 1;
             const C* src = a.in + (long long)f * a.in_n + (long long)z * a.in_z;
             Pair q;
-            q.x = ya < ny ? src[(long long)ya * a.in_y + kx] : mk<C>((T)0, (T)0);
-            q.y = yb < ny ? src[(long long)yb * a.in_y + kx] : mk<C>((T)0, (T)0);
+            q.x = ya < ny ? ldc<COH>(src + (long long)ya * a.in_y + kx) : mk<C>((T)0, (T)0);
+            q.y = yb < ny ? ldc<COH>(src + (long long)yb * a.in_y + kx) : mk<C>((T)0, (T)0);
             return q;
           },
           [&](int e, Pair q) {
@@ -744,7 +763,7 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
           t1 += s_red[k * 4 + 0]; t2 += s_red[k * 4 + 1];
           tm = fmax(tm, s_red[k * 4 + 2]); tb += s_red[k * 4 + 3];
         }
-        double* dst = a.partials + ((long long)blockIdx.x * a.g.lu + f) * 4;
+        double* dst = a.partials + ((long long)bid * a.g.lu + f) * 4;
         dst[0] = t1; dst[1] = t2; dst[2] = tm; dst[3] = tb;
       }
       __syncthreads();
@@ -905,12 +924,17 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
     __syncthreads();
   }
 }
+template <typename T, int PATH>
+__global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBlocks<T, kPassX, PATH>::value)
+    k_x_pass(const __grid_constant__ XPassArgs<T> a, const FftPlan* __restrict__ gpl) {
+  x_pass_body<T, PATH>(a, gpl, blockIdx.x);
+}
 
 // --------------------------------------------------------------- y forward
 // Tile: field m, kx column i, planes z0 .. z0+TZ-1.  Output D(m, kx, ky, z)
 // keeps |ky| <= ky_max (xy_trans_f.f:45-52).
-template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value) k_y_fwd(YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+template <typename T, int PATH, bool COH = false>
+__device__ __forceinline__ void y_fwd_body(const YFwdArgs<T>& a, const FftPlan* __restrict__ gpl, int bid) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -921,7 +945,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
   const int ny = a.g.ny, my = a.g.my, km = a.g.ky, nz = a.g.nz;
   const int ld = a.ld;
   const int ntz = (nz + a.tz - 1) / a.tz;
-  int b = blockIdx.x;
+  int b = bid;
   const int zt = b % ntz; b /= ntz;
   const int i = b % a.g.mx; b /= a.g.mx;
   const int m = b;
@@ -933,10 +957,15 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value
   // the first stage reads its inputs straight from the rows of C (no
   // shared-memory staging); the rows are contiguous in y
   fft_lines_from<-1, PATH>(s_ln, ld, nl, s_tw, pl,
-                           [&](int L) { return RowLoad<C>{src + (long long)L * a.in_z}; });
+                           [&](int L) { return RowLoad<C, COH>{src + (long long)L * a.in_z}; });
   __syncthreads();
   C* dst = a.out + (long long)m * a.out_n + (long long)i * a.out_kx + z0;
   store_tile_rows(dst, a.out_ky, s_ln, ld, a.tz, nl, my, [&](int j) { return kpos(j, km, my, ny); });
+}
+template <typename T, int PATH>
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassYFwd, PATH>::value)
+    k_y_fwd(const __grid_constant__ YFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+  y_fwd_body<T, PATH>(a, gpl, blockIdx.x);
 }
 
 __device__ __forceinline__ double wexp(double x) { return exp(x); }
@@ -1097,8 +1126,8 @@ __device__ __forceinline__ void epi_mode(const ZFwdArgs<T>& a, const cx_t<T>* ln
 //   mode 0: write the truncated modes back in place (z_trans_f),
 //   mode 1: rhs epilogue (rhs.f:108-142) into r with u_sav from memory,
 //   mode 2: full stage epilogue: rhs, then sam.f:210-221 and 293-314.
-template <typename T, int PATH>
-__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value) k_z_fwd(ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+template <typename T, int PATH, bool COH = false>
+__device__ __forceinline__ void z_fwd_body(const ZFwdArgs<T>& a, const FftPlan* __restrict__ gpl, int bid) {
   using C = cx_t<T>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ FftPlan pl;
@@ -1110,8 +1139,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
   const int nz = g.nz, mz = g.mz, km = g.kz, my = g.my;
   const int ld = a.ld, nf = a.nf;
   const int nty = (my + a.ty - 1) / a.ty;
-  const int jt = blockIdx.x % nty;
-  const int i = blockIdx.x / nty;
+  const int jt = bid % nty;
+  const int i = bid / nty;
   const int j0 = jt * a.ty;
   const int nl = min(a.ty, my - j0);
   load_twiddles<T>(s_tw, a.tw, tw_load<PATH>(pl));
@@ -1120,7 +1149,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
   __syncthreads();
   fft_lines_from<-1, PATH>(s_ln, ld, nf * nl, s_tw, pl, [&](int L) {
     const int f = L / nl, t = L - f * nl;
-    return RowLoad<C>{a.in + (long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky};
+    return RowLoad<C, COH>{a.in + (long long)f * a.in_n + (long long)i * a.in_kx + (long long)(j0 + t) * a.in_ky};
   });
   __syncthreads();
   const T nz_inv = a.nz_inv;
@@ -1137,7 +1166,7 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
     return;
   }
   double dt = 0.0;
-  if (a.mode == 2) dt = a.state->dt;
+  if (a.mode == 2) dt = ldc<COH>(&a.state->dt);
   // the epilogue constants once per CTA (FP64 arithmetic on one thread)
   __shared__ EpiConst<T> s_cw;
   if (threadIdx.x == 0) s_cw = epi_const<T>(a, dt);
@@ -1167,11 +1196,16 @@ __global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value
     epi_load<double>(a, 0, 0, 0, ind);
     epi_mode<double, T>(a, s_ln + sidx(kpos(0, km, mz, nz)), nl * ld, 0, 0, 0, epi_const<double>(a, dt), ind);
   }
-  if (a.mode == 2 && a.sc.last && blockIdx.x == 0 && threadIdx.x == 0) {
+  if (a.mode == 2 && a.sc.last && bid == 0 && threadIdx.x == 0) {
     // sam.f:318 time = time + dt, once per step (no CTA of this launch reads
     // time, and none writes dt)
     a.state->time = a.state->time + dt;
   }
+}
+template <typename T, int PATH>
+__global__ void __launch_bounds__(kThreads, MinBlocks<T, kPassZFwd, PATH>::value)
+    k_z_fwd(const __grid_constant__ ZFwdArgs<T> a, const FftPlan* __restrict__ gpl) {
+  z_fwd_body<T, PATH>(a, gpl, blockIdx.x);
 }
 
 // ----------------------------------------------------- vel_max completion
@@ -1190,7 +1224,8 @@ __device__ __forceinline__ DF df_add_wsq(DF a, float v, float w) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict__ u, Grid g, double* __restrict__ pv) {
+__device__ __forceinline__ void parseval_body(const cx_t<T>* __restrict__ u, const Grid& g, double* __restrict__ pv,
+                                              int bid, int nblk) {
   __shared__ double red[4][kThreads];
   const long long nm = (long long)g.mx * g.my * g.mz;
   const int plane = g.my * g.mz;
@@ -1198,8 +1233,8 @@ __global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict
     // kx = 0 modes count once, kx > 0 twice (their conjugates): sum w |u|^2
     // with w = 1/2 for kx = 0 and 1 otherwise, then double
     DF acc[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
-    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < nm;
-         m += (long long)gridDim.x * blockDim.x) {
+    for (long long m = bid * (long long)blockDim.x + threadIdx.x; m < nm;
+         m += (long long)nblk * blockDim.x) {
       const float w = m < plane ? 0.5f : 1.0f;
 #pragma unroll
       for (int f = 0; f < 4; ++f)
@@ -1213,8 +1248,8 @@ __global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict
   } else {
     // kx = 0 modes count once, kx > 0 twice (their conjugates): separate sums
     double acc0[4] = {0.0, 0.0, 0.0, 0.0}, acc1[4] = {0.0, 0.0, 0.0, 0.0};
-    for (long long m = blockIdx.x * (long long)blockDim.x + threadIdx.x; m < nm;
-         m += (long long)gridDim.x * blockDim.x) {
+    for (long long m = bid * (long long)blockDim.x + threadIdx.x; m < nm;
+         m += (long long)nblk * blockDim.x) {
       const bool kx0 = m < plane;
 #pragma unroll
       for (int f = 0; f < 4; ++f)
@@ -1235,14 +1270,116 @@ __global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict
       for (int f = 0; f < 4; ++f) red[f][threadIdx.x] += red[f][threadIdx.x + s];
     __syncthreads();
   }
-  if (threadIdx.x < g.lu) pv[(long long)blockIdx.x * g.lu + threadIdx.x] = red[threadIdx.x][0];
-  if (blockIdx.x == 0 && threadIdx.x < g.lu) pv[(long long)gridDim.x * g.lu + threadIdx.x] = (double)u[threadIdx.x * nm].x;
+  if (threadIdx.x < g.lu) pv[(long long)bid * g.lu + threadIdx.x] = red[threadIdx.x][0];
+  if (bid == 0 && threadIdx.x < g.lu) pv[(long long)nblk * g.lu + threadIdx.x] = (double)u[threadIdx.x * nm].x;
+}
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_parseval(const cx_t<T>* __restrict__ u, Grid g, double* __restrict__ pv) {
+  parseval_body<T>(u, g, pv, blockIdx.x, gridDim.x);
 }
 
 template <typename T>
 void launch_parseval(const cx_t<T>* u, const Grid& g, double* pv, cudaStream_t s) {
   k_parseval<T><<<kParsevalBlocks, kThreads, 0, s>>>(u, g, pv);
 }
+// vel_max.f:28-49 on the per-CTA partials written by the x pass (or, in the
+// FP32 and double-float forms, on the wave-space sums and the max keys).
+template <bool COH = false>
+__device__ __forceinline__ void vel_max_finish_body(const double* __restrict__ partials, int nblk, const Grid& g,
+                                                    DevState* st, int i_cfl, double cfl0, double adv_cfl_limit,
+                                                    const double* __restrict__ pv, int npv, int* __restrict__ vmax,
+                                                    int vkind) {
+  __shared__ double red[kThreads];
+  __shared__ double fin[4][4];
+  if (!pv) {
+    // a thread reads whole per-CTA records (lu x 4 doubles, contiguous) of
+    // the CTAs b = t, t + 256, ... into 16 accumulators, then one fixed-order
+    // tree per quantity: deterministic for a given number of CTAs
+    __shared__ double redq[16][kThreads / 2];
+    double v[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = 0.0;
+    const int nq = 4 * g.lu;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) {
+      const double2* rec = reinterpret_cast<const double2*>(partials + (long long)b * nq);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+        if (2 * i < nq) {
+          const double2 x = ldc<COH>(rec + i);
+          v[2 * i] = ((2 * i) % 4 == 2) ? fmax(v[2 * i], x.x) : v[2 * i] + x.x;
+          v[2 * i + 1] = ((2 * i + 1) % 4 == 2) ? fmax(v[2 * i + 1], x.y) : v[2 * i + 1] + x.y;
+        }
+    }
+    // first tree level straight from the registers (threads t and t + 128)
+    const int h = blockDim.x / 2;
+    if (threadIdx.x >= h)
+#pragma unroll
+      for (int i = 0; i < 16; ++i) redq[i][threadIdx.x - h] = v[i];
+    __syncthreads();
+    if (threadIdx.x < h)
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        redq[i][threadIdx.x] = (i % 4 == 2) ? fmax(v[i], redq[i][threadIdx.x]) : v[i] + redq[i][threadIdx.x];
+    __syncthreads();
+    for (int st = h / 2; st > 0; st >>= 1) {
+      if (threadIdx.x < st)
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          redq[i][threadIdx.x] = (i % 4 == 2) ? fmax(redq[i][threadIdx.x], redq[i][threadIdx.x + st])
+                                              : redq[i][threadIdx.x] + redq[i][threadIdx.x + st];
+      __syncthreads();
+    }
+    if (threadIdx.x < nq) fin[threadIdx.x / 4][threadIdx.x % 4] = redq[threadIdx.x][0];
+    __syncthreads();
+  }
+  if (pv) {
+    // sums from wave space: sum u = N u(0,0,0), sum u^2 = N sum w |u|^2
+    for (int f = 0; f < g.lu; ++f) {
+      double v = 0.0;
+      for (int b = threadIdx.x; b < npv; b += blockDim.x) v += ldc<COH>(pv + (long long)b * g.lu + f);
+      red[threadIdx.x] = v;
+      __syncthreads();
+      for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+        if (threadIdx.x < s) red[threadIdx.x] += red[threadIdx.x + s];
+        __syncthreads();
+      }
+      if (threadIdx.x == 0) {
+        const double n = (double)g.nx * (double)g.ny * (double)g.nz;
+        fin[f][0] = ldc<COH>(pv + (long long)npv * g.lu + f) * n;
+        fin[f][1] = red[0] * n;
+        fin[f][2] = vkind ? dd_key_value(ldc<COH>(reinterpret_cast<const unsigned long long*>(vmax) + f))
+                          : (double)__int_as_float(ldc<COH>(vmax + f));
+        fin[f][3] = (double)ldc<COH>(vmax + 8);
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    if (threadIdx.x < kVmaxInts) vmax[threadIdx.x] = 0;  // ready for the next step's maxima
+  }
+  if (threadIdx.x == 0) {
+    const double inv = 1.0 / ((double)g.nx * (double)g.ny * (double)g.nz);
+    int bad = 0;
+    for (int f = 0; f < g.lu; ++f) {
+      st->u_avg[f] = fin[f][0] * inv;
+      st->u_var[f] = fin[f][1] * inv - st->u_avg[f] * st->u_avg[f];
+      st->u_max[f] = fin[f][2];
+      bad |= fin[f][3] != 0.0;
+    }
+    st->energy = 0.5 * (st->u_var[0] + st->u_var[1] + st->u_var[2]);
+    const double cx = st->u_max[0] * g.kx * g.wave_x;
+    const double cy = st->u_max[1] * g.ky * g.wave_y;
+    const double cz = st->u_max[2] * g.kz * g.wave_z;
+    if (i_cfl == 1) {
+      const double cb = fmax(cx, fmax(cy, cz));
+      if (cb > 0.0 && !bad) st->dt = cfl0 * adv_cfl_limit / cb;
+    }
+    st->cfl_x = cx * st->dt;
+    st->cfl_y = cy * st->dt;
+    st->cfl_z = cz * st->dt;
+    if (bad) st->nonfinite = 1;
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 template <typename T>
 void launch_z_inv(const ZInvArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
@@ -1284,14 +1421,31 @@ template <typename T>
 int x_pass_blocks(const XPassArgs<T>& a) {
   return a.g.nz * ((a.g.ny + a.yt - 1) / a.yt);
 }
+// the launch-time fields of the x pass's and the z-forward pass's argument
+// blocks (fast divisors, scales), shared by the launchers and the ensemble
+// stage recorder
 template <typename T>
-void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
+XPassArgs<T> prep_x_pass(const XPassArgs<T>& a0) {
   XPassArgs<T> a = a0;
   a.fd_mx = make_fastdiv(a.g.mx);
   a.fd_yp = make_fastdiv(a.yt / 2);
   a.fd_nx = make_fastdiv(a.g.nx);
   a.fd_y = make_fastdiv(a.yt);
   a.fn = (T)(0.5 / ((double)a.g.nx * (double)a.g.ny));
+  return a;
+}
+template <typename T>
+ZFwdArgs<T> prep_z_fwd(const ZFwdArgs<T>& a0) {
+  ZFwdArgs<T> a = a0;
+  a.fd_t = make_fastdiv(a.ty);
+  a.fd_m = make_fastdiv(a.g.mz);
+  a.nz_inv = (T)(1.0 / (double)a.g.nz);
+  return a;
+}
+
+template <typename T>
+void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
+  const XPassArgs<T> a = prep_x_pass(a0);
   switch (a.g.nx) {
     case 256:
       if (a.sched) k_x_pass<T, 256><<<x_pass_blocks(a), x_threads(sizeof(T), false), smem, s>>>(a, pl);
@@ -1325,10 +1479,7 @@ void launch_y_fwd(const YFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStr
 }
 template <typename T>
 void launch_z_fwd(const ZFwdArgs<T>& a0, const FftPlan* pl, size_t smem, cudaStream_t s) {
-  ZFwdArgs<T> a = a0;
-  a.fd_t = make_fastdiv(a.ty);
-  a.fd_m = make_fastdiv(a.g.mz);
-  a.nz_inv = (T)(1.0 / (double)a.g.nz);
+  const ZFwdArgs<T> a = prep_z_fwd(a0);
   const int nty = (a.g.my + a.ty - 1) / a.ty;
   const int grid = a.g.mx * nty;
   switch (a.g.nz) {

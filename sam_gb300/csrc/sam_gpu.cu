@@ -12,12 +12,14 @@
 #include <algorithm>
 #include <initializer_list>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/sam_gpu.h"
 #include "closure.cuh"
 #include "common.cuh"
 #include "diag.cuh"
+#include "ens.cuh"
 #include "fields.cuh"
 #include "les.cuh"
 #include "passes.cuh"
@@ -207,6 +209,9 @@ struct Ctx {
   cudaGraphExec_t gexec = nullptr;
   cudaStream_t graph_stream = nullptr;
   int graph_stale = 1;
+  // set while an ensemble records this member's stage for its persistent
+  // launch: the FP32 passes are recorded instead of launched
+  EnsRecorder* rec = nullptr;
 };
 
 static Ctx* g_ctx = nullptr;
@@ -218,6 +223,14 @@ struct Ensemble {
   cudaStream_t stream = nullptr;
   cudaGraphExec_t gexec = nullptr;
   std::vector<cudaEvent_t> events;
+  // the persistent stage launches (one per RK3 stage) over the members that
+  // qualify (ens_eligible), with at most `persistent` CTAs per SM; the others
+  // keep their own branches of the graph (0: every member its own branch)
+  int persistent = 2;
+  EnsStageLaunch stages[3];
+  std::vector<EnsRecorder> recs;
+  int* err = nullptr;  // a persistent launch's dependency wait timed out
+  int n_persistent = 0;
 };
 static Ensemble* g_ens = nullptr;
 
@@ -285,7 +298,14 @@ static int run_z_inv(Ctx& c, const void* in, void* out, int nvar, long long in_k
   a.ld = line_ld(c.g.nz);
   a.in_ky = in_ky; a.in_kx = in_kx; a.in_n = in_n;
   a.out_kx = out_kx; a.out_z = out_z; a.out_n = out_n;
-  launch_z_inv<T>(a, c.pz.d, tile_smem(c.pz, a.ty, sizeof(cx_t<T>), a.sched), c.stream);
+  const size_t smem = tile_smem(c.pz, a.ty, sizeof(cx_t<T>), a.sched);
+  if constexpr (std::is_same<T, float>::value) {
+    if (c.rec) {
+      ens_record_z_inv(*c.rec, a, c.pz.d, smem);
+      return 0;
+    }
+  }
+  launch_z_inv<T>(a, c.pz.d, smem, c.stream);
   return 0;
 }
 
@@ -304,7 +324,14 @@ static int run_y_inv(Ctx& c, const void* in, void* out, int nvar, int in_full, l
   a.in_full = in_full;
   a.in_kx = in_kx; a.in_z = in_z; a.in_n = in_n;
   a.out_y = out_y; a.out_z = out_z; a.out_n = out_n;
-  launch_y_inv<T>(a, c.py.d, tile_smem(c.py, a.tx, sizeof(cx_t<T>), a.sched), c.stream);
+  const size_t smem = tile_smem(c.py, a.tx, sizeof(cx_t<T>), a.sched);
+  if constexpr (std::is_same<T, float>::value) {
+    if (c.rec) {
+      ens_record_y_inv(*c.rec, a, c.py.d, smem);
+      return 0;
+    }
+  }
+  launch_y_inv<T>(a, c.py.d, smem, c.stream);
   return 0;
 }
 
@@ -411,6 +438,16 @@ static int run_x_pass(Ctx& c, int in_mode, int out_mode, int nin, const void* in
     a.max_only = (sizeof(T) == 4 || kIsDD<T>) && in_mode == 0 && in == c.S2;
     a.vmax = reinterpret_cast<int*>(c.pv + 4 * ((size_t)kParsevalBlocks + 1));
   }
+  if constexpr (std::is_same<T, float>::value) {
+    if (c.rec) {
+      EnsParsevalArgs pa{(const float2*)c.U, c.g, c.pv};
+      EnsFinishArgs fa{c.partials, nblk, c.g, c.state, c.cfg.i_cfl, c.cfg.cfl0, c.adv_cfl_limit, c.pv,
+                       kParsevalBlocks, a.vmax};
+      if (stats && !a.max_only) return fail(SAM_GPU_EUNSUPPORTED, "ensemble stage: FP64 vel_max partials");
+      ens_record_x_pass(*c.rec, a, c.px.d, x_smem<T>(c, nin, a.yt, a.group), stats, &pa, &fa);
+      return 0;
+    }
+  }
   launch_x_pass<T>(a, c.px.d, x_smem<T>(c, nin, a.yt, a.group), c.stream);
   if (stats) {
     if (a.max_only) launch_parseval<T>((const cx_t<T>*)c.U, c.g, c.pv, c.stream);
@@ -434,7 +471,14 @@ static int run_y_fwd(Ctx& c, const void* in, void* out, int nvar, long long in_k
   a.ld = line_ld(c.g.ny);
   a.in_kx = in_kx; a.in_z = in_z; a.in_n = in_n;
   a.out_ky = out_ky; a.out_kx = out_kx; a.out_n = out_n;
-  launch_y_fwd<T>(a, c.py.d, tile_smem(c.py, a.tz, sizeof(cx_t<T>), a.sched), c.stream);
+  const size_t smem = tile_smem(c.py, a.tz, sizeof(cx_t<T>), a.sched);
+  if constexpr (std::is_same<T, float>::value) {
+    if (c.rec) {
+      ens_record_y_fwd(*c.rec, a, c.py.d, smem);
+      return 0;
+    }
+  }
+  launch_y_fwd<T>(a, c.py.d, smem, c.stream);
   return 0;
 }
 
@@ -471,7 +515,14 @@ static int run_z_fwd(Ctx& c, ZFwdArgs<T>& a) {
     launch_if_tables(c.state, a.sc, c.g, c.ift, c.stream);
     a.ift = c.ift;
   }
-  launch_z_fwd<T>(a, c.pz.d, tile_smem(c.pz, a.ty * a.nf, sizeof(cx_t<T>), a.sched), c.stream);
+  const size_t smem = tile_smem(c.pz, a.ty * a.nf, sizeof(cx_t<T>), a.sched);
+  if constexpr (std::is_same<T, float>::value) {
+    if (c.rec) {
+      ens_record_z_fwd(*c.rec, a, c.pz.d, smem);
+      return 0;
+    }
+  }
+  launch_z_fwd<T>(a, c.pz.d, smem, c.stream);
   return 0;
 }
 
@@ -810,6 +861,8 @@ static void ensemble_free() {
     free_ctx(m);
   }
   if (g_ens->gexec) cudaGraphExecDestroy(g_ens->gexec);
+  for (auto& s : g_ens->stages) ens_free_stage(s);
+  cudaFree(g_ens->err);
   for (cudaEvent_t e : g_ens->events) cudaEventDestroy(e);
   if (g_ens->stream) cudaStreamDestroy(g_ens->stream);
   delete g_ens;
@@ -835,6 +888,23 @@ int sam_gpu_ensemble_create(const sam_gpu_config* cfgs, int n) {
   CK(cudaStreamCreateWithFlags(&g_ens->stream, cudaStreamNonBlocking));
   g_ens->events.resize((size_t)n + 1);
   for (auto& e : g_ens->events) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  CK(cudaMalloc(&g_ens->err, sizeof(int)));
+  CK(cudaMemset(g_ens->err, 0, sizeof(int)));
+  return 0;
+}
+
+int sam_gpu_ensemble_set_persistent(int ctas_per_sm) {
+  if (!g_ens) return fail(SAM_GPU_ENOTINIT, "no ensemble (sam_gpu_ensemble_create)");
+  if (ctas_per_sm < 0 || ctas_per_sm > 2) return fail(SAM_GPU_EINVAL, "ensemble_set_persistent: 0, 1 or 2");
+  g_ens->persistent = ctas_per_sm;
+  if (g_ens->gexec) { cudaGraphExecDestroy(g_ens->gexec); g_ens->gexec = nullptr; }
+  return 0;
+}
+
+int sam_gpu_ensemble_persistent_members(int* n) {
+  if (!g_ens) return fail(SAM_GPU_ENOTINIT, "no ensemble (sam_gpu_ensemble_create)");
+  if (!n) return fail(SAM_GPU_EINVAL, "ensemble_persistent_members: null output");
+  *n = g_ens->n_persistent;
   return 0;
 }
 
@@ -843,6 +913,15 @@ int sam_gpu_ensemble_select(int m) {
   if (m < 0 || m >= (int)g_ens->members.size()) return fail(SAM_GPU_EINVAL, "ensemble member %d out of range", m);
   g_ctx = g_ens->members[(size_t)m];
   return 0;
+}
+
+// Members the persistent stage launch takes: the FP32 bulk form without a
+// subgrid closure, every transform length with a compile-time FFT path of the
+// launch (32, 64, 96, 128), and tiles whose shared memory lets two CTAs share
+// an SM.
+static bool ens_eligible(const Ctx& c) {
+  return c.cfg.precision == 32 && c.les_model == 0 && ens_length_ok(c.g.nx) && ens_length_ok(c.g.ny) &&
+         ens_length_ok(c.g.nz);
 }
 
 static int enqueue_step(Ctx& c) {
@@ -866,16 +945,56 @@ int sam_gpu_ensemble_step(int nsteps) {
   if (stale) {
     if (E.gexec) { cudaGraphExecDestroy(E.gexec); E.gexec = nullptr; }
     for (Ctx* m : E.members) CK(cudaStreamSynchronize(m->stream));
+    // the persistent members (larger first, so that their tiles start early
+    // in each pass level) and their recorded stages
+    std::vector<size_t> pm;
+    std::vector<char> in_pm(E.members.size(), 0);
+    if (E.persistent)
+      for (size_t i = 0; i < E.members.size(); ++i)
+        if (ens_eligible(*E.members[i])) pm.push_back(i);
+    std::stable_sort(pm.begin(), pm.end(), [&](size_t a, size_t b) {
+      const Grid &ga = E.members[a]->g, &gb = E.members[b]->g;
+      return (long long)ga.nx * ga.ny * ga.nz > (long long)gb.nx * gb.ny * gb.nz;
+    });
+    E.recs.assign(pm.size() * 3, EnsRecorder());
+    for (int s = 0; s < 3; ++s) {
+      std::vector<EnsRecorder*> rs;
+      for (size_t k = 0; k < pm.size(); ++k) {
+        Ctx& m = *E.members[pm[k]];
+        if (s + 1 > m.cfg.nrk_max) continue;
+        EnsRecorder* r = &E.recs[k * 3 + (size_t)s];
+        m.rec = r;
+        const int rc = stage_any(m, s + 1);
+        m.rec = nullptr;
+        if (rc) return rc;
+        rs.push_back(r);
+      }
+      const int brc = ens_build_stage(rs, E.stages[s]);
+      if (brc == -2) return fail(SAM_GPU_EUNSUPPORTED, "ensemble stage: a member's tiles do not fit the persistent launch");
+      if (brc) return fail(SAM_GPU_ECUDA, "ensemble stage: device allocation failed");
+    }
+    for (size_t k : pm) in_pm[k] = 1;
+    E.n_persistent = (int)pm.size();
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(E.stream, cudaStreamCaptureModeThreadLocal));
     CK(cudaEventRecord(E.events.back(), E.stream));
     int rc = 0;
     for (size_t i = 0; i < E.members.size() && !rc; ++i) {
+      if (in_pm[i]) continue;
       Ctx& m = *E.members[i];
       cudaStreamWaitEvent(m.stream, E.events.back(), 0);
       rc = enqueue_step(m);
       cudaEventRecord(E.events[i], m.stream);
       cudaStreamWaitEvent(E.stream, E.events[i], 0);
+    }
+    // the persistent members: one launch per stage on the ensemble's stream
+    // (concurrent with the other members' branches), then their forcing
+    if (!rc && !pm.empty()) {
+      for (int s = 0; s < 3; ++s) ens_launch_stage(E.stages[s], E.persistent, E.err, E.stream);
+      for (size_t k : pm) {
+        Ctx& m = *E.members[k];
+        if (m.ou) ou_apply<float>((float2*)m.U, m.g, m.ou, m.state, E.stream);
+      }
     }
     cudaError_t e = cudaStreamEndCapture(E.stream, &graph);
     if (rc) return rc;
@@ -888,6 +1007,12 @@ int sam_gpu_ensemble_step(int nsteps) {
   for (int s = 0; s < nsteps; ++s) CK(cudaGraphLaunch(E.gexec, E.stream));
   for (Ctx* m : E.members) m->nrk = m->cfg.nrk_max;
   CK(cudaStreamSynchronize(E.stream));
+  int herr = 0;
+  CK(cudaMemcpy(&herr, E.err, sizeof(int), cudaMemcpyDeviceToHost));
+  if (herr) {
+    cudaMemset(E.err, 0, sizeof(int));
+    return fail(SAM_GPU_ECUDA, "ensemble stage: a dependency wait of the persistent launch timed out");
+  }
   return check_launch();
 }
 

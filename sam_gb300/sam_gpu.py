@@ -35,6 +35,7 @@ EXPORTS = [
     "sam_gpu_mlp_set_backward",
     "sam_gpu_mma_selftest", "sam_gpu_box_filter", "sam_gpu_closure_inputs",
     "sam_gpu_ensemble_create", "sam_gpu_ensemble_select", "sam_gpu_ensemble_step", "sam_gpu_ensemble_destroy",
+    "sam_gpu_ensemble_set_persistent", "sam_gpu_ensemble_persistent_members",
 ]
 
 MLP_PARAMS = 5122
@@ -130,6 +131,8 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_ensemble_create.argtypes = [P, C.c_int]
     lib.sam_gpu_ensemble_select.argtypes = [C.c_int]
     lib.sam_gpu_ensemble_step.argtypes = [C.c_int]
+    lib.sam_gpu_ensemble_set_persistent.argtypes = [C.c_int]
+    lib.sam_gpu_ensemble_persistent_members.argtypes = [C.POINTER(C.c_int)]
     lib.sam_gpu_closure_inputs.argtypes = [P, P]
     lib.sam_gpu_les_coef.argtypes = [C.POINTER(C.c_double)]
     lib.sam_gpu_planes.argtypes = [P, C.c_int, P, C.c_int, P, C.c_int, P, P, P, P]
@@ -575,6 +578,21 @@ class SamEnsemble:
         if rc != SAM_GPU_OK:
             raise SamGpuError(f"ensemble_step failed ({ERRORS.get(rc, rc)}): "
                               + load_library().sam_gpu_error_string().decode(errors="replace"))
+
+    def set_persistent(self, on=True, ctas_per_sm=2):
+        """Members that qualify advance in one persistent launch per RK3 stage
+        (on; at most ctas_per_sm CTAs per SM) or each in its own branch of the
+        step graph (off)."""
+        rc = load_library().sam_gpu_ensemble_set_persistent(ctas_per_sm if on else 0)
+        if rc != SAM_GPU_OK:
+            raise SamGpuError(f"ensemble_set_persistent failed ({ERRORS.get(rc, rc)})")
+
+    def persistent_members(self):
+        n = C.c_int(0)
+        rc = load_library().sam_gpu_ensemble_persistent_members(C.byref(n))
+        if rc != SAM_GPU_OK:
+            raise SamGpuError(f"ensemble_persistent_members failed ({ERRORS.get(rc, rc)})")
+        return n.value
 
     def close(self):
         if SamGpu._live is self:

@@ -71,3 +71,52 @@ def test_ensemble_member_selection_errors(gpu_lib):
     g.init_taylor_green()
     g.step(1)
     g.close()
+
+
+PERSISTENT = [
+    (dict(nx=32, ny=32, nz=32, i_strat=1, buoy_fac_z=2.0, lapse=1.0, vis=2e-3, i_cfl=1, cfl0=0.5, precision=32),
+     None),
+    (dict(nx=64, ny=32, nz=96, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=1e-3, i_cfl=1, cfl0=0.5, precision=32),
+     None),
+    (dict(nx=128, ny=64, nz=64, vis=1e-3, dt0=0.002, precision=32), None),
+    (dict(nx=32, ny=32, nz=32, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=2e-3, i_cfl=1, cfl0=0.5), None),
+    (dict(nx=32, ny=64, nz=32, vis=3e-3, i_cfl=1, cfl0=0.5, precision=32), ("force", 5)),
+    (dict(nx=96, ny=96, nz=96, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=1e-3, i_cfl=1, cfl0=0.5, nrk_max=2,
+          precision=32), None),
+]
+
+
+@pytest.mark.parametrize("persistent", [True, False])
+def test_persistent_stage_launch_equals_single_runs(gpu_lib, persistent):
+    """The FP32 members without a closure whose lengths are 32, 64, 96 or 128
+    (five of the six here: the FP64 member keeps its own branch) advance in
+    one persistent launch per RK3 stage; every member ends bit for bit where
+    it ends when run alone, with either arrangement."""
+    params = CL.init_params(9)
+    starts = []
+    for cfg, _ in PERSISTENT:
+        c = dict(cfg)
+        c.pop("precision", None)
+        starts.append(O.Oracle(**c).init_random(len(starts) + 11, 6, 1.0, 6, 0.1))
+    singles = []
+    for (cfg, extra), u0 in zip(PERSISTENT, starts):
+        g = SamGpu(**cfg)
+        _setup(g, extra, u0, params)
+        g.step(3)
+        singles.append((g.download(), g.stats()))
+        g.close()
+    ens = SamEnsemble([cfg for cfg, _ in PERSISTENT])
+    try:
+        ens.set_persistent(persistent)
+        for m, ((cfg, extra), u0) in enumerate(zip(PERSISTENT, starts)):
+            _setup(ens[m], extra, u0, params)
+        ens.step(1)
+        assert ens.persistent_members() == (5 if persistent else 0)
+        ens.step(2)
+        for m, (u, st) in enumerate(singles):
+            assert np.array_equal(ens[m].download(), u), m
+            got = ens[m].stats()
+            assert got["time"] == st["time"] and got["dt"] == st["dt"], m
+            assert np.array_equal(got["u_max"], st["u_max"]), m
+    finally:
+        ens.close()
