@@ -101,18 +101,52 @@ template <int SIGN, typename C> __device__ __forceinline__ C ctw(C a, C w) {
   if (SIGN < 0) return mk<C>(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
   return mk<C>(a.x * w.x + a.y * w.y, a.y * w.x - a.x * w.y);
 }
-// double-float pairs: each part as one fused product difference (one
-// renormalisation instead of three)
-template <int SIGN> __device__ __forceinline__ ddc ctw(ddc a, ddc w) {
-  ddc r;
-  if (SIGN < 0) {
-    r.x = dd_mul_sub(a.x, w.x, a.y, w.y);
-    r.y = dd_mul_add(a.x, w.y, a.y, w.x);
-  } else {
-    r.x = dd_mul_add(a.x, w.x, a.y, w.y);
-    r.y = dd_mul_sub(a.y, w.x, a.x, w.y);
-  }
+__device__ __forceinline__ unsigned long long f2mul(unsigned long long a, unsigned long long b) {
+  unsigned long long r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
   return r;
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b,
+                                                    unsigned long long c) {
+  unsigned long long r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+// Complex double-float product a * (u + i v)-style: the real and imaginary
+// parts as one packed pair each step, lane k = x (0) or y (1):
+//   R_k = ax * U_k + ay * V_k
+// with U = (c1, c3), V = (c2, c4) the caller's coefficient pairs, given as
+// their high and low parts.  The two exact products (FMA TwoProduct, the
+// error terms formed negated from -ax, -ay so no packed negation is needed),
+// a TwoSum of them, the four cross terms and one renormalisation: the
+// operations of dd_mul_sub on both parts at once.
+__device__ __forceinline__ ddc dd_cplx_dot(ddc a, unsigned long long Uh, unsigned long long Ul,
+                                           unsigned long long Vh, unsigned long long Vl) {
+  const unsigned long long Xh = f2p(a.x.hi, a.x.hi), Xl = f2p(a.x.lo, a.x.lo), nXh = f2p(-a.x.hi, -a.x.hi);
+  const unsigned long long Yh = f2p(a.y.hi, a.y.hi), Yl = f2p(a.y.lo, a.y.lo), nYh = f2p(-a.y.hi, -a.y.hi);
+  const unsigned long long P = f2mul(Xh, Uh), Q = f2mul(Yh, Vh);
+  const unsigned long long nEP = f2fma(nXh, Uh, P), nEQ = f2fma(nYh, Vh, Q);  // -(exact error of P, Q)
+  const unsigned long long s = f2add(P, Q);
+  const unsigned long long bb = f2sub(s, P);
+  unsigned long long e = f2add(f2sub(P, f2sub(s, bb)), f2sub(Q, bb));
+  e = f2sub(e, f2add(nEP, nEQ));
+  e = f2fma(Xh, Ul, e);
+  e = f2fma(Xl, Uh, e);
+  e = f2fma(Yh, Vl, e);
+  e = f2fma(Yl, Vh, e);
+  const unsigned long long h = f2add(s, e);
+  const unsigned long long l = f2sub(e, f2sub(h, s));
+  ddc r;
+  f2u(h, r.x.hi, r.y.hi);
+  f2u(l, r.x.lo, r.y.lo);
+  return r;
+}
+// double-float pairs: a * w as a packed pair (SIGN = -1: U = (wx, wy),
+// V = (-wy, wx); SIGN = +1, a * conj(w): U = (wx, -wy), V = (wy, wx))
+template <int SIGN> __device__ __forceinline__ ddc ctw(ddc a, ddc w) {
+  if (SIGN < 0)
+    return dd_cplx_dot(a, f2p(w.x.hi, w.y.hi), f2p(w.x.lo, w.y.lo), f2p(-w.y.hi, w.x.hi), f2p(-w.y.lo, w.x.lo));
+  return dd_cplx_dot(a, f2p(w.x.hi, -w.y.hi), f2p(w.x.lo, -w.y.lo), f2p(w.y.hi, w.x.hi), f2p(w.y.lo, w.x.lo));
 }
 // multiply by SIGN * i  (exp(SIGN i pi/2))
 template <int SIGN, typename C> __device__ __forceinline__ C cmul_si(C a) {
@@ -262,10 +296,7 @@ template <typename C, typename T> __device__ __forceinline__ C crot(C v, T cr, T
   return mk<C>(v.x * cr - v.y * si, v.x * si + v.y * cr);
 }
 __device__ __forceinline__ ddc crot(ddc v, dd cr, dd si) {
-  ddc r;
-  r.x = dd_mul_sub(v.x, cr, v.y, si);
-  r.y = dd_mul_add(v.x, si, v.y, cr);
-  return r;
+  return dd_cplx_dot(v, f2p(cr.hi, si.hi), f2p(cr.lo, si.lo), f2p(-si.hi, cr.hi), f2p(-si.lo, cr.lo));
 }
 
 // 16-point DFT in registers as 4 x 4: DFT4 over n1 of x[4 n1 + n2], the
