@@ -291,7 +291,7 @@ def les_cfg(precision):
                 lapse=1.0, precision=precision)
 
 
-def les_forms(stream, K, W, t_spin=1.5, t_win=8.0, n_win=40):
+def les_forms(stream, K, W, t_spin=1.5, t_win=6.0, n_win=30):
     """The LES workload.  Speed: the FP64 drop-in with dm.f's dynamic closure
     and the FP32 bulk form with the learned closure, K steps each from their
     developed state after W warm-up steps (CUDA events on the launching
