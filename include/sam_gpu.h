@@ -165,8 +165,10 @@ int sam_gpu_profile_stage(int nrk, int reps, float* ms5);
  * sam_gpu_set_fft_schedule / sam_gpu_fft_schedule: the FFT schedule of each
  * pass (z inverse, y inverse, x, y forward, z forward) for lines of length
  * 256: 0 the 16 x 16 register path, 1 compile-time Stockham stages of radix
- * 8, 8, 4 (other lengths have one schedule and ignore the value); values
- * other than 0 and 1 are rejected (SAM_GPU_EINVAL). */
+ * 8, 8, 4 (other lengths have one schedule and ignore the value).  The x
+ * pass also takes 2: the 16 x 16 path inside the general x-pass kernel,
+ * where 0 runs the fused FP32 kernel of the plain step (same results,
+ * bit for bit).  Other values are rejected (SAM_GPU_EINVAL). */
 int sam_gpu_autotune(int reps);
 int sam_gpu_tiles(int* out6);
 int sam_gpu_set_fft_schedule(const int* sched5);

@@ -65,6 +65,21 @@ inline int sm_count() {
   return cache[dev];
 }
 
+// The largest dynamic shared memory a block of the current device may opt
+// into (looked up once per device).
+inline int smem_optin() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (!cache[dev]) {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess || n < 1)
+      n = 48 * 1024;
+    cache[dev] = n;
+  }
+  return cache[dev];
+}
+
 // Records the message returned by sam_gpu_error_string(); returns code.
 int set_error(int code, const char* msg);
 

@@ -148,6 +148,13 @@ template <int SIGN> __device__ __forceinline__ ddc ctw(ddc a, ddc w) {
     return dd_cplx_dot(a, f2p(w.x.hi, w.y.hi), f2p(w.x.lo, w.y.lo), f2p(-w.y.hi, w.x.hi), f2p(-w.y.lo, w.x.lo));
   return dd_cplx_dot(a, f2p(w.x.hi, -w.y.hi), f2p(w.x.lo, -w.y.lo), f2p(w.y.hi, w.x.hi), f2p(w.y.lo, w.x.lo));
 }
+// FP32: the same products with their rounding spelled out (the second
+// product rounded, the first fused with the sum), so every kernel computes
+// the same bits whatever the compiler would contract at each call site
+template <int SIGN> __device__ __forceinline__ float2 ctw(float2 a, float2 w) {
+  if (SIGN < 0) return make_float2(__fmaf_rn(a.x, w.x, -__fmul_rn(a.y, w.y)), __fmaf_rn(a.x, w.y, __fmul_rn(a.y, w.x)));
+  return make_float2(__fmaf_rn(a.x, w.x, __fmul_rn(a.y, w.y)), __fmaf_rn(a.y, w.x, -__fmul_rn(a.x, w.y)));
+}
 // multiply by SIGN * i  (exp(SIGN i pi/2))
 template <int SIGN, typename C> __device__ __forceinline__ C cmul_si(C a) {
   if (SIGN < 0) return mk<C>(a.y, -a.x);
@@ -294,6 +301,9 @@ template <int SIGN, typename C> __device__ __forceinline__ void dft5(C* a) {
 // v * (cr + i si) for real constants cr, si
 template <typename C, typename T> __device__ __forceinline__ C crot(C v, T cr, T si) {
   return mk<C>(v.x * cr - v.y * si, v.x * si + v.y * cr);
+}
+__device__ __forceinline__ float2 crot(float2 v, float cr, float si) {
+  return make_float2(__fmaf_rn(v.x, cr, -__fmul_rn(v.y, si)), __fmaf_rn(v.x, si, __fmul_rn(v.y, cr)));
 }
 __device__ __forceinline__ ddc crot(ddc v, dd cr, dd si) {
   return dd_cplx_dot(v, f2p(cr.hi, si.hi), f2p(cr.lo, si.lo), f2p(-si.hi, cr.hi), f2p(-si.lo, cr.lo));

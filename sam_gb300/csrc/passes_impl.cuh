@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "common.cuh"
 #include "passes.cuh"
 
@@ -343,6 +345,16 @@ __device__ __forceinline__ DF df_add_sq(DF a, float v) {
   return df_add(df_add(a, p), e);
 }
 
+// The products of rhs.f:46-60, rounded once each.  In FP32 the rounding is
+// spelled out (__fmul_rn is never fused into a neighbouring sum), so the
+// general kernel and the fused FP32 x pass compute the same bits.  (A packed
+// mul.rn.f32x2 would not do: where its result feeds an add/sub.rn.f32x2 the
+// compiler fuses the pair into one FMA despite the .rn modifiers; measured
+// on 2^20 random operand pairs, every differing result equalled fmaf.)
+__device__ __forceinline__ float pmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double pmul(double a, double b) { return a * b; }
+__device__ __forceinline__ dd pmul(dd a, dd b) { return a * b; }
+
 // First-stage loader of the forward x transform: element idx of line a, or,
 // when b is given, of line a times line b component by component (the two
 // real rows of a pair multiply separately), i.e. a product line of rhs.f.
@@ -354,9 +366,9 @@ template <typename C> struct ProductLoad {
     const C va = a[sidx(idx)];
     if (!b) return va;
     const C vb = b[sidx(idx)];
-    if (!g) return mk<C>(va.x * vb.x, va.y * vb.y);
+    if (!g) return mk<C>(pmul(va.x, vb.x), pmul(va.y, vb.y));
     const C vg = g[sidx(idx)];
-    return mk<C>(va.x * vb.x + vg.x, va.y * vb.y + vg.y);
+    return mk<C>(pmul(va.x, vb.x) + vg.x, pmul(va.y, vb.y) + vg.y);
   }
 };
 
@@ -930,6 +942,244 @@ __global__ void __launch_bounds__(x_threads(sizeof(T), PATH == kFft256), MinBloc
   x_pass_body<T, PATH>(a, gpl, blockIdx.x);
 }
 
+// ------------------------------------------------ x pass, FP32 at Nx = 256
+// The x pass of the plain FP32 step with 256-point x lines (spectral input
+// rows, products out, no subgrid terms; at stage 1 vel_max's max |u| and
+// non-finite flag) as one kernel without run-time generality.  Its
+// arithmetic is x_pass_body's 16 x 16 register path operation for operation,
+// so the results are bit-identical; the bookkeeping around it differs:
+//  - the truncated band kx_max < p < Nx - kx_max of each staged line is
+//    written as zeros once, so the first transform stage reads plain shared
+//    memory (no per-element band test);
+//  - a team of 16 threads owns one scratch line and takes a product line
+//    from its first transform stage to HBM by itself: it forms the product
+//    while loading, transforms it, pairs Z(kx) with Z(Nx - kx) by shuffles
+//    within the team (thread k holds Z(k + 16 j) after the second stage, and
+//    Z(256 - k - 16 j) sits in thread (16 - k) mod 16 at j' = 15 - j, or at
+//    (16 - j) mod 16 for k = 0) and stores the split pair.  Teams synchronise
+//    only among their own 16 threads: the product phase has no CTA barrier
+//    and no separate output loop.
+// Shared memory: the 16 x 16 twiddles w_256^{k q} at [16 q + k], the Nin *
+// Y/2 input lines, one scratch line per team (vel_max's reduction scratch
+// before the products).
+constexpr int kXf256Threads = 288;                  // 18 teams of 16 (two rounds of 9 x 4 product lines)
+constexpr int kXf256Teams = kXf256Threads / 16;
+constexpr int kXf256Ld = 271;                       // line_stride(256)
+static_assert(kXf256Ld == ((256 + (255 >> 4)) | 1), "line stride of a 256-point line");
+__host__ __device__ constexpr size_t x_f256_smem(int lines) {
+  return sizeof(float2) * (256 + (size_t)(lines + kXf256Teams) * kXf256Ld);
+}
+
+// the second stage of the 16 x 16 path on a line already in shared memory:
+// thread k reads row 16 k + q, applies w_256^{k q} and transforms it, leaving
+// Z(k + 16 j) in v[j]
+template <int SIGN>
+__device__ __forceinline__ void f256_rows(float2* v, const float2* line, const float2* w, int k) {
+  v[0] = line[17 * k];
+#pragma unroll
+  for (int q = 1; q < 16; ++q) v[q] = ctw<SIGN>(line[17 * k + q], w[16 * q]);
+  dft16<SIGN>(v);
+}
+
+// (a template only so that the translation units including this header
+// share one instantiation)
+template <int V = 0>
+__global__ void __launch_bounds__(kXf256Threads, 3) k_x_pass_f256(const __grid_constant__ XPassArgs<float> a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int nx = 256, LD = kXf256Ld;
+  float2* s_tw = reinterpret_cast<float2*>(smem_raw);
+  float2* s_in = s_tw + 256;
+  const int ny = a.g.ny, kmx = a.g.kx, mx = a.g.mx;
+  const int Y = a.yt, yp = Y / 2, nl = a.nin * yp;
+  float2* s_pr = s_in + nl * LD;
+  const int nyt = (ny + Y - 1) / Y;
+  const int z = blockIdx.x / nyt;
+  const int y0 = (blockIdx.x - z * nyt) * Y;
+  const int yv = min(Y, ny - y0);
+  const int tid = threadIdx.x;
+  if (tid < 256) s_tw[tid] = a.tw[tid];
+  {
+    // zeros in the truncated band (sidx of its ends: one contiguous run)
+    const int b0 = sidx(kmx + 1), nb = sidx(nx - kmx - 1) - b0 + 1;
+    for (int L = tid / 18; L < nl; L += kXf256Threads / 18)
+      for (int j = tid % 18; j < nb; j += 18) s_in[L * LD + b0 + j] = make_float2(0.f, 0.f);
+  }
+  {
+    // the stored half spectra, two rows per line (x + i y): a thread keeps
+    // one kx and issues the loads of a batch of lines before its stores
+    const int kspan = min(mx, kXf256Threads);
+    const int lanes = kXf256Threads / kspan;
+    const int lane = tid / kspan;
+    if (lane < lanes)
+      for (int kx = tid - lane * kspan; kx < mx; kx += kspan) {
+        const float2* src0 = a.in + (long long)z * a.in_z + kx;
+        const int sa = sidx(kx), sb = sidx(kx == 0 ? 0 : nx - kx);
+        for (int L0 = lane; L0 < nl; L0 += kBatch * lanes) {
+          float2 X[kBatch], Yv[kBatch];
+#pragma unroll
+          for (int u = 0; u < kBatch; ++u) {
+            const int L = L0 + u * lanes;
+            X[u] = make_float2(0.f, 0.f);
+            Yv[u] = make_float2(0.f, 0.f);
+            if (L < nl) {
+              const int f = (int)fdiv(L, a.fd_yp), c = L - f * yp;
+              const int ya = y0 + 2 * c;
+              const float2* src = src0 + (long long)f * a.in_n + (long long)ya * a.in_y;
+              if (ya < ny) X[u] = src[0];
+              if (ya + 1 < ny) Yv[u] = src[a.in_y];
+            }
+          }
+#pragma unroll
+          for (int u = 0; u < kBatch; ++u) {
+            const int L = L0 + u * lanes;
+            if (L < nl) {
+              if (kx == 0) {  // xy_trans_b.f:28-31 keeps only the real part of kx = 0
+                X[u].y = 0.f;
+                Yv[u].y = 0.f;
+              }
+              s_in[L * LD + sa] = make_float2(X[u].x - Yv[u].y, X[u].y + Yv[u].x);
+              if (kx > 0) s_in[L * LD + sb] = make_float2(X[u].x + Yv[u].y, Yv[u].x - X[u].y);
+            }
+          }
+        }
+      }
+  }
+  __syncthreads();
+
+  // ---- the backward transforms (xy_trans_b.f:39-60), in place
+  const int team = tid >> 4, k = tid & 15;
+  const unsigned tmask = 0xFFFFu << (tid & 16);
+  const float2* w = s_tw + k;
+  for (int L = team; L < nl; L += kXf256Teams) {
+    float2* line = s_in + L * LD;
+    float2 v[16];
+    // the first stage reads and writes the thread's own column (k + 17 q)
+#pragma unroll
+    for (int q = 0; q < 16; ++q) v[q] = line[k + 17 * q];
+    dft16<+1>(v);
+#pragma unroll
+    for (int s = 0; s < 16; ++s) line[17 * s + k] = v[s];
+    __syncwarp(tmask);
+    f256_rows<+1>(v, line, w, k);
+    __syncwarp(tmask);
+#pragma unroll
+    for (int s = 0; s < 16; ++s) line[k + 17 * s] = v[s];
+  }
+  __syncthreads();
+
+  // ---- vel_max (vel_max.f:11-21): max |u| of each field and the
+  // non-finite flag; the sums come from wave space (k_parseval)
+  if (a.partials) {
+    float mx4[4] = {0.f, 0.f, 0.f, 0.f};
+    int bad = 0;
+    for (int e = tid; e < yp * nx; e += kXf256Threads) {
+      const int c = e >> 8, x = e & 255;
+      const bool ra = y0 + 2 * c < ny, rb = y0 + 2 * c + 1 < ny;
+#pragma unroll
+      for (int f = 0; f < 4; ++f)
+        if (f < a.g.lu) {
+          const float2 v = s_in[(f * yp + c) * LD + sidx(x)];
+          if (ra) {
+            mx4[f] = fmaxf(mx4[f], fabsf(v.x));
+            bad |= !isfinite(v.x);
+          }
+          if (rb) {
+            mx4[f] = fmaxf(mx4[f], fabsf(v.y));
+            bad |= !isfinite(v.y);
+          }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int f = 0; f < 4; ++f) mx4[f] = fmaxf(mx4[f], __shfl_xor_sync(0xffffffffu, mx4[f], o));
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    constexpr int nw = kXf256Threads / 32;
+    float* s_mx = reinterpret_cast<float*>(s_pr);
+    int* s_bad = reinterpret_cast<int*>(s_mx + 4 * nw);
+    if ((tid & 31) == 0) {
+#pragma unroll
+      for (int f = 0; f < 4; ++f) s_mx[(tid >> 5) * 4 + f] = mx4[f];
+      s_bad[tid >> 5] = bad;
+    }
+    __syncthreads();
+    // one atomic per field and CTA: the max of non-negative floats is the
+    // max of their bit patterns (order-independent, so deterministic)
+    if (tid < a.g.lu) {
+      float tm = 0.f;
+      int tb = 0;
+      for (int q = 0; q < nw; ++q) {
+        tm = fmaxf(tm, s_mx[q * 4 + tid]);
+        tb |= s_bad[q];
+      }
+      atomicMax(a.vmax + tid, __float_as_int(tm));
+      if (tid == 0 && tb) atomicOr(a.vmax + 8, 1);
+    }
+    __syncthreads();
+  }
+
+  // ---- products (rhs.f:46-60), forward transforms, split, scale, store
+  // C(m, z, kx, y) (xy_trans_f.f:20-37)
+  const float fn = a.fn;
+  float2* tline = s_pr + team * LD;
+  const int partner = (tid & 16) | ((16 - k) & 15);
+  const int nq = a.g.lr * yp;
+  for (int q = team; q < nq; q += kXf256Teams) {
+    const int m = (int)fdiv(q, a.fd_yp), c = q - m * yp;
+    int fa, fb;
+    product_pair(m, fa, fb);
+    const float2* pa = s_in + (fa * yp + c) * LD + k;
+    const float2* pb = s_in + (fb * yp + c) * LD + k;
+    float2 v[16];
+    // (scalar products: a packed mul.rn.f32x2 feeding the first stage's
+    // packed sums is fused by the compiler into an FMA despite the .rn)
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const float2 ea = pa[17 * j], eb = pb[17 * j];
+      v[j] = make_float2(pmul(ea.x, eb.x), pmul(ea.y, eb.y));
+    }
+    dft16<-1>(v);
+    __syncwarp(tmask);  // the team's reads of its previous line are done
+#pragma unroll
+    for (int s = 0; s < 16; ++s) tline[17 * s + k] = v[s];
+    __syncwarp(tmask);
+    f256_rows<-1>(v, tline, w, k);
+    float2* o = a.out + (long long)z * a.out_z + (long long)m * a.out_n + (long long)k * a.out_kx + y0 + 2 * c;
+    const bool two = 2 * c + 1 < yv, one = 2 * c < yv;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      if (16 * j > kmx) break;
+      // Z(Nx - kx) for kx = k + 16 j, from the partner thread
+      const float2 snd = k == 0 ? v[(16 - j) & 15] : v[15 - j];
+      float2 z2;
+      z2.x = __shfl_sync(tmask, snd.x, partner);
+      z2.y = __shfl_sync(tmask, snd.y, partner);
+      const float2 z1 = v[j];
+      if (k + 16 * j <= kmx) {
+        const float2 ve = make_float2((z1.x + z2.x) * fn, (z1.y - z2.y) * fn);
+        const float2 vo = make_float2((z1.y + z2.y) * fn, (z2.x - z1.x) * fn);
+        float2* oj = o + (long long)(16 * j) * a.out_kx;
+        if (two) {
+          if ((reinterpret_cast<uintptr_t>(oj) & 15) == 0) {
+            store_pair(oj, ve, vo);
+          } else {  // odd Ny: the pair straddles a vector boundary
+            oj[0] = ve;
+            oj[1] = vo;
+          }
+        } else if (one) {
+          oj[0] = ve;
+        }
+      }
+    }
+  }
+}
+
+// whether k_x_pass_f256 runs this launch (else the general kernel)
+__host__ __device__ inline bool x_f256_applies(const XPassArgs<float>& a) {
+  return a.g.nx == 256 && a.sched == 0 && a.in_mode == 0 && a.out_mode == 2 && a.les == 0 && a.nin == a.g.lu &&
+         a.nin <= 4 && (a.g.lr == 6 || a.g.lr == 9) && (!a.partials || a.max_only) && a.yt >= 2 && a.yt % 2 == 0;
+}
+
 // --------------------------------------------------------------- y forward
 // Tile: field m, kx column i, planes z0 .. z0+TZ-1.  Output D(m, kx, ky, z)
 // keeps |ky| <= ky_max (xy_trans_f.f:45-52).
@@ -1448,8 +1698,18 @@ void launch_x_pass(const XPassArgs<T>& a0, const FftPlan* pl, size_t smem, cudaS
   const XPassArgs<T> a = prep_x_pass(a0);
   switch (a.g.nx) {
     case 256:
-      if (a.sched) k_x_pass<T, 256><<<x_pass_blocks(a), x_threads(sizeof(T), false), smem, s>>>(a, pl);
-      else k_x_pass<T, kFft256><<<x_pass_blocks(a), x_threads(sizeof(T), true), smem, s>>>(a, pl);
+      if (a.sched == 1) {
+        k_x_pass<T, 256><<<x_pass_blocks(a), x_threads(sizeof(T), false), smem, s>>>(a, pl);
+        break;
+      }
+      if constexpr (std::is_same<T, float>::value) {
+        const size_t fsm = x_f256_smem(a.nin * (a.yt / 2));
+        if (x_f256_applies(a) && fsm <= (size_t)smem_optin()) {
+          k_x_pass_f256<><<<x_pass_blocks(a), kXf256Threads, fsm, s>>>(a);
+          break;
+        }
+      }
+      k_x_pass<T, kFft256><<<x_pass_blocks(a), x_threads(sizeof(T), true), smem, s>>>(a, pl);
       break;
     case 32: k_x_pass<T, 32><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
     case 64: k_x_pass<T, 64><<<x_pass_blocks(a), kThreads, smem, s>>>(a, pl); break;
@@ -1528,6 +1788,7 @@ void smem_limits_yinv(int optin) {
 }
 template <typename T>
 void smem_limits_x(int optin) {
+  if constexpr (std::is_same<T, float>::value) allow_dynamic_smem((const void*)k_x_pass_f256<>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, kFft256>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, kFftGeneric>, optin);
   allow_dynamic_smem((const void*)k_x_pass<T, 32>, optin);

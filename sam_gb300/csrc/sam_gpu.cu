@@ -187,7 +187,9 @@ struct Ctx {
   // tile choices
   int ty_zi = 16, tx_yi = 16, yt_x = 8, grp_x = 9, tz_yf = 16, ty_zf = 4;
   // FFT schedule of each pass for length-256 lines (z_inv, y_inv, x, y_fwd,
-  // z_fwd): 0 the 16 x 16 register path, 1 compile-time Stockham (8, 8, 4)
+  // z_fwd): 0 the 16 x 16 register path, 1 compile-time Stockham (8, 8, 4);
+  // the x pass also takes 2: the register path inside the general x-pass
+  // kernel even where the fused FP32 kernel applies (0 picks that one)
   int sched[5] = {0, 0, 0, 0, 0};
   OuForcing* ou = nullptr;  // device OU forcing state, null when off
   // subgrid closure coupled into the stage (sam_gpu_set_les)
@@ -268,7 +270,7 @@ static int line_ld(int n) { return line_stride(n); }
 // shared memory of a tile of `lines` lines of length n plus the twiddles
 // the kernel loads (schedule 1 of a length-256 pass loads the whole table)
 static size_t tile_smem(const Plan& P, int lines, size_t es, int sched = 0) {
-  const int ntw = sched && P.h.n == 256 ? P.h.tw_total : P.h.tw_pass;
+  const int ntw = sched == 1 && P.h.n == 256 ? P.h.tw_total : P.h.tw_pass;
   return es * ((size_t)ntw + (size_t)lines * line_ld(P.h.n)) + 16;
 }
 
@@ -336,7 +338,7 @@ static int run_y_inv(Ctx& c, const void* in, void* out, int nvar, int in_full, l
 }
 
 // whether the x pass runs the 16 x 16 register path
-static bool x_reg16(const Ctx& c) { return c.g.nx == 256 && c.sched[2] == 0; }
+static bool x_reg16(const Ctx& c) { return c.g.nx == 256 && c.sched[2] != 1; }
 
 // lines the reduction scratch of vel_max occupies (FP64 partials of each warp)
 template <typename T>
@@ -1779,7 +1781,8 @@ int sam_gpu_set_fft_schedule(const int* sched5) {
   NEED_CTX();
   if (!sched5) return fail(SAM_GPU_EINVAL, "set_fft_schedule: null array");
   for (int p = 0; p < 5; ++p)
-    if (sched5[p] != 0 && sched5[p] != 1) return fail(SAM_GPU_EINVAL, "FFT schedule %d of pass %d", sched5[p], p);
+    if (sched5[p] != 0 && sched5[p] != 1 && !(p == 2 && sched5[p] == 2))
+      return fail(SAM_GPU_EINVAL, "FFT schedule %d of pass %d", sched5[p], p);
   for (int p = 0; p < 5; ++p) c.sched[p] = sched5[p];
   if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
   c.graph_stale = 1;

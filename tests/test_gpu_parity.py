@@ -169,6 +169,35 @@ def test_fft_schedules_agree_in_fp32(gpu_lib):
     assert relerr(out[1], out[0]) < 1e-5
 
 
+@pytest.mark.parametrize("case", [
+    dict(ny=256, nz=12, i_strat=1, n_dealias=1),   # the benchmark's lines, stratified
+    dict(ny=243, nz=10, i_strat=0, n_dealias=1),   # odd Ny: ragged tiles, unaligned pair stores
+    dict(ny=40, nz=8, i_strat=1, n_dealias=0),     # no truncation: kx_max = 127
+    dict(ny=36, nz=9, i_strat=1, n_dealias=2),
+])
+def test_fused_fp32_x_pass_bit_identical(gpu_lib, case):
+    """The fused FP32 x pass at Nx = 256 (schedule 0) against the 16 x 16 path
+    of the general kernel (schedule 2): two CFL steps, bit for bit, with
+    vel_max's max |u| taken in the fused kernel at stage 1."""
+    cfg = dict(nx=256, i_cfl=1, cfl0=0.5, vis=2e-3, pr=1.0, buoy_fac_z=1.0, lapse=1.0, **case)
+    o = O.Oracle(**cfg)
+    u = o.init_random(11, 6, 1.0, 6, 0.1)
+    o.close()
+    out = []
+    for sched in ([0, 0, 0, 0, 0], [0, 0, 2, 0, 0]):
+        g = SamGpu(precision=32, **cfg)
+        g.set_fft_schedule(sched)
+        assert g.fft_schedule() == sched
+        g.upload(u)
+        g.step(2)
+        out.append((g.download(), g.stats()["dt"]))
+        g.close()
+    (u0, dt0), (u2, dt2) = out
+    assert np.isfinite(u0).all()
+    assert dt0 == dt2
+    assert np.array_equal(u0, u2), np.abs(u0 - u2).max() / np.abs(u2).max()
+
+
 def test_taylor_green_64_200_steps(gpu_lib):
     """Config 1: Taylor-Green 64^3, nu = 1/400, dt = 0.01, 200 RK3 steps."""
     cfg = dict(nx=64, ny=64, nz=64, vis=1.0 / 400, dt0=0.01)
