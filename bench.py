@@ -796,11 +796,11 @@ def main():
         xb32 = x_pass_bytes(w=4)
         a32 = xb32 / (x32_ms / 1e3) / 1e9
         tr32 = profile_traffic("x_pass_fp32_traffic.json")
-        fp32["roofline"] = {"bound": "hbm", "kernel": "k_x_pass<float> (C2R, 9 products, R2C; stages 2 and 3)",
+        fp32["roofline"] = {"bound": "hbm", "kernel": "k_x_pass_f256 (C2R, 9 products, R2C; stages 2 and 3)",
                             "achieved": a32, "peak": hbm_peak, "unit": "GB/s", "frac": a32 / hbm_peak,
                             "traffic": tr32.get("bytes_per_launch") if tr32 else None,
                             "algorithmic_bytes_per_launch": xb32, "ms": x32_ms,
-                            "note": "instruction- and latency-bound: counters in profiles/x_pass_256_ncu.md"}
+                            "note": "bound by shared-memory traffic and latency: counters in profiles/x_pass_f256_fp32_256_ncu.md"}
     if ddf is not None:
         xd_ms = ddf.pop("_x_ms")
         ad = x_pass_bytes(w=8) / (xd_ms / 1e3) / 1e9
