@@ -493,7 +493,7 @@ def ensemble_form(K, W):
 def run_probe(args):
     """A short fixed launch sequence for ncu: init, 3 steps (each stage: the
     five passes), nothing else; --les 3 uses the LES start with the learned
-    closure (network kernel launched once per stage)."""
+    closure (network kernel launched at stage 1 of each step)."""
     from sam_gb300 import SamGpu, build as B
     B.build()
     if args.les:

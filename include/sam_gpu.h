@@ -246,11 +246,16 @@ int sam_gpu_set_forcing(unsigned long long seed, double k_f, double sigma, doubl
  *            coefficient (dm.f:176) of the physical velocity, evaluated at
  *            stage 1 of every step (as vel_max is, rhs.f:26-28) and clipped
  *            at zero; it starts at 0 until the first stage 1;
- *   model 3: learned closure: every stage also takes the vorticity to
- *            physical space, forms 12 invariants of S, w and dT/dx per point
- *            (BF16), runs the network of sam_gpu_mlp_set on the tensor cores
- *            and uses its per-point (C_nu, C_kappa): nu_t = C_nu delta^2 |S|,
- *            kappa_t = C_kappa delta^2 |S| (pr_t unused).
+ *   model 3: learned closure: stage 1 of every step also takes the
+ *            vorticity to physical space, forms 12 invariants of S, w and
+ *            dT/dx per point (BF16) and runs the network of sam_gpu_mlp_set
+ *            on the tensor cores; every stage uses the per-point (C_nu,
+ *            C_kappa) of the last stage 1 with its own |S|:
+ *            nu_t = C_nu delta^2 |S|, kappa_t = C_kappa delta^2 |S| (pr_t
+ *            unused).  The coefficients are formed once per step like
+ *            model 2's and the reference's own model coefficient
+ *            (sam.f:128-132, cl_energy at nrk = 1); they are zero until the
+ *            first stage 1.
  * Allocates the extra pencil, dm.f and invariant buffers on first use. */
 int sam_gpu_set_les(int model, double c_smag, double pr_t);
 /* C delta^2 last used (0 with the closure off) */

@@ -60,6 +60,7 @@ struct so_ctx {
   double *les_uh;     /* haloed velocity (Lx, Ly, Lz, 3) for so_dm */
   double *les_vt;     /* haloed vt of so_dm */
   float les_mlp[5122]; /* learned closure parameters (so_mlp_set) */
+  float *les_cf;      /* learned closure: (C_nu, C_kappa) per point, from stage 1 */
 };
 
 static const double SO_PI = 3.14159265358979323846;
@@ -158,7 +159,7 @@ void so_destroy(so_ctx *c) {
   so_cplan_free(&c->py); so_cplan_free(&c->pz);
   free(c->k_x); free(c->k_y); free(c->k_z);
   free(c->zb); free(c->uu); free(c->usav);
-  free(c->les_w); free(c->les_zb); free(c->les_g); free(c->les_uh); free(c->les_vt);
+  free(c->les_w); free(c->les_zb); free(c->les_g); free(c->les_uh); free(c->les_vt); free(c->les_cf);
   free(c);
 }
 
@@ -1547,9 +1548,13 @@ static void so_les_stress(so_ctx *c, const double *uu, int nrk) {
   const double cds = c->les_cds, prt_inv = c->les_prt_inv;
   double *g = c->les_g;
   if (c->les_model == 3) {
+    /* the network's coefficients once per step, at stage 1, as the
+     * reference's model coefficient (sam.f:128-132: cl_energy at nrk = 1);
+     * stages 2 and 3 keep them and take |S| from their own strain */
     const double dsq = delta_sq_of(c), bz = c->cfg.buoy_fac_z, n2 = c->cfg.buoy_fac_z * c->cfg.lapse;
     const double nu_ref = c->cfg.vis > 1e-12 ? c->cfg.vis : 1e-12;
     const int lr = c->lr;
+    float *cfs = c->les_cf;
     set_threads(c);
 #pragma omp parallel for schedule(static)
     for (size_t p = 0; p < np; ++p) {
@@ -1558,9 +1563,12 @@ static void so_les_stress(so_ctx *c, const double *uu, int nrk) {
       if (lr == 9)
         for (int m = 0; m < 3; ++m) gt[m] = g[p + (6 + m) * np];
       for (int m = 0; m < 3; ++m) w[m] = g[p + (lr + m) * np];
-      float f[12], cf[2];
-      so_invariants(S, gt, w, bz, n2, dsq, nu_ref, f);
-      so_mlp_eval(c->les_mlp, f, cf);
+      float *cf = cfs + 2 * p;
+      if (nrk == 1) {
+        float f[12];
+        so_invariants(S, gt, w, bz, n2, dsq, nu_ref, f);
+        so_mlp_eval(c->les_mlp, f, cf);
+      }
       double sum = 0.0;
       for (int m = 0; m < 6; ++m) sum += (m == 1 || m == 3 || m == 4 ? 2.0 : 1.0) * S[m] * S[m];
       const double sm = sqrt(2.0 * sum);
@@ -1590,8 +1598,9 @@ int so_set_les(so_ctx *c, int model, double c_smag, double pr_t) {
   if (model < 0 || model > 3 || !(pr_t > 0.0)) return -1;
   if (c->les_w && model == 3 && c->les_model != 3) {
     /* the learned closure carries three more fields: reallocate */
-    free(c->les_w); free(c->les_zb); free(c->les_g); free(c->les_uh); free(c->les_vt);
+    free(c->les_w); free(c->les_zb); free(c->les_g); free(c->les_uh); free(c->les_vt); free(c->les_cf);
     c->les_w = NULL;
+    c->les_cf = NULL;
   }
   c->les_model = model;
   c->les_c_smag = c_smag;
@@ -1605,6 +1614,7 @@ int so_set_les(so_ctx *c, int model, double c_smag, double pr_t) {
   c->les_w = (so_cplx *)calloc(nw, sizeof(so_cplx));
   c->les_zb = (so_cplx *)calloc((size_t)c->ny_min * c->nx_min * c->nze * ng, sizeof(so_cplx));
   c->les_g = (double *)calloc(np * ng, sizeof(double));
+  c->les_cf = (float *)calloc(np * 2, sizeof(float));
   c->les_uh = (double *)calloc(vol * 3, sizeof(double));
   c->les_vt = (double *)calloc(vol, sizeof(double));
   return 0;

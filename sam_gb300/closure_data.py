@@ -355,7 +355,7 @@ if __name__ == "__main__":
     ap.add_argument("--n", type=int, default=512)
     ap.add_argument("--filters", type=int, nargs="+", default=[4, 8], help="box-filter ratios of the samples")
     ap.add_argument("--snaps", type=int, default=10)
-    ap.add_argument("--steps", type=int, default=0, help="Adam steps (default: one pass over the data)")
+    ap.add_argument("--steps", type=int, default=12000, help="Adam steps (0: one pass over the data)")
     ap.add_argument("--batch", type=int, default=8192)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--vis", type=float, default=5e-4)
@@ -363,7 +363,7 @@ if __name__ == "__main__":
     ap.add_argument("--every", type=float, default=0.1)
     ap.add_argument("--eval", type=float, default=1.0, help="a posteriori comparison window")
     ap.add_argument("--neval", type=int, default=4, help="comparison times in the window")
-    ap.add_argument("--sigma", type=float, default=0.5, help="OU forcing rms amplitude")
+    ap.add_argument("--sigma", type=float, default=0.15, help="OU forcing rms amplitude")
     ap.add_argument("--tl", type=float, default=0.5, help="OU forcing correlation time")
     ap.add_argument("--out", default=WEIGHTS)
     a = ap.parse_args()

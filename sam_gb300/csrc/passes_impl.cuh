@@ -38,16 +38,18 @@ __device__ __forceinline__ void load_twiddles(cx_t<T>* s_tw, const cx_t<T>* __re
 constexpr int kBatch = 8;
 
 // Resident CTAs per SM each kernel's register budget is sized for (measured
-// at 256^3): in FP32 the transpose passes fit 64 registers (four CTAs) and
-// the x pass 72 (three CTAs of 288 threads) without spills; the FP32 z_fwd
-// epilogue spills below 128 and keeps two (three measured slower); FP64 CTAs
-// are bound by the FP64 pipe.
+// at 256^3): in FP32 the transpose passes of the 16 x 16 register path fit
+// 64 registers (four CTAs) and the x pass 72 (three CTAs of 288 threads)
+// without spills; the compile-time Stockham transposes (lengths 32-512)
+// spilled 40-110 bytes at 64 and keep three CTAs (80 registers; 128^3 y
+// forward 10 % faster); the FP32 z_fwd epilogue spills below 128 and keeps
+// two (three measured slower); FP64 CTAs are bound by the FP64 pipe.
 // The run-time-radix path (kFftGeneric, lengths without a compile-time
 // path) needs more registers: one x pass CTA per SM, two of the others.
 enum PassKind { kPassZInv, kPassYInv, kPassX, kPassYFwd, kPassZFwd };
 template <typename T, int K, int PATH = kFft256> struct MinBlocks {
   static constexpr int value =
-      PATH == kFftGeneric ? (K == kPassX ? 1 : 2) : (K == kPassZFwd ? 2 : (K == kPassX ? 3 : 4));
+      PATH == kFftGeneric ? (K == kPassX ? 1 : 2) : (K == kPassZFwd ? 2 : (K == kPassX ? 3 : (PATH == kFft256 ? 4 : 3)));
 };
 template <int K, int PATH> struct MinBlocks<double, K, PATH> {
   static constexpr int value = PATH == kFftGeneric ? 1 : 2;

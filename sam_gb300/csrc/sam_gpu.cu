@@ -541,7 +541,12 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
   // gradient fields the products need
   const bool les = c.les_model != 0;
   const int nin = g.lu + (les ? g.lr : 0);
-  const int ninv = nin + (c.les_model == 3 ? 3 : 0);  // + vorticity for the invariants
+  // the learned closure's coefficients are formed once per step, at stage
+  // 1, like the reference's model coefficient (sam.f:128-132: cl_energy at
+  // nrk = 1) and dm.f's here; stages 2 and 3 keep them and take |S| from
+  // their own strain
+  const bool coef_stage = c.les_model == 3 && nrk == 1;
+  const int ninv = nin + (coef_stage ? 3 : 0);  // + vorticity for the invariants
   if (ev) cudaEventRecord(ev[0], c.stream);
   // z inverse: U(n, kx, ky, kz) -> A(n, z, kx, ky)
   if (run(0))
@@ -568,7 +573,7 @@ static int enqueue_stage(Ctx& c, int nrk, cudaEvent_t* ev = nullptr, int only = 
     }
   }
   // learned closure: the invariants of every point, then the network
-  if (run(2) && c.les_model == 3) {
+  if (run(2) && coef_stage) {
     const long long bn = (long long)g.nz * g.ny * g.mx;
     rc = run_x_pass<T>(c, 0, 4, g.lr + 3, (const cx_t<T>*)c.S2 + g.lu * bn, nullptr, g.mx, (long long)g.ny * g.mx,
                        bn, nullptr, nullptr, 0, 0, 0, 0, 0, 0, false);
@@ -1388,6 +1393,8 @@ int sam_gpu_set_les(int model, double c_smag, double pr_t) {
       if (rc) return rc;
       CK(cudaMalloc(&c.les_feat, 32 * np));
       CK(cudaMalloc(&c.les_coef, sizeof(float2) * np));
+      // zero until the first stage 1 forms them (no subgrid terms before)
+      CK(cudaMemsetAsync(c.les_coef, 0, sizeof(float2) * np, c.stream));
     }
   }
   double dsq;

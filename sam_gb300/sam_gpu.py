@@ -378,7 +378,9 @@ class SamGpu:
     def set_les(self, model, c_smag=0.01, pr_t=1.0):
         """Subgrid closure coupled into every stage: 0 off, 1 Smagorinsky
         (C delta^2 = c_smag delta^2), 2 dynamic (dm.f's coefficient at stage
-        1 of each step); kappa_t = nu_t / pr_t."""
+        1 of each step), 3 the learned closure (the network's per-point
+        coefficients at stage 1 of each step); kappa_t = nu_t / pr_t
+        (models 1, 2)."""
         self._check(load_library().sam_gpu_set_les(model, c_smag, pr_t), "set_les")
 
     def les_coef(self):
