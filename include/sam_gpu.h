@@ -324,7 +324,7 @@ int sam_gpu_ensemble_destroy(void);
  * lengths are 32, 64, 96 or 128 advance together in one persistent launch per
  * RK3 stage (a ticket-ordered queue of (member, pass, tile) work items with
  * bounded dependency waits; no counterpart in the reference, which has no
- * ensembles), with at most ctas_per_sm (1 or 2, the default) CTAs per SM;
+ * ensembles), with at most ctas_per_sm (1, 2 or 3, the default) CTAs per SM;
  * 0 gives every member its own branch of the step graph instead.  The same
  * results either way. */
 int sam_gpu_ensemble_set_persistent(int ctas_per_sm);

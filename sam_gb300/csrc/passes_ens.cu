@@ -69,7 +69,7 @@ __device__ __forceinline__ void ens_pass(int kind, const unsigned char* args, co
   }
 }
 
-__global__ void __launch_bounds__(kThreads, 2)
+__global__ void __launch_bounds__(kThreads, 3)
     k_ens_stage(const EnsSeg* __restrict__ seg, int nseg, int total, const unsigned char* __restrict__ blob,
                 unsigned* counters, int* err) {
   __shared__ int s_tk, s_seg, s_ok;

@@ -228,7 +228,7 @@ struct Ensemble {
   // the persistent stage launches (one per RK3 stage) over the members that
   // qualify (ens_eligible), with at most `persistent` CTAs per SM; the others
   // keep their own branches of the graph (0: every member its own branch)
-  int persistent = 2;
+  int persistent = 3;
   EnsStageLaunch stages[3];
   std::vector<EnsRecorder> recs;
   int* err = nullptr;  // a persistent launch's dependency wait timed out
@@ -902,7 +902,7 @@ int sam_gpu_ensemble_create(const sam_gpu_config* cfgs, int n) {
 
 int sam_gpu_ensemble_set_persistent(int ctas_per_sm) {
   if (!g_ens) return fail(SAM_GPU_ENOTINIT, "no ensemble (sam_gpu_ensemble_create)");
-  if (ctas_per_sm < 0 || ctas_per_sm > 2) return fail(SAM_GPU_EINVAL, "ensemble_set_persistent: 0, 1 or 2");
+  if (ctas_per_sm < 0 || ctas_per_sm > 3) return fail(SAM_GPU_EINVAL, "ensemble_set_persistent: 0 .. 3");
   g_ens->persistent = ctas_per_sm;
   if (g_ens->gexec) { cudaGraphExecDestroy(g_ens->gexec); g_ens->gexec = nullptr; }
   return 0;

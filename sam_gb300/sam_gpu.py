@@ -581,7 +581,7 @@ class SamEnsemble:
             raise SamGpuError(f"ensemble_step failed ({ERRORS.get(rc, rc)}): "
                               + load_library().sam_gpu_error_string().decode(errors="replace"))
 
-    def set_persistent(self, on=True, ctas_per_sm=2):
+    def set_persistent(self, on=True, ctas_per_sm=3):
         """Members that qualify advance in one persistent launch per RK3 stage
         (on; at most ctas_per_sm CTAs per SM) or each in its own branch of the
         step graph (off)."""
