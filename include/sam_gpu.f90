@@ -174,6 +174,10 @@ module sam_gpu
       import :: c_int
       integer(c_int), intent(out) :: out6(6)
     end function
+    integer(c_int) function sam_gpu_set_tiles(in6) bind(C, name="sam_gpu_set_tiles")
+      import :: c_int
+      integer(c_int), intent(in) :: in6(6)
+    end function
     integer(c_int) function sam_gpu_set_fft_schedule(sched5) bind(C, name="sam_gpu_set_fft_schedule")
       import :: c_int
       integer(c_int), intent(in) :: sched5(5)

@@ -171,6 +171,12 @@ int sam_gpu_profile_stage(int nrk, int reps, float* ms5);
  * bit for bit).  Other values are rejected (SAM_GPU_EINVAL). */
 int sam_gpu_autotune(int reps);
 int sam_gpu_tiles(int* out6);
+/* The tiles in out6's order, set by hand instead of by the autotuner
+ * (reproducible tilings); each in 1 .. 64, the x-pass rows even.  A tile
+ * that does not fit a pass's shared memory is shrunk when the pass runs, as
+ * the autotuner's are.  The results do not depend on the tiles beyond the
+ * summation order of the vel_max partial sums. */
+int sam_gpu_set_tiles(const int* in6);
 int sam_gpu_set_fft_schedule(const int* sched5);
 int sam_gpu_fft_schedule(int* out5);
 /* Measurement hook: FP64 FMA throughput of this GPU (TFLOP/s), the ALU

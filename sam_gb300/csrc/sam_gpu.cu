@@ -1805,7 +1805,20 @@ int sam_gpu_fft_schedule(int* out5) {
 
 int sam_gpu_tiles(int* out6) {
   NEED_CTX();
+  if (!out6) return fail(SAM_GPU_EINVAL, "tiles: null array");
   out6[0] = c.ty_zi; out6[1] = c.tx_yi; out6[2] = c.yt_x; out6[3] = c.grp_x; out6[4] = c.tz_yf; out6[5] = c.ty_zf;
+  return 0;
+}
+
+int sam_gpu_set_tiles(const int* in6) {
+  NEED_CTX();
+  if (!in6) return fail(SAM_GPU_EINVAL, "set_tiles: null array");
+  for (int p = 0; p < 6; ++p)
+    if (in6[p] < 1 || in6[p] > 64) return fail(SAM_GPU_EINVAL, "set_tiles: tile %d of entry %d", in6[p], p);
+  if (in6[2] % 2) return fail(SAM_GPU_EINVAL, "set_tiles: x-pass rows %d (row pairs: even)", in6[2]);
+  c.ty_zi = in6[0]; c.tx_yi = in6[1]; c.yt_x = in6[2]; c.grp_x = in6[3]; c.tz_yf = in6[4]; c.ty_zf = in6[5];
+  if (c.gexec) { cudaGraphExecDestroy(c.gexec); c.gexec = nullptr; }
+  c.graph_stale = 1;
   return 0;
 }
 

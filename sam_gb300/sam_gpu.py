@@ -29,7 +29,8 @@ EXPORTS = [
     "sam_gpu_init_random", "sam_gpu_init_packet", "sam_gpu_profile_stage", "sam_gpu_measure_fp64_peak",
     "sam_gpu_vel_max_noalloc", "sam_gpu_filter", "sam_gpu_sm", "sam_gpu_dm", "sam_gpu_get_mean",
     "sam_gpu_force", "sam_gpu_write_field", "sam_gpu_read_field", "sam_gpu_write_header", "sam_gpu_read_header",
-    "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_set_fft_schedule", "sam_gpu_fft_schedule", "sam_gpu_planes",
+    "sam_gpu_autotune", "sam_gpu_tiles", "sam_gpu_set_tiles", "sam_gpu_set_fft_schedule", "sam_gpu_fft_schedule",
+    "sam_gpu_planes",
     "sam_gpu_set_forcing", "sam_gpu_set_les", "sam_gpu_les_coef",
     "sam_gpu_mlp_set", "sam_gpu_mlp_get", "sam_gpu_mlp_forward", "sam_gpu_mlp_grad", "sam_gpu_mlp_train",
     "sam_gpu_mlp_set_backward",
@@ -38,6 +39,7 @@ EXPORTS = [
     "sam_gpu_ensemble_set_persistent", "sam_gpu_ensemble_persistent_members",
 ]
 
+TILE_KEYS = ("z_inv_rows", "y_inv_cols", "x_rows", "x_group", "y_fwd_planes", "z_fwd_rows")
 MLP_PARAMS = 5122
 MLP_FEATURES = 12
 
@@ -117,6 +119,7 @@ def load_library(path: str = LIB_PATH):
     lib.sam_gpu_autotune.argtypes = [C.c_int]
     lib.sam_gpu_tiles.argtypes = [P]
     lib.sam_gpu_set_fft_schedule.argtypes = [P]
+    lib.sam_gpu_set_tiles.argtypes = [P]
     lib.sam_gpu_fft_schedule.argtypes = [P]
     lib.sam_gpu_set_forcing.argtypes = [C.c_ulonglong, C.c_double, C.c_double, C.c_double, C.POINTER(C.c_int)]
     lib.sam_gpu_set_les.argtypes = [C.c_int, C.c_double, C.c_double]
@@ -336,10 +339,26 @@ class SamGpu:
         self._check(load_library().sam_gpu_autotune(reps), "autotune")
         t = np.zeros(6, dtype=np.int32)
         self._check(load_library().sam_gpu_tiles(t.ctypes.data_as(C.c_void_p)), "tiles")
-        out = dict(zip(("z_inv_rows", "y_inv_cols", "x_rows", "x_group", "y_fwd_planes", "z_fwd_rows"),
-                       [int(x) for x in t]))
+        out = dict(zip(TILE_KEYS, [int(x) for x in t]))
         out["fft_schedule"] = self.fft_schedule()
         return out
+
+    def tiles(self):
+        """The tiles in use (the autotuner's or set_tiles')."""
+        t = np.zeros(6, dtype=np.int32)
+        self._check(load_library().sam_gpu_tiles(t.ctypes.data_as(C.c_void_p)), "tiles")
+        return dict(zip(TILE_KEYS, [int(x) for x in t]))
+
+    def set_tiles(self, **tiles):
+        """Set tiles by name (z_inv_rows, y_inv_cols, x_rows, x_group,
+        y_fwd_planes, z_fwd_rows); the others keep their values."""
+        cur = self.tiles()
+        unknown = set(tiles) - set(TILE_KEYS)
+        if unknown:
+            raise ValueError(f"unknown tiles {sorted(unknown)}")
+        cur.update(tiles)
+        t = np.array([cur[k] for k in TILE_KEYS], dtype=np.int32)
+        self._check(load_library().sam_gpu_set_tiles(t.ctypes.data_as(C.c_void_p)), "set_tiles")
 
     def set_fft_schedule(self, sched):
         """FFT schedule of the five passes (z inverse, y inverse, x, y forward,

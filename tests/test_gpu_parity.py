@@ -175,10 +175,12 @@ def test_fft_schedules_agree_in_fp32(gpu_lib):
     dict(ny=40, nz=8, i_strat=1, n_dealias=0),     # no truncation: kx_max = 127
     dict(ny=36, nz=9, i_strat=1, n_dealias=2),
 ])
-def test_fused_fp32_x_pass_bit_identical(gpu_lib, case):
+@pytest.mark.parametrize("x_rows", [2, 4, 8, 16])
+def test_fused_fp32_x_pass_bit_identical(gpu_lib, case, x_rows):
     """The fused FP32 x pass at Nx = 256 (schedule 0) against the 16 x 16 path
     of the general kernel (schedule 2): two CFL steps, bit for bit, with
-    vel_max's max |u| taken in the fused kernel at stage 1."""
+    vel_max's max |u| taken in the fused kernel at stage 1, for every x-pass
+    tile height (1 to 8 row pairs: fewer lines than teams, more, ragged)."""
     cfg = dict(nx=256, i_cfl=1, cfl0=0.5, vis=2e-3, pr=1.0, buoy_fac_z=1.0, lapse=1.0, **case)
     o = O.Oracle(**cfg)
     u = o.init_random(11, 6, 1.0, 6, 0.1)
@@ -188,6 +190,8 @@ def test_fused_fp32_x_pass_bit_identical(gpu_lib, case):
         g = SamGpu(precision=32, **cfg)
         g.set_fft_schedule(sched)
         assert g.fft_schedule() == sched
+        g.set_tiles(x_rows=x_rows)
+        assert g.tiles()["x_rows"] == x_rows
         g.upload(u)
         g.step(2)
         out.append((g.download(), g.stats()["dt"]))
@@ -410,4 +414,19 @@ def test_autotune_leaves_the_state(gpu_lib, prec):
     assert np.array_equal(r0, r1)
     for key, v in s0.items():
         assert np.array_equal(np.asarray(v), np.asarray(s1[key])), key
+    g.close()
+
+
+def test_set_tiles_rejects_bad_tiles(gpu_lib):
+    """sam_gpu_set_tiles: odd x-pass rows and out-of-range tiles are refused
+    and leave the tiles as they were; a valid set reads back."""
+    g = SamGpu(nx=32, ny=32, nz=32, vis=1e-2, dt0=0.01)
+    before = g.tiles()
+    for bad in (dict(x_rows=3), dict(z_inv_rows=0), dict(y_fwd_planes=65)):
+        with pytest.raises(Exception):
+            g.set_tiles(**bad)
+        assert g.tiles() == before
+    g.set_tiles(z_inv_rows=4, x_rows=2, z_fwd_rows=1)
+    t = g.tiles()
+    assert (t["z_inv_rows"], t["x_rows"], t["z_fwd_rows"]) == (4, 2, 1)
     g.close()
