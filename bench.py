@@ -812,7 +812,8 @@ def main():
     ms_step = ms / K
     line = {"metric": METRIC, "value": value, "unit": "steps/s", "n_gpus": ws, "steps": K, "warmup": W,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == 64 else "f32", "data": "synthetic (seeded, generated on the device)",
+            "dtype": {64: "f64", 48: "f32 pairs (double-float)", 32: "f32"}[args.precision],
+            "data": "synthetic (seeded, generated on the device)",
             "config": {"workload": WORKLOAD, "grid": [N, N, N], "fields": 4, "products": 9,
                        "l2": "inputs larger than L2 (state 161 MB, pencils up to 811 MB per pass)",
                        "parallelism": f"replicas x{ws}" if ws > 1 else "1 GPU",
