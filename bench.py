@@ -424,12 +424,14 @@ def ensemble_members(seed=5):
 
 
 def ensemble_form(K, W):
-    """Aggregate member-steps/s of the 96-member ensemble: the 72 members
-    without a closure in one persistent launch per RK3 stage and the 24
-    learned-closure members in their own branches of the same step graph;
-    the same ensemble with every member in its own branch; the members run
-    one after another in the same FP32 forms (the gain from running them
-    together); and one after another in the plain FP64 drop-in."""
+    """Aggregate member-steps/s of the 96-member ensemble: the 64 members
+    without a closure in one persistent launch per RK3 stage and the 32
+    learned-closure members in their own branches of the same step graph
+    (tiles and FFT schedules from the ensemble autotuner, one tuning per
+    member class); the same ensemble with every member in its own branch;
+    the members run one after another in the same FP32 forms and tiles (the
+    gain from running them together); and one after another in the plain
+    FP64 drop-in."""
     import torch
     from sam_gb300 import SamEnsemble, SamGpu
     params, src = closure_params()
@@ -445,6 +447,9 @@ def ensemble_form(K, W):
                 if learned:
                     ens[m].mlp_set(params)
                     ens[m].set_les(3)
+            tuned = ens.autotune(3)  # setup, outside the timed region
+            if persistent:
+                class_tiles.update(tuned)
             ens.step(W)
             npers = ens.persistent_members()
             torch.cuda.synchronize()
@@ -454,6 +459,7 @@ def ensemble_form(K, W):
         finally:
             ens.close()
 
+    class_tiles = {}
     t_ens, npers = timed_ensemble(True)
     t_br, _ = timed_ensemble(False)
 
@@ -466,6 +472,11 @@ def ensemble_form(K, W):
             if closure and learned:
                 g.mlp_set(params)
                 g.set_les(3)
+                t = dict(class_tiles.get((c["nx"], c["ny"], c["nz"], 32, 3), {}))
+                if t:  # the ensemble's tiles for this class
+                    sched = t.pop("fft_schedule")
+                    g.set_tiles(**t)
+                    g.set_fft_schedule(sched)
             g.step(1)
             torch.cuda.synchronize()
             t0 = time.perf_counter()

@@ -559,8 +559,19 @@ class _Member(SamGpu):
                         "ensemble_select")
         return attr
 
+    def set_les(self, model, c_smag=0.01, pr_t=1.0):
+        SamGpu.set_les(self, model, c_smag, pr_t)
+        self._les = model
+
     def close(self):
         pass
+
+
+def _persistent_eligible(cfg, les):
+    """Whether a member runs in the ensemble's persistent launch (the C
+    library's rule: FP32 bulk form, no closure, lengths with a compile-time
+    FFT path)."""
+    return cfg.precision == 32 and les == 0 and all(n in (32, 64, 96, 128) for n in (cfg.nx, cfg.ny, cfg.nz))
 
 
 class SamEnsemble:
@@ -586,6 +597,7 @@ class SamEnsemble:
             raise SamGpuError(f"ensemble_create failed ({ERRORS.get(rc, rc)}): "
                               + lib.sam_gpu_error_string().decode(errors="replace"))
         SamGpu._live = self
+        self._persistent = 3
         self.members = [_Member(self, i, arr[i]) for i in range(len(cfgs))]
 
     def __len__(self):
@@ -607,6 +619,31 @@ class SamEnsemble:
         rc = load_library().sam_gpu_ensemble_set_persistent(ctas_per_sm if on else 0)
         if rc != SAM_GPU_OK:
             raise SamGpuError(f"ensemble_set_persistent failed ({ERRORS.get(rc, rc)})")
+        self._persistent = ctas_per_sm if on else 0
+
+    def autotune(self, reps=3):
+        """The autotuner over the ensemble: for each class of members that run
+        in branches of the step graph (grid, precision, closure model) one
+        member is tuned on its resident state (sam_gpu_autotune) and its tiles
+        and FFT schedules are copied to the others of the class
+        (sam_gpu_set_tiles, sam_gpu_set_fft_schedule).  Members of the
+        persistent launch keep the tiles the launch is sized for.  Call after
+        the members' set-up (closures), before stepping; returns the tiles per
+        class."""
+        done = {}
+        for m in self.members:
+            c, les = m.cfg, getattr(m, "_les", 0)
+            if self._persistent and _persistent_eligible(c, les):
+                continue
+            key = (c.nx, c.ny, c.nz, c.precision, les)
+            if key not in done:
+                done[key] = m.autotune(reps)
+            else:
+                t = dict(done[key])
+                sched = t.pop("fft_schedule")
+                m.set_tiles(**t)
+                m.set_fft_schedule(sched)
+        return done
 
     def persistent_members(self):
         n = C.c_int(0)

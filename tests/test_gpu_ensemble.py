@@ -120,3 +120,51 @@ def test_persistent_stage_launch_equals_single_runs(gpu_lib, persistent):
             assert np.array_equal(got["u_max"], st["u_max"]), m
     finally:
         ens.close()
+
+
+def test_ensemble_autotune_per_class(gpu_lib):
+    """SamEnsemble.autotune tunes one member per class of branch members and
+    copies its tiles and FFT schedules to the rest of the class; members of
+    the persistent launch keep their tiles; each member then steps exactly
+    as its own run with the same tiles."""
+    params = CL.init_params(4)
+    les_cfg = dict(nx=32, ny=32, nz=32, i_strat=1, buoy_fac_z=1.0, lapse=1.0, vis=2e-3, i_cfl=1, cfl0=0.5,
+                   precision=32)
+    small = dict(nx=32, ny=32, nz=32, vis=1e-2, i_cfl=1, cfl0=0.5, precision=32)
+    cfgs = [les_cfg, les_cfg, small]
+    starts = []
+    for c in cfgs:
+        c0 = dict(c)
+        c0.pop("precision")
+        starts.append(O.Oracle(**c0).init_random(len(starts) + 21, 0, 1.0, 0, 0.1))
+    ens = SamEnsemble(cfgs)
+    try:
+        defaults = ens[2].tiles()
+        for m in range(3):
+            ens[m].upload(starts[m])
+        for m in (0, 1):
+            ens[m].mlp_set(params)
+            ens[m].set_les(3)
+        tuned = ens.autotune(2)
+        assert list(tuned) == [(32, 32, 32, 32, 3)]
+        t0 = dict(tuned[(32, 32, 32, 32, 3)])
+        sched = t0.pop("fft_schedule")
+        assert ens[1].tiles() == t0 and ens[1].fft_schedule() == sched
+        assert ens[2].tiles() == defaults
+        ens.step(2)
+        assert ens.persistent_members() == 1
+        out = [(ens[m].download(), ens[m].stats()["dt"]) for m in range(3)]
+    finally:
+        ens.close()
+    for m in range(3):
+        g = SamGpu(**cfgs[m])
+        g.upload(starts[m])
+        if m < 2:
+            g.mlp_set(params)
+            g.set_les(3)
+            g.set_tiles(**t0)
+            g.set_fft_schedule(sched)
+        g.step(2)
+        assert np.array_equal(g.download(), out[m][0]), m
+        assert g.stats()["dt"] == out[m][1]
+        g.close()
