@@ -621,19 +621,21 @@ class SamEnsemble:
             raise SamGpuError(f"ensemble_set_persistent failed ({ERRORS.get(rc, rc)})")
         self._persistent = ctas_per_sm if on else 0
 
-    def autotune(self, reps=3):
+    def autotune(self, reps=3, persistent_members=False):
         """The autotuner over the ensemble: for each class of members that run
         in branches of the step graph (grid, precision, closure model) one
         member is tuned on its resident state (sam_gpu_autotune) and its tiles
         and FFT schedules are copied to the others of the class
         (sam_gpu_set_tiles, sam_gpu_set_fft_schedule).  Members of the
-        persistent launch keep the tiles the launch is sized for.  Call after
-        the members' set-up (closures), before stepping; returns the tiles per
-        class."""
+        persistent launch keep the tiles the launch is sized for unless
+        persistent_members is set (tiles tuned on a member's own kernels are
+        larger than the persistent launch favours: 4479 -> 4391 member-steps/s
+        on the 96-member benchmark ensemble).  Call after the members' set-up
+        (closures), before stepping; returns the tiles per class."""
         done = {}
         for m in self.members:
             c, les = m.cfg, getattr(m, "_les", 0)
-            if self._persistent and _persistent_eligible(c, les):
+            if self._persistent and _persistent_eligible(c, les) and not persistent_members:
                 continue
             key = (c.nx, c.ny, c.nz, c.precision, les)
             if key not in done:
