@@ -170,3 +170,30 @@ def test_learned_closure_step_matches_oracle(gpu_lib, precision, tol):
     ug = g.download()
     for n in range(o.d.lu):
         assert _relerr(ug[..., n], u[..., n]) <= tol, n
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_learned_coefficients_kept_across_stages(gpu_lib, precision):
+    """The learned closure's coefficients are formed at stage 1 and kept by
+    stages 2 and 3: three separate stage calls give the step's fields bit
+    for bit."""
+    import oracle as O
+    p = CL.init_params(5)
+    p[CL.OFF_W3:CL.OFF_B3] *= 10
+    o = O.Oracle(**CFG3)
+    u = o.init_random(3, 0, 1.0, 0, 0.1)
+    o.close()
+    out = []
+    for mode in ("step", "stages"):
+        g = SamGpu(precision=precision, **CFG3)
+        g.upload(u)
+        g.mlp_set(p)
+        g.set_les(3, pr_t=1.0)
+        if mode == "step":
+            g.step(1)
+        else:
+            for nrk in (1, 2, 3):
+                g.stage(nrk)
+        out.append(g.download())
+        g.close()
+    assert np.array_equal(out[0], out[1])
