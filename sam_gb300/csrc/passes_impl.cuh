@@ -39,8 +39,9 @@ constexpr int kBatch = 8;
 
 // Resident CTAs per SM each kernel's register budget is sized for (measured
 // at 256^3): in FP32 the transpose passes of the 16 x 16 register path fit
-// 64 registers (four CTAs) and the x pass 72 (three CTAs of 288 threads)
-// without spills; the compile-time Stockham transposes (lengths 32-512)
+// 64 registers (four CTAs; the y inverse 48 with five, 5 % faster; the y
+// forward at six measured 12 % slower) and the x pass 72 (three CTAs of 288
+// threads) without spills; the compile-time Stockham transposes (lengths 32-512)
 // spilled 40-110 bytes at 64 and keep three CTAs (80 registers; 128^3 y
 // forward 10 % faster); the FP32 z_fwd epilogue spills below 128 and keeps
 // two (three measured slower); FP64 CTAs are bound by the FP64 pipe.
@@ -49,7 +50,7 @@ constexpr int kBatch = 8;
 enum PassKind { kPassZInv, kPassYInv, kPassX, kPassYFwd, kPassZFwd };
 template <typename T, int K, int PATH = kFft256> struct MinBlocks {
   static constexpr int value =
-      PATH == kFftGeneric ? (K == kPassX ? 1 : 2) : (K == kPassZFwd ? 2 : (K == kPassX ? 3 : (PATH == kFft256 ? 4 : 3)));
+      PATH == kFftGeneric ? (K == kPassX ? 1 : 2) : (K == kPassZFwd ? 2 : (K == kPassX ? 3 : (PATH == kFft256 ? (K == kPassYInv ? 5 : 4) : 3)));
 };
 template <int K, int PATH> struct MinBlocks<double, K, PATH> {
   static constexpr int value = PATH == kFftGeneric ? 1 : 2;
