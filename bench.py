@@ -157,7 +157,10 @@ def measured_peaks():
 
 
 def profile_traffic(name="x_pass_traffic.json"):
-    """DRAM traffic per x-pass launch from the committed ncu summary, if any."""
+    """DRAM traffic per x-pass launch from the committed ncu summary, if any;
+    the summaries cover the 256^3 workload, so other grids get none."""
+    if N != 256:
+        return None
     try:
         return json.load(open(os.path.join(ROOT, "profiles", name)))
     except (OSError, ValueError):
@@ -807,11 +810,13 @@ def main():
         xb32 = x_pass_bytes(w=4)
         a32 = xb32 / (x32_ms / 1e3) / 1e9
         tr32 = profile_traffic("x_pass_fp32_traffic.json")
-        fp32["roofline"] = {"bound": "hbm", "kernel": "k_x_pass_f256 (C2R, 9 products, R2C; stages 2 and 3)",
+        xk = "k_x_pass_f256" if N == 256 else "k_x_pass<float>"
+        fp32["roofline"] = {"bound": "hbm", "kernel": xk + " (C2R, 9 products, R2C; stages 2 and 3)",
                             "achieved": a32, "peak": hbm_peak, "unit": "GB/s", "frac": a32 / hbm_peak,
                             "traffic": tr32.get("bytes_per_launch") if tr32 else None,
                             "algorithmic_bytes_per_launch": xb32, "ms": x32_ms,
-                            "note": "bound by shared-memory traffic and latency: counters in profiles/x_pass_f256_fp32_256_ncu.md"}
+                            "note": "bound by shared-memory traffic and latency: counters at 256^3 in "
+                                    "profiles/x_pass_f256_fp32_256_ncu.md"}
     if ddf is not None:
         xd_ms = ddf.pop("_x_ms")
         ad = x_pass_bytes(w=8) / (xd_ms / 1e3) / 1e9
